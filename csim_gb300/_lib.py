@@ -1,0 +1,118 @@
+"""ctypes binding of libcsimgpu.so (the C ABI declared in include/csimgpu.h).
+
+The library is the only compute path: importing this module fails loudly if
+the shared object is missing, and every call raises CsgError on a non-zero
+status. There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcsimgpu.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "csimgpu.h")
+
+P = C.c_void_p
+I = C.c_int
+D = C.c_double
+SZ = C.c_size_t
+U64 = C.c_uint64
+
+CSG_LAYOUT_COLMAJOR = 0
+CSG_LAYOUT_ROWMAJOR = 1
+CSG_PREC_BF16X6 = 6
+CSG_PREC_BF16X3 = 3
+
+STATUS = {0: "CSG_OK", -1: "CSG_E_ARG", -2: "CSG_E_SHAPE", -3: "CSG_E_CUDA", -4: "CSG_E_TIMEOUT",
+          -5: "CSG_E_NOMEM", -6: "CSG_E_NAN", -7: "CSG_E_STATE"}
+
+
+class CsgError(RuntimeError):
+    def __init__(self, code: int, fn: str, msg: str):
+        super().__init__(f"{fn}: {STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+# name -> (argtypes, restype); restype None means "int status"
+SIGNATURES = {
+    "csg_create": ([C.POINTER(P), I], None),
+    "csg_destroy": ([P], None),
+    "csg_last_error": ([], C.c_char_p),
+    "csg_sync": ([P], None),
+    "csg_set_stream": ([P, P], None),
+    "csg_get_stream": ([P], P),
+    "csg_alloc": ([P, SZ, C.POINTER(P)], None),
+    "csg_free": ([P, P], None),
+    "csg_memcpy_h2d": ([P, P, P, SZ], None),
+    "csg_memcpy_d2h": ([P, P, P, SZ], None),
+    "csg_memset": ([P, P, I, SZ], None),
+    "csg_version": ([], C.c_char_p),
+    "csg_field_upload": ([P, P, I, I, I, I, P, P], None),
+    "csg_field_download": ([P, P, I, I, I, P, P, I], None),
+    "csg_point_source": ([P, P, I, I, I, D, D, P, P, P], None),
+    "csg_mask_real": ([P, P, I, I, I, P, I], None),
+    "csg_phase_screen": ([P, P, I, I, I, P, P, D], None),
+    "csg_complex_mask": ([P, P, I, I, I, P, P, I, I], None),
+    "csg_fft2d": ([P, P, I, I, I], None),
+    "csg_fresnel": ([P, P, I, I, P, D, D], None),
+    "csg_mft_create": ([P, C.POINTER(P), I, I, I, I, P, P, P, P, I, P, P, D, I], None),
+    "csg_mft_destroy": ([P], None),
+    "csg_mft_execute": ([P, P, P, P, I, P, I, P, P], None),
+    "csg_mft_workspace_bytes": ([P, I], SZ),
+    "csg_hex_mask": ([P, P, P, I, I, P, I, I, P, P, D, I, D, I, P], None),
+    "csg_hex_tables": ([P, P, P, I, I, I, D, D, I, I, D, D, P, P], None),
+    "csg_region_reduce": ([P, P, I, I, I, I, P, I, I, D, P], None),
+    "csg_intensity": ([P, P, I, I, I, P, P], None),
+    "csg_respobj_create": ([P, C.POINTER(P), P, I, I, I, P, D, D, I], None),
+    "csg_respobj_destroy": ([P], None),
+    "csg_respobj_execute": ([P, P, I, P], None),
+    "csg_de_mutate": ([P, P, P, I, I, I, D, D, P, P, U64, U64, P, P], None),
+    "csg_de_select": ([P, P, P, P, P, I, I], None),
+}
+
+
+def header_symbols() -> list[str]:
+    """Every function the public header declares."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(csg_\w+)\s*\(", txt, re.M)))
+
+
+def _load() -> C.CDLL:
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with csim_gb300.build.build() "
+                          "(there is no CPU fallback)")
+    return C.CDLL(LIB_PATH)
+
+
+lib = _load()
+
+
+class _Fn:
+    def __init__(self, name: str, argtypes, restype):
+        self.name = name
+        self.fn = getattr(lib, name)
+        self.fn.argtypes = argtypes
+        self.status = restype is None
+        self.fn.restype = I if restype is None else restype
+
+    def __call__(self, *args):
+        r = self.fn(*args)
+        if self.status and r != 0:
+            msg = lib.csg_last_error()
+            raise CsgError(r, self.name, msg.decode() if msg else "")
+        return r
+
+
+lib.csg_last_error.restype = C.c_char_p
+lib.csg_last_error.argtypes = []
+api = {name: _Fn(name, a, r) for name, (a, r) in SIGNATURES.items() if hasattr(lib, name)}
+
+
+def call(name: str, *args):
+    return api[name](*args)
+
+
+def version() -> str:
+    return api["csg_version"]().decode()

@@ -1,0 +1,335 @@
+// Matrix Fourier transform (the reference's zoomFft / chirp-Z zoom) on
+// tcgen05 tensor cores.
+//
+//   out = pref * A_y . in . B_x^T,  A_y[v][y] = e^{sgn 2 pi i yin_y yout_v / lf},
+//                                  B_x[u][x] = e^{sgn 2 pi i xin_x xout_u / lf}
+//
+// Stage 1 contracts x: T[y][u] = sum_x in[y][x] B_x[u][x]; the epilogue writes
+// T transposed and already split into three bf16 parts.
+// Stage 2 contracts y: out[v][u] = sum_y (pref A_y)[v][y] T^T[u][y] in fp32.
+// Operators are generated once per plan in FP64 (phase reduced in turns) and
+// stored split as [slot][part][sel: re, im, -im][rows][K] bf16.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+#include <vector>
+
+#include "ctx.hpp"
+#include "tc_gemm.cuh"
+
+namespace csg {
+
+// ------------------------------------------------------------ tensor maps
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static int get_encoder() {
+  static std::once_flag once;
+  static int rc = CSG_OK;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+      rc = CSG_E_CUDA;
+    } else {
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+  });
+  if (rc != CSG_OK) set_error("cuTensorMapEncodeTiled entry point unavailable");
+  return rc;
+}
+
+// 3-D bf16 map: (k inner, rows, planes), box (64, box_rows, 1), 128B swizzle.
+static int make_map(CUtensorMap* m, const void* base, int k, int rows, long long planes,
+                    int box_rows) {
+  int rc = get_encoder();
+  if (rc) return rc;
+  CSG_CHECK(((uintptr_t)base & 15) == 0, CSG_E_ARG, "TMA base not 16-byte aligned");
+  CSG_CHECK((k % 8) == 0, CSG_E_SHAPE, "TMA inner extent must be a multiple of 8 elements");
+  cuuint64_t dims[3] = {(cuuint64_t)k, (cuuint64_t)rows, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)k * 2, (cuuint64_t)k * 2 * rows};
+  cuuint32_t box[3] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CSG_CHECK(r == CUDA_SUCCESS, CSG_E_CUDA,
+            "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return CSG_OK;
+}
+
+// ------------------------------------------------------------ kernels
+// Operator generator: op[slot][part][sel][r][k] for r < rows, k < K.
+// value = pref_s * exp(sgn 2 pi i frac(cout_r cin_k / lf_s)); sel 0/1/2 = re/im/-im.
+__global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* __restrict__ cout,
+                                 const double* __restrict__ cin, int rows, int K, int n_slots,
+                                 const double* __restrict__ lf, const double* __restrict__ pref,
+                                 double sgn) {
+  const long long n = (long long)n_slots * rows * K;
+  const long long plane = (long long)rows * K;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(i % K);
+    const long long t = i / K;
+    const int r = (int)(t % rows);
+    const int s = (int)(t / rows);
+    double turns = cout[r] * cin[k] / lf[s];
+    turns -= rint(turns);  // exact in FP64 for |turns| < 2^52
+    double sn, cs;
+    sincospi(2.0 * sgn * turns, &sn, &cs);
+    double pr = 1.0, pi = 0.0;
+    if (pref) {
+      pr = pref[2 * s];
+      pi = pref[2 * s + 1];
+    }
+    const double re = pr * cs - pi * sn;
+    const double im = pr * sn + pi * cs;
+    __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+    split3((float)re, a0, a1, a2);
+    split3((float)im, b0, b1, b2);
+    const long long off = (long long)r * K + k;
+    const __nv_bfloat16 pre[3] = {a0, a1, a2};
+    const __nv_bfloat16 pim[3] = {b0, b1, b2};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      __nv_bfloat16* base = op + ((long long)(s * 3 + q) * 3) * plane + off;
+      base[0] = pre[q];
+      base[plane] = pim[q];
+      base[2 * plane] = __hneg(pim[q]);
+    }
+  }
+}
+
+// Data split: planar fp32 [F][2][R][C] (optionally times a complex multiplier
+// [n_mul][2][R][C] chosen by mul_idx[f]) -> bf16 [F][3][2][R][C].
+__global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int R,
+                              int C, int F, const float* __restrict__ mul,
+                              const int* __restrict__ mul_idx) {
+  const long long plane = (long long)R * C;
+  const long long n = plane * F;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(i / plane);
+    const long long o = i % plane;
+    float re = in[(long long)f * 2 * plane + o];
+    float im = in[(long long)f * 2 * plane + plane + o];
+    if (mul) {
+      const long long mb = (long long)mul_idx[f] * 2 * plane;
+      const float mr = mul[mb + o], mi = mul[mb + plane + o];
+      const float tr = re * mr - im * mi;
+      im = re * mi + im * mr;
+      re = tr;
+    }
+    __nv_bfloat16 a[3], b[3];
+    split3(re, a[0], a[1], a[2]);
+    split3(im, b[0], b[1], b[2]);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      out[((long long)(f * 3 + q) * 2 + 0) * plane + o] = a[q];
+      out[((long long)(f * 3 + q) * 2 + 1) * plane + o] = b[q];
+    }
+  }
+}
+
+// Product terms of the three-way split, largest first.
+static void terms_for(int precision, tc::Params& p) {
+  static const int a6[6] = {0, 0, 1, 0, 1, 2};
+  static const int b6[6] = {0, 1, 0, 2, 1, 0};
+  p.n_terms = precision == CSG_PREC_BF16X3 ? 3 : 6;
+  for (int i = 0; i < p.n_terms; ++i) {
+    p.term_a[i] = a6[i];
+    p.term_b[i] = b6[i];
+  }
+}
+
+template <int BN, bool OP_IS_A, int EPI>
+static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Params& p,
+                       int grid, cudaStream_t st) {
+  auto kern = tc::k_split_gemm<BN, OP_IS_A, EPI>;
+  constexpr size_t smem = tc::smem_bytes<BN>();
+  static bool attr_set = false;  // per template instance
+  if (!attr_set) {
+    CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  kern<<<grid, tc::THREADS, smem, st>>>(a, b, p);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
+}  // namespace csg
+
+using namespace csg;
+
+struct csg_mft {
+  csg_ctx* ctx = nullptr;
+  int ny = 0, nx = 0, mo = 0, no = 0, n_slots = 0, precision = 6;
+  __nv_bfloat16* op1 = nullptr;  // [slot][3][3][no][nx]
+  __nv_bfloat16* op2 = nullptr;  // [slot][3][3][mo][ny]
+  Scratch split_in;               // [F][3][2][ny][nx] bf16
+  Scratch tt;                     // [F][3][2][no][ny] bf16
+};
+
+extern "C" {
+
+int csg_mft_create(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_out_y,
+                   int n_out_x, const double* yin, const double* xin, const double* yout,
+                   const double* xout, int n_slots, const double* lf, const double* pref,
+                   double sgn, int precision) {
+  CSG_CHECK(ctx && plan && yin && xin && yout && xout && lf, CSG_E_ARG,
+            "csg_mft_create: null argument");
+  CSG_CHECK(n_in_y > 0 && n_in_x > 0 && n_out_y > 0 && n_out_x > 0 && n_slots > 0, CSG_E_SHAPE,
+            "csg_mft_create: non-positive size");
+  CSG_CHECK(n_in_x % 8 == 0 && n_in_y % 8 == 0, CSG_E_SHAPE,
+            "csg_mft_create: input sizes must be multiples of 8");
+  CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3, CSG_E_ARG,
+            "csg_mft_create: precision must be CSG_PREC_BF16X6 or CSG_PREC_BF16X3");
+  for (int s = 0; s < n_slots; ++s)
+    CSG_CHECK(lf[s] != 0.0, CSG_E_ARG, "csg_mft_create: zero lambda*f");
+  DeviceGuard g(ctx->device);
+  csg_mft* m = new csg_mft();
+  m->ctx = ctx;
+  m->ny = n_in_y;
+  m->nx = n_in_x;
+  m->mo = n_out_y;
+  m->no = n_out_x;
+  m->n_slots = n_slots;
+  m->precision = precision;
+  const size_t op1_elems = (size_t)n_slots * 9 * n_out_x * n_in_x;
+  const size_t op2_elems = (size_t)n_slots * 9 * n_out_y * n_in_y;
+  double* dvec = nullptr;
+  const size_t nvec = (size_t)n_in_y + n_in_x + n_out_y + n_out_x + 3 * n_slots;
+  if (cudaMalloc(&m->op1, op1_elems * 2) != cudaSuccess ||
+      cudaMalloc(&m->op2, op2_elems * 2) != cudaSuccess ||
+      cudaMalloc(&dvec, nvec * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(m->op1);
+    cudaFree(m->op2);
+    cudaFree(dvec);
+    delete m;
+    set_error("csg_mft_create: operator allocation failed");
+    return CSG_E_NOMEM;
+  }
+  std::vector<double> h(nvec, 0.0);
+  size_t o = 0;
+  const size_t o_yin = o; for (int i = 0; i < n_in_y; ++i) h[o++] = yin[i];
+  const size_t o_xin = o; for (int i = 0; i < n_in_x; ++i) h[o++] = xin[i];
+  const size_t o_yout = o; for (int i = 0; i < n_out_y; ++i) h[o++] = yout[i];
+  const size_t o_xout = o; for (int i = 0; i < n_out_x; ++i) h[o++] = xout[i];
+  const size_t o_lf = o; for (int i = 0; i < n_slots; ++i) h[o++] = lf[i];
+  const size_t o_pref = o;
+  for (int i = 0; i < n_slots; ++i) {
+    h[o++] = pref ? pref[2 * i] : 1.0;
+    h[o++] = pref ? pref[2 * i + 1] : 0.0;
+  }
+  cudaStream_t st = ctx->stream;
+  CSG_CUDA(cudaMemcpyAsync(dvec, h.data(), nvec * sizeof(double), cudaMemcpyHostToDevice, st));
+  // stage-1 operator: rows u (xout), K = x (xin), no prefactor
+  k_build_operator<<<grid_for((long long)n_slots * n_out_x * n_in_x, 256), 256, 0, st>>>(
+      m->op1, dvec + o_xout, dvec + o_xin, n_out_x, n_in_x, n_slots, dvec + o_lf, nullptr, sgn);
+  CSG_LAUNCH_CHECK();
+  // stage-2 operator: rows v (yout), K = y (yin), carries the prefactor
+  k_build_operator<<<grid_for((long long)n_slots * n_out_y * n_in_y, 256), 256, 0, st>>>(
+      m->op2, dvec + o_yout, dvec + o_yin, n_out_y, n_in_y, n_slots, dvec + o_lf,
+      dvec + o_pref, sgn);
+  CSG_LAUNCH_CHECK();
+  CSG_CUDA(cudaStreamSynchronize(st));
+  cudaFree(dvec);
+  *plan = m;
+  return CSG_OK;
+}
+
+int csg_mft_destroy(csg_mft* m) {
+  if (!m) return CSG_OK;
+  DeviceGuard g(m->ctx->device);
+  cudaStreamSynchronize(m->ctx->stream);
+  cudaFree(m->op1);
+  cudaFree(m->op2);
+  m->split_in.release();
+  m->tt.release();
+  delete m;
+  return CSG_OK;
+}
+
+size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
+  if (!m) return 0;
+  return (size_t)n_fields * 12 * ((size_t)m->ny * m->nx + (size_t)m->no * m->ny);
+}
+
+int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
+                    const int* slot, int accumulate, const float* in_mul, const int* mul_idx) {
+  CSG_CHECK(ctx && m && in && out && slot, CSG_E_ARG, "csg_mft_execute: null argument");
+  CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_mft_execute: n_fields must be positive");
+  CSG_CHECK(!in_mul || mul_idx, CSG_E_ARG, "csg_mft_execute: in_mul needs mul_idx");
+  DeviceGuard g(ctx->device);
+  cudaStream_t st = ctx->stream;
+  int rc;
+  if ((rc = m->split_in.ensure((size_t)n_fields * 12 * m->ny * m->nx))) return rc;
+  if ((rc = m->tt.ensure((size_t)n_fields * 12 * m->no * m->ny))) return rc;
+  auto* sin = static_cast<__nv_bfloat16*>(m->split_in.ptr);
+  auto* tt = static_cast<__nv_bfloat16*>(m->tt.ptr);
+
+  k_split_field<<<grid_for((long long)n_fields * m->ny * m->nx, 256), 256, 0, st>>>(
+      in, sin, m->ny, m->nx, n_fields, in_mul, mul_idx);
+  CSG_LAUNCH_CHECK();
+
+  const int bn1 = m->no >= 256 ? 256 : 128;
+  // ---- stage 1: T^T = split(in . B_x^T)^T
+  {
+    CUtensorMap ta, tb;
+    if ((rc = make_map(&ta, sin, m->nx, m->ny, (long long)n_fields * 6, tc::BM))) return rc;
+    if ((rc = make_map(&tb, m->op1, m->nx, m->no, (long long)m->n_slots * 9, bn1))) return rc;
+    tc::Params p{};
+    p.n_fields = n_fields;
+    p.m_tiles = (m->ny + tc::BM - 1) / tc::BM;
+    p.n_half = (m->no + bn1 - 1) / bn1;
+    p.n_tiles = 2 * p.n_half;
+    p.m_half = p.m_tiles;
+    p.rows_valid = m->ny;
+    p.cols_valid = m->no;
+    p.k_blocks = (m->nx + tc::BK - 1) / tc::BK;
+    terms_for(m->precision, p);
+    p.slot = slot;
+    p.out = tt;
+    p.out_rows = m->no;
+    p.out_cols = m->ny;
+    p.accumulate = 0;
+    p.status = ctx->status;
+    const int grid = n_fields * p.m_tiles * p.n_tiles;
+    rc = bn1 == 256 ? launch_gemm<256, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
+                    : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
+    if (rc) return rc;
+  }
+  // ---- stage 2: out = (pref A_y) . T
+  {
+    CUtensorMap ta, tb;
+    if ((rc = make_map(&ta, m->op2, m->ny, m->mo, (long long)m->n_slots * 9, tc::BM))) return rc;
+    if ((rc = make_map(&tb, tt, m->ny, m->no, (long long)n_fields * 6, bn1))) return rc;
+    tc::Params p{};
+    p.n_fields = n_fields;
+    p.m_half = (m->mo + tc::BM - 1) / tc::BM;
+    p.m_tiles = 2 * p.m_half;
+    p.n_tiles = (m->no + bn1 - 1) / bn1;
+    p.n_half = p.n_tiles;
+    p.rows_valid = m->mo;
+    p.cols_valid = m->no;
+    p.k_blocks = (m->ny + tc::BK - 1) / tc::BK;
+    terms_for(m->precision, p);
+    p.slot = slot;
+    p.out = out;
+    p.out_rows = m->mo;
+    p.out_cols = m->no;
+    p.accumulate = accumulate;
+    p.status = ctx->status;
+    const int grid = n_fields * p.m_tiles * p.n_tiles;
+    rc = bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st)
+                    : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st);
+    if (rc) return rc;
+  }
+  return CSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,372 @@
+// tcgen05 split-bf16 GEMM for the matrix Fourier transforms.
+//
+// One launch computes, for a batch of fields, the real-ified complex product
+//   C = sum_{terms (pa,pb)} sum_{comp c} A[pa, sel] * B[pb, sel]^T
+// with both operands K-major bf16 tiles staged by TMA (128B swizzle) into a
+// 4-deep shared-memory ring, accumulated in fp32 in tensor memory by a single
+// issuing thread (tcgen05.mma.cta_group::1.kind::f16, M = 128, N = BN,
+// K = 16 per instruction) and drained by four epilogue warps with
+// tcgen05.ld.32x32b.
+//
+// Operand roles: one operand is a field ("data", indexed by field and split
+// part) and the other an MFT operator ("op", indexed by the field's slot and
+// split part). Complex arithmetic is real-ified: each tile produces one
+// output component d (re or im), and each K segment pairs data component c
+// with operator plane sel(d, c) in {re, im, -im}:
+//   (d,c) = (re,re): re   (re,im): -im   (im,re): im   (im,im): re
+#pragma once
+#include <cuda.h>
+#include "common.cuh"
+
+namespace csg {
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int BK = 64;  // bf16 elements per 128-byte swizzled row
+constexpr int STAGES = 4;
+constexpr int THREADS = 128;
+
+enum Epi { EPI_T_SPLIT = 0, EPI_F32 = 1 };
+
+struct Params {
+  int n_fields;
+  int m_tiles;      // tiles along M (stage 2 counts both components)
+  int n_tiles;      // tiles along N (stage 1 counts both components)
+  int m_half;       // stage 2: tiles per component along M
+  int n_half;       // stage 1: tiles per component along N
+  int rows_valid;   // stage 1: Ny (data rows); stage 2: Mo (operator rows per comp)
+  int cols_valid;   // No (valid output columns)
+  int k_blocks;     // ceil(K / BK)
+  int n_terms;
+  int term_a[8];
+  int term_b[8];
+  const int* slot;  // [n_fields] operator slot of each field
+  void* out;
+  int out_rows;     // EPI_T_SPLIT: No (rows of T^T); EPI_F32: Mo
+  int out_cols;     // EPI_T_SPLIT: Ny; EPI_F32: No
+  int accumulate;   // EPI_F32 only
+  int* status;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ uint32_t mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok;
+}
+
+// Bounded wait: false once the cycle budget is spent.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  if (mbar_try_wait(a, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(a, parity)) {
+    if (clock64() - t0 > kWaitBudgetCycles) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, uint64_t* bar,
+                                            int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// K-major, 128-byte swizzle, 8-row atoms of 1024 bytes stacked along M/N.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;                 // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset: next 8-row atom
+  d |= (uint64_t)1 << 46;                 // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+  return d;
+}
+
+// kind::f16 instruction descriptor: bf16 x bf16 -> f32, both K-major.
+__host__ __device__ constexpr uint32_t instr_desc(int m, int n) {
+  return (1u << 4)                 // D format f32
+         | (1u << 7)               // A format bf16
+         | (1u << 10)              // B format bf16
+         | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                     uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ int sel_plane(int d, int c) {
+  // (re,re)->0 re, (re,im)->2 -im, (im,re)->1 im, (im,im)->0 re
+  return d == 0 ? (c == 0 ? 0 : 2) : (c == 0 ? 1 : 0);
+}
+
+// Dynamic shared memory: STAGES x (A tile + B tile), 1024-byte aligned, then
+// barriers and the TMEM base address.
+template <int BN>
+constexpr size_t smem_bytes() {
+  return (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 1024 /*align*/ + 256 /*barriers*/;
+}
+
+// OP_IS_A = false: stage 1 (A = data rows y, B = operator rows u, d from N tile)
+// OP_IS_A = true : stage 2 (A = operator rows v, B = data rows u, d from M tile)
+template <int BN, bool OP_IS_A, int EPI>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                 const Params p) {
+  extern __shared__ uint8_t smem_raw[];
+  constexpr uint32_t A_BYTES = BM * BK * 2;
+  constexpr uint32_t B_BYTES = BN * BK * 2;
+  constexpr uint32_t TMEM_COLS = BN;  // fp32 accumulator columns (power of 2 >= 32)
+
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
+  uint8_t* sA = sbase;
+  uint8_t* sB = sbase + STAGES * A_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + STAGES * B_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  // tile decode: n fastest, then m, then field
+  int t = blockIdx.x;
+  const int nt = t % p.n_tiles;
+  t /= p.n_tiles;
+  const int mt = t % p.m_tiles;
+  const int field = t / p.m_tiles;
+  if (field >= p.n_fields) return;
+  const int slot = p.slot[field];
+
+  int d, row_a0, row_b0;
+  if (!OP_IS_A) {
+    d = nt / p.n_half;
+    row_a0 = mt * BM;                    // data rows (y)
+    row_b0 = (nt % p.n_half) * BN;       // operator rows (u)
+  } else {
+    d = mt / p.m_half;
+    row_a0 = (mt % p.m_half) * BM;       // operator rows (v)
+    row_b0 = nt * BN;                    // data rows (u)
+  }
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accum, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const int k_iters = p.n_terms * 2 * p.k_blocks;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    int stage = 0;
+    uint32_t phase = 0;
+    for (int it = 0; it < k_iters; ++it) {
+      if (it >= STAGES) {
+        if (!mbar_wait(&empty[stage], phase ^ 1)) {
+          atomicExch(p.status, 1);
+          *abort_flag = 1;
+          break;
+        }
+      }
+      if (*abort_flag) break;
+      const int kb = it % p.k_blocks;
+      const int c = (it / p.k_blocks) & 1;
+      const int term = it / (2 * p.k_blocks);
+      const int pa = p.term_a[term], pb = p.term_b[term];
+      int za, zb;
+      if (!OP_IS_A) {
+        za = (field * 3 + pa) * 2 + c;
+        zb = (slot * 3 + pb) * 3 + sel_plane(d, c);
+      } else {
+        za = (slot * 3 + pa) * 3 + sel_plane(d, c);
+        zb = (field * 3 + pb) * 2 + c;
+      }
+      mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
+      tma_load_3d(sA + stage * A_BYTES, &tmA, &full[stage], kb * BK, row_a0, za);
+      tma_load_3d(sB + stage * B_BYTES, &tmB, &full[stage], kb * BK, row_b0, zb);
+      if (++stage == STAGES) {
+        stage = 0;
+        phase ^= 1;
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    constexpr uint32_t idesc = instr_desc(BM, BN);
+    int stage = 0;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int it = 0; it < k_iters; ++it) {
+      if (!mbar_wait(&full[stage], phase)) {
+        atomicExch(p.status, 2);
+        *abort_flag = 1;
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(sA + stage * A_BYTES);
+      const uint32_t b0 = smem_u32(sB + stage * B_BYTES);
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k) {
+        umma(tmem, smem_desc(a0 + k * 32), smem_desc(b0 + k * 32), idesc,
+             (it > 0 || k > 0) ? 1u : 0u);
+      }
+      umma_commit(&empty[stage]);
+      if (++stage == STAGES) {
+        stage = 0;
+        phase ^= 1;
+      }
+    }
+    // signal the epilogue (also on abort, so nobody waits forever)
+    if (ok) umma_commit(accum);
+    else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(accum)) : "memory");
+  }
+  __syncwarp();
+
+  // ---------------- epilogue: all four warps
+  bool ready = mbar_wait(accum, 0);
+  if (!ready) atomicExch(p.status, 3);
+  tc_fence_after();
+  const int row = warp * 32 + lane;  // tile row held by this thread
+  // tcgen05.ld is warp-collective: decide per warp
+  ready = __all_sync(0xffffffffu, ready && !*abort_flag);
+  if (ready) {
+    for (int cb = 0; cb < BN; cb += 32) {
+      uint32_t r[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb, r);
+      if (EPI == EPI_T_SPLIT) {
+        // C[y][u] -> T^T parts [field][part][d][u][y] (bf16), y = row
+        const int y = row_a0 + row;
+        const int u0 = row_b0 + cb;
+        if (y < p.out_cols) {
+          __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+          const size_t plane = (size_t)p.out_rows * p.out_cols;
+#pragma unroll 4
+          for (int j = 0; j < 32; ++j) {
+            const int u = u0 + j;
+            if (u < p.cols_valid) {
+              __nv_bfloat16 h0, h1, h2;
+              split3(__uint_as_float(r[j]), h0, h1, h2);
+              const size_t off = (size_t)u * p.out_cols + y;
+              out[((size_t)(field * 3 + 0) * 2 + d) * plane + off] = h0;
+              out[((size_t)(field * 3 + 1) * 2 + d) * plane + off] = h1;
+              out[((size_t)(field * 3 + 2) * 2 + d) * plane + off] = h2;
+            }
+          }
+        }
+      } else {
+        // C[v][u] -> out fp32 [field][d][v][u], v = row
+        const int v = row_a0 + row;
+        const int u0 = row_b0 + cb;
+        if (v < p.rows_valid) {
+          float* out = reinterpret_cast<float*>(p.out) +
+                       ((size_t)(field * 2 + d) * p.out_rows + v) * p.out_cols;
+          if (u0 + 32 <= p.cols_valid && (p.out_cols & 3) == 0) {
+            float4* o4 = reinterpret_cast<float4*>(out + u0);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              float4 val = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                                       __uint_as_float(r[4 * j + 2]),
+                                       __uint_as_float(r[4 * j + 3]));
+              if (p.accumulate) {
+                const float4 old = o4[j];
+                val.x += old.x; val.y += old.y; val.z += old.z; val.w += old.w;
+              }
+              o4[j] = val;
+            }
+          } else {
+            for (int j = 0; j < 32; ++j) {
+              const int u = u0 + j;
+              if (u < p.cols_valid) {
+                float val = __uint_as_float(r[j]);
+                if (p.accumulate) val += out[u];
+                out[u] = val;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+}  // namespace tc
+}  // namespace csg

@@ -1,0 +1,225 @@
+/*
+ * csimgpu.h - C ABI of the GB300-native csim propagation hot path.
+ *
+ * Every entry point replaces one reference call on the propagation path; the
+ * reference interface it stands in for is cited beside it (paths are relative
+ * to the csim source tree). The ABI carries plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Device fields are planar fp32 ("c32p"): for a batch of F fields of
+ *    R rows (y) x C cols (x) the layout is [F][2][R][C] (real plane, then
+ *    imaginary plane), row-major, x fastest. Row r / column c is the
+ *    reference's Armadillo element (r, c) (csim_geom.cpp:203-214: x runs
+ *    along columns).
+ *  - Host fields handed to the upload/download calls are complex<double>
+ *    interleaved, either Armadillo column-major (CSG_LAYOUT_COLMAJOR, the
+ *    layout of efield.E[s][p] cubes, efield.hpp:45-52) or row-major.
+ *  - Wavelengths, coordinates and phases are passed in FP64.
+ *  - Every call returns 0 or a negative CSG_E_* code; csg_last_error() gives
+ *    the message of the last failure on the calling thread.
+ *  - Calls are asynchronous on the context's stream; csg_sync() waits and
+ *    reports device-side failures (bounded waits that ran out).
+ */
+#ifndef CSIMGPU_H
+#define CSIMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define CSG_OK 0
+#define CSG_E_ARG (-1)      /* bad pointer / size / enum */
+#define CSG_E_SHAPE (-2)    /* unsupported or inconsistent shape */
+#define CSG_E_CUDA (-3)     /* CUDA runtime/driver error */
+#define CSG_E_TIMEOUT (-4)  /* a device-side bounded wait ran out */
+#define CSG_E_NOMEM (-5)    /* device allocation failed */
+#define CSG_E_NAN (-6)      /* non-finite value where a finite one is required */
+#define CSG_E_STATE (-7)    /* object used in the wrong state */
+
+#define CSG_LAYOUT_COLMAJOR 0 /* Armadillo cube: (r,c,s) at r + c*R + s*R*C */
+#define CSG_LAYOUT_ROWMAJOR 1 /* numpy C order [s][r][c] */
+
+/* MFT precision: number of bf16 cross products kept of the 3-way split.
+ * 6 keeps every product down to 2^-16 relative (fp32-class results), 3 keeps
+ * x1y1 + x1y2 + x2y1 (about 2^-16 relative error per product). */
+#define CSG_PREC_BF16X6 6
+#define CSG_PREC_BF16X3 3
+
+typedef struct csg_ctx csg_ctx;
+typedef struct csg_mft csg_mft;
+typedef struct csg_chain csg_chain;
+typedef struct csg_respobj csg_respobj;
+typedef struct csg_de csg_de;
+
+/* ------------------------------------------------------------ context */
+/* One context per host thread: owns a CUDA stream on `device`. No global
+ * state (the reference's globalTelescope / globalCoronagraph / initialEfield,
+ * telescope.cpp:15, coronagraph.cpp:36, efield.cpp:20, become arguments). */
+int csg_create(csg_ctx** ctx, int device);
+int csg_destroy(csg_ctx* ctx);
+const char* csg_last_error(void);
+/* Wait for the context's stream and report CSG_E_TIMEOUT if a kernel gave up
+ * on a bounded wait since the last call. */
+int csg_sync(csg_ctx* ctx);
+/* Run subsequent work on an external stream (cudaStream_t, NULL = own). */
+int csg_set_stream(csg_ctx* ctx, void* stream);
+void* csg_get_stream(csg_ctx* ctx);
+/* Context-owned device memory (freed at csg_destroy if not freed before). */
+int csg_alloc(csg_ctx* ctx, size_t bytes, void** dptr);
+int csg_free(csg_ctx* ctx, void* dptr);
+int csg_memcpy_h2d(csg_ctx* ctx, void* dst, const void* src, size_t bytes);
+int csg_memcpy_d2h(csg_ctx* ctx, void* dst, const void* src, size_t bytes);
+int csg_memset(csg_ctx* ctx, void* dst, int value, size_t bytes);
+/* Version string of the library build. */
+const char* csg_version(void);
+
+/* ---------------------------------------------------- field transfer */
+/* Upload n_fields complex<double> fields (host, interleaved) of rows x cols
+ * into planar fp32 device fields. Replaces the implicit residency of
+ * efield.E[s][p] cubes (efield.hpp:45-52); `layout` is CSG_LAYOUT_*.
+ * `staging` is a device scratch of >= n_fields*rows*cols*16 bytes. */
+int csg_field_upload(csg_ctx* ctx, const double* host, int layout, int rows, int cols,
+                     int n_fields, void* staging, float* dev_field);
+int csg_field_download(csg_ctx* ctx, const float* dev_field, int rows, int cols, int n_fields,
+                       void* staging, double* host, int layout);
+
+/* ------------------------------------------------------ field sources */
+/* efield::init_point_sources (efield.cpp:179-206) with the pointSource
+ * setter's sqrt(flux) and magnification scaling (efield.cpp:295-304):
+ * E_f = amp_f * exp(2 pi i (2 x tip_f / Lx + 2 y tilt_f / Ly)) on the
+ * pixel-centre grid x_c = -(C dx - dx)/2 + c dx (csim_geom.cpp:113-142).
+ * amp/tip/tilt are per field (tip/tilt already multiplied by magnification). */
+int csg_point_source(csg_ctx* ctx, float* field, int n_fields, int rows, int cols,
+                     double dx, double dy, const double* amp, const double* tip,
+                     const double* tilt);
+
+/* ------------------------------------------------------ field elements */
+/* mask::execute (mask.cpp:23-51): E *= m (real mask, fp32 [rows][cols]).
+ * ref_quirk != 0 multiplies by (m + i m) as the reference does
+ * (cxMaskMat.set_real(m); set_imag(m), mask.cpp:53-58). */
+int csg_mask_real(csg_ctx* ctx, float* field, int n_fields, int rows, int cols,
+                  const float* mask, int ref_quirk);
+/* mirror::execute / deformableMirror::execute (mirror.cpp:23-49, :66-72;
+ * deformableMirror.cpp:22-45): E *= exp(-sign 4 pi i sag / lambda_f).
+ * sag is fp32 metres [rows][cols]; the phase is reduced in turns in FP64
+ * per pixel before the fp32 sincos. lambda is per field. */
+int csg_phase_screen(csg_ctx* ctx, float* field, int n_fields, int rows, int cols,
+                     const float* sag, const double* lambda, double sign);
+/* complexMask::execute (complexMask.cpp:24-55): centred sub-array
+ * E[r0+r][c0+c] *= amp exp(-i ph), r0 = rows/2 - mrows/2. */
+int csg_complex_mask(csg_ctx* ctx, float* field, int n_fields, int rows, int cols,
+                     const float* amp, const float* ph, int mrows, int mcols);
+
+/* ------------------------------------------------------ 2-D transforms */
+/* fft::execute / ifft::execute on a square N x N slice (csim_fft.cpp:62-95,
+ * :127, :192-193): forward exp(-i), inverse exp(+i) divided by N^2.
+ * N is a power of two, 64 <= N <= 4096. direction: -1 forward, +1 inverse. */
+int csg_fft2d(csg_ctx* ctx, float* field, int n_fields, int n, int direction);
+/* fresnelPropagateAS::execute (csim_fft.cpp:371-392): per field
+ * E <- IFFT(FFT(E) exp(i 2 pi / lambda_f z sqrt(1 - (lambda_f/apRad)^2 H / 4))),
+ * H = fftshifted integer frequency index squared. One fused pipeline:
+ * row FFT, column FFT x transfer x column IFFT, row IFFT. */
+int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
+                double ap_rad, double z);
+
+/* ------------------------------------------------------------------ MFT */
+/* Matrix Fourier transform plan: the reference's zoomFft (csim_fft.cpp:
+ * 670-708 init, 786-826 execute; Bluestein CZT 422-665) evaluated as
+ *   out[v][u] = pref_s * sum_{y,x} in[y][x] exp(sgn 2 pi i (xin_x xout_u + yin_y yout_v) / lf_s)
+ * with one (lf, pref) per operator slot s (one slot per wavelength).
+ * zoomFft semantics: sgn = -1, pref = dxin dyin / (i lf).
+ * The two contractions run on tcgen05 tensor cores with a three-way bf16
+ * split of both operands and fp32 accumulation; `precision` is CSG_PREC_*.
+ * Coordinates are FP64 vectors (xin: n_in_x, yin: n_in_y, xout: n_out_x,
+ * yout: n_out_y); pref is interleaved (re, im) per slot. */
+int csg_mft_create(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_out_y,
+                   int n_out_x, const double* yin, const double* xin, const double* yout,
+                   const double* xout, int n_slots, const double* lf, const double* pref,
+                   double sgn, int precision);
+int csg_mft_destroy(csg_mft* plan);
+/* Transform n_fields planar fields (in: [F][2][n_in_y][n_in_x]) into
+ * out ([F][2][n_out_y][n_out_x]); slot[f] picks the operator slot of field f
+ * (device int array). accumulate != 0 adds into out (the Babinet "+ E" of
+ * fpmPupToLyot.cpp:155-158). `in_mul` (optional, planar complex
+ * [n_mul][2][n_in_y][n_in_x], field f uses mul index mul_idx[f]) multiplies
+ * the input first (the focal-plane mask of doubleFraunhoferFPM /
+ * fpmPupToLyot). */
+int csg_mft_execute(csg_ctx* ctx, csg_mft* plan, const float* in, float* out, int n_fields,
+                    const int* slot, int accumulate, const float* in_mul, const int* mul_idx);
+/* Bytes of device scratch the plan uses for n_fields (informational). */
+size_t csg_mft_workspace_bytes(csg_mft* plan, int n_fields);
+
+/* ---------------------------------------------------------- hex FPM */
+/* complexHexMaskFPM::make_complex_intpolated_mask (complexHexMaskFPM.cpp:
+ * 44-99) for a batch of (candidate, wavelength) masks:
+ *   M = sum_{k<3} n[k] exp(i phaseSign 4 pi sag[id[k]] / lambda) / nSub^2
+ * with sag 0 where id < 0. Tables: hex_id int16 [3][S][S], count uint16
+ * [3][S][S] (the reference's interpHexNum / interpNSubPix cubes).
+ * sags: [n_cand][n_hex] FP64. For output j: candidate cand[j], wavelength
+ * lambda[j]; out is planar [n_out][2][S][S] holding fliplr(M) - subtract
+ * (fpmIntHexCMCForPupToLyot::set_fpmMatAmp, fpmPupToLyot.cpp:441-451:
+ * flip = 1, subtract = 1 for the Babinet form). use_only_hex selects one
+ * hex as the reference's useOnlyThisHex (-1 = all; n_hex = outside only). */
+int csg_hex_mask(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S, int n_sub,
+                 const double* sags, int n_hex, int n_out, const int* cand, const double* lambda,
+                 double phase_sign, int flip, double subtract, int use_only_hex, float* out);
+/* Build the interpolation tables on the GPU (complexHexMaskFPM.cpp:317-469,
+ * make_hex_array + make_interpolation_data). centres in hex-step units
+ * (hex_x, hex_y), design array A x A, mask S x S at pixel_scale. */
+int csg_hex_tables(csg_ctx* ctx, const double* hex_x, const double* hex_y, int n_hex,
+                   int n_rings, int design_size, double fpm_scale_factor, double hex_gap,
+                   int S, int n_sub, double pixel_scale, double fpm_radius, int16_t* hex_id,
+                   uint16_t* count);
+
+/* ---------------------------------------------------- intensity / contrast */
+/* regionContrast::compute_intensity (regionContrast.cpp:124-143) and the
+ * contrast mean (:195) / optObjective mean-or-max (optObjective.cpp:56-67):
+ * For each group g (n_groups groups of `per_group` consecutive fields),
+ * I_g = sum_fields |E|^2 restricted to the n_pix region pixels pix_idx
+ * (row-major flat indices); out[g] = reduce(I_g) * scale where reduce is
+ * mean (mode 0) or max (mode 1). FP64 accumulation. */
+int csg_region_reduce(csg_ctx* ctx, const float* field, int rows, int cols, int n_groups,
+                      int per_group, const int* pix_idx, int n_pix, int mode, double scale,
+                      double* out);
+/* Full-image intensity sum over n_fields fields into out [rows][cols]
+ * (FP64) and its maximum into out_max (the calibration max of
+ * regionContrast.cpp:139-142). */
+int csg_intensity(csg_ctx* ctx, const float* field, int rows, int cols, int n_fields,
+                  double* out, double* out_max);
+
+/* ---------------------------------------- response-matrix objective */
+/* optHexRespObjective (optObjective.cpp:24-69): M cubes for every (s, p, l)
+ * as complex<double> interleaved host row-major [n_mat][npix][ncol]
+ * (ncol = nhex + 1), wavelength of each matrix, calibration intensity. */
+int csg_respobj_create(csg_ctx* ctx, csg_respobj** obj, const double* m_host, int n_mat,
+                       int npix, int ncol, const double* wavelength, double calib,
+                       double phase_sign, int objective /*0 mean, 1 max*/);
+int csg_respobj_destroy(csg_respobj* obj);
+/* optHexRespObjective::execute(mat& optData, rowvec& objVal): x is device
+ * FP64 [pop][nvar] (nvar = ncol - 1; candidate-major, i.e. the transpose of
+ * the reference's nvar x pop matrix), out device FP64 [pop]. */
+int csg_respobj_execute(csg_respobj* obj, const double* x, int pop, double* out);
+
+/* ------------------------------------------------ differential evolution */
+/* differentialEvolutionOptimizer generation step (differentialEvolution
+ * Optimizer.cpp:261-281; deStrategy.cpp:23-158) on device FP64 populations
+ * [pop][nvar]: strategy 0 = DE/rand/1, 1 = DE/local-to-best/1, 2 = either-or;
+ * binomial crossover without a forced index (:360-369); bounce-back into
+ * [lo, hi] (:395-434). Random numbers come from a counter-based generator
+ * keyed by (seed, generation), so a generation is reproducible. */
+int csg_de_mutate(csg_ctx* ctx, const double* pop_x, const double* best, int pop, int nvar,
+                  int strategy, double f_weight, double cr, const double* lo, const double* hi,
+                  uint64_t seed, uint64_t generation, double* trial, double* origin);
+/* Greedy selection (differentialEvolutionOptimizer.cpp:436-453):
+ * where f_trial < f, x <- trial, f <- f_trial. */
+int csg_de_select(csg_ctx* ctx, double* pop_x, double* f, const double* trial,
+                  const double* f_trial, int pop, int nvar);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CSIMGPU_H */

@@ -1,0 +1,89 @@
+"""CPU tests of the oracle against the reference's own fixtures and identities."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import csim_fft as of
+from oracle import elements as oe
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_response_objective_known_answer():
+    """optHexRespObjective(mono M, bestOptVector) reproduces the recorded DE
+    best value (optObjective.cpp:24-69; optBestVal.txt last line, %g)."""
+    g = np.load(os.path.join(GOLD, "mono_response.npz"))
+    for x, rec in zip(g["best_x"], g["best_val"]):
+        f = oe.opt_hex_resp_objective([g["M"]], g["wavelengths"], float(g["calib"]), x[:, None])
+        assert abs(f[0] - 1.3501189541e-10) / 1.35e-10 < 1e-8
+        assert abs(f[0] - rec) / rec < 5e-6  # recorded with 6 significant digits
+
+
+def test_response_objective_max_and_batch():
+    g = np.load(os.path.join(GOLD, "mono_response.npz"))
+    rng = np.random.default_rng(3)
+    x = np.hstack([g["best_x"][0][:, None], rng.uniform(-5e-8, 5e-8, (499, 3))])
+    f = oe.opt_hex_resp_objective([g["M"]], g["wavelengths"], float(g["calib"]), x)
+    fm = oe.opt_hex_resp_objective([g["M"]], g["wavelengths"], float(g["calib"]), x, objective="max")
+    assert f.shape == (4,) and np.all(fm >= f)
+    assert abs(f[0] - 1.3501189541e-10) / 1.35e-10 < 1e-8
+
+
+def test_bluestein_equals_mft():
+    rng = np.random.default_rng(0)
+    for n, k in [(64, 48), (50, 64), (128, 37)]:
+        e = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        z = of.ZoomFft(of.ArrayGeom.set_xy(n, n, 1e-4), of.ArrayGeom.set_xy(k, k, 3e-6), [2.3e-6])
+        a, b = z.execute(e, 0), z.mft(e, 0)
+        assert np.abs(a - b).max() / np.abs(b).max() < 1e-12
+
+
+def test_pup_to_lyot_conv_equals_mft_form():
+    rng = np.random.default_rng(1)
+    n, s = 32, 24
+    e = rng.standard_normal((2, n, n)) + 1j * rng.standard_normal((2, n, n))
+    m1 = rng.standard_normal((2, s, s)) + 1j * rng.standard_normal((2, s, s))
+    eg, mg = of.ArrayGeom.set_xy(n, n, 1e-4), of.ArrayGeom.set_xy(s, s, 2.3e-6)
+    lam = [6.5e-7, 7e-7]
+    lfl = -np.array(lam) * 3.0 * 2 * n * 1e-4 / 2
+    a = oe.pup_to_lyot_conv(e, lam, eg, mg, m1, lfl, -1.0, 1.0)
+    b = oe.pup_to_lyot_mft(e, lam, eg, mg, m1, lfl, -1.0, 1.0)
+    assert np.abs(a - b).max() / np.abs(a).max() < 1e-12
+
+
+def test_hex_counts_match_reference_layouts():
+    assert len(oe.hex_centers(20)[0]) == 499      # fixture width - 1
+    g = np.load(os.path.join(GOLD, "hex_counts.npz"))
+    assert len(oe.hex_centers(32)[0]) == int(g["wfirst_sags_len"])
+    assert len(oe.hex_centers_standard(8)[0]) == 217
+    assert len(oe.hex_centers_standard(20)[0]) == 1261
+
+
+def test_fresnel_is_unitary_and_reversible():
+    rng = np.random.default_rng(2)
+    e = rng.standard_normal((1, 64, 64)) + 1j * rng.standard_normal((1, 64, 64))
+    p = of.fresnel_propagate_as(e, [6.5e-7], 0.01, 1.0)
+    assert abs(np.linalg.norm(p) / np.linalg.norm(e) - 1) < 1e-12
+    back = of.fresnel_propagate_as(p, [6.5e-7], 0.01, -1.0)
+    assert np.abs(back - e).max() < 1e-10
+
+
+def test_fft_shift_floor_and_truncate():
+    a = np.arange(25.0).reshape(5, 5)
+    assert np.array_equal(of.fft_shift(a), np.fft.fftshift(a))  # floor(5/2)=2 == numpy for odd
+    b = np.arange(36.0).reshape(6, 6) + 0j
+    t = of.fft_truncate(b, 4, 4)
+    assert t.shape == (4, 4)
+    assert t[0, 0] == b[0, 0]
+    assert t[2, 0] == (b[2, 0] + b[4, 0]) / 2
+
+
+def test_mask_quirk_and_mirror():
+    e = np.ones((1, 4, 4), complex)
+    m = np.full((4, 4), 0.5)
+    assert np.allclose(oe.mask_apply(e, m), 0.5 + 0.5j)
+    s = np.full((4, 4), 1e-7)
+    out = oe.mirror_apply(e, s, [6.5e-7], 1.0)
+    assert np.allclose(out, np.exp(-4j * math.pi * 1e-7 / 6.5e-7))
