@@ -111,7 +111,10 @@ int csg_sync(csg_ctx* c) {
 
 int csg_set_stream(csg_ctx* c, void* stream) {
   CSG_CHECK(c != nullptr, CSG_E_ARG, "csg_set_stream: null context");
-  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  // NULL selects CUDA's default stream (stream 0), which is what torch's
+  // default stream handle is; the context's own stream is used until this
+  // call is made.
+  c->stream = static_cast<cudaStream_t>(stream);
   return CSG_OK;
 }
 

@@ -3,10 +3,10 @@
 // One launch computes, for a batch of fields, the real-ified complex product
 //   C = sum_{terms (pa,pb)} sum_{comp c} A[pa, sel] * B[pb, sel]^T
 // with both operands K-major bf16 tiles staged by TMA (128B swizzle) into a
-// 4-deep shared-memory ring, accumulated in fp32 in tensor memory by a single
-// issuing thread (tcgen05.mma.cta_group::1.kind::f16, M = 128, N = BN,
-// K = 16 per instruction) and drained by four epilogue warps with
-// tcgen05.ld.32x32b.
+// shared-memory ring, multiplied by a single issuing thread
+// (tcgen05.mma.cta_group::1.kind::f16, M = 128, N = BN, K = 16 per
+// instruction) into rotating tensor-memory slots, and drained by eight warps
+// (tcgen05.ld.32x32b) into fp32 register accumulators.
 //
 // Operand roles: one operand is a field ("data", indexed by field and split
 // part) and the other an MFT operator ("op", indexed by the field's slot and
@@ -23,8 +23,6 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BK = 64;  // bf16 elements per 128-byte swizzled row
-constexpr int STAGES = 4;
-constexpr int THREADS = 128;
 
 enum Epi { EPI_T_SPLIT = 0, EPI_F32 = 1 };
 
@@ -155,11 +153,32 @@ __device__ __forceinline__ int sel_plane(int d, int c) {
   return d == 0 ? (c == 0 ? 0 : 2) : (c == 0 ? 1 : 0);
 }
 
-// Dynamic shared memory: STAGES x (A tile + B tile), 1024-byte aligned, then
-// barriers and the TMEM base address.
+
+// Tensor-core fp32 accumulation truncates at every instruction, so a long
+// accumulation chain in tensor memory shrinks the result by ~2^-24 per
+// instruction. The kernel therefore never accumulates more than one K block
+// (BK = 64, four instructions) in tensor memory: each K block goes to a fresh
+// tensor-memory slot (NSLOT slots rotate through the 512 columns) and eight
+// drain warps add every finished slot into fp32 registers with
+// round-to-nearest adds while the next blocks are multiplied.
+constexpr int DRAIN_WARPS = 8;
+constexpr int THREADS = (DRAIN_WARPS + 2) * 32;  // + TMA producer warp + MMA warp
+constexpr int PRODUCER_WARP = DRAIN_WARPS;
+constexpr int MMA_WARP = DRAIN_WARPS + 1;
+
+template <int BN>
+struct Cfg {
+  static constexpr int NSLOT = 512 / BN;           // tensor-memory slots
+  static constexpr int STAGES = BN == 256 ? 4 : 6; // shared-memory ring depth
+  static constexpr uint32_t A_BYTES = BM * BK * 2;
+  static constexpr uint32_t B_BYTES = BN * BK * 2;
+  static constexpr int COLS_PER_WARP = BN / 2;     // two warps share a lane quadrant
+  static constexpr size_t SMEM = (size_t)STAGES * (A_BYTES + B_BYTES) + 1024 + 512;
+};
+
 template <int BN>
 constexpr size_t smem_bytes() {
-  return (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 1024 /*align*/ + 256 /*barriers*/;
+  return Cfg<BN>::SMEM;
 }
 
 // OP_IS_A = false: stage 1 (A = data rows y, B = operator rows u, d from N tile)
@@ -168,25 +187,26 @@ template <int BN, bool OP_IS_A, int EPI>
 __global__ void __launch_bounds__(THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const Params p) {
+  using CF = Cfg<BN>;
+  constexpr int STAGES = CF::STAGES;
+  constexpr int NSLOT = CF::NSLOT;
+  constexpr int CPW = CF::COLS_PER_WARP;
   extern __shared__ uint8_t smem_raw[];
-  constexpr uint32_t A_BYTES = BM * BK * 2;
-  constexpr uint32_t B_BYTES = BN * BK * 2;
-  constexpr uint32_t TMEM_COLS = BN;  // fp32 accumulator columns (power of 2 >= 32)
 
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
   uint8_t* sA = sbase;
-  uint8_t* sB = sbase + STAGES * A_BYTES;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + STAGES * B_BYTES);
+  uint8_t* sB = sbase + STAGES * CF::A_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + STAGES * CF::B_BYTES);
   uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* tfull = empty + STAGES;   // slot filled by the MMA warp
+  uint64_t* tempty = tfull + NSLOT;   // slot drained by the drain warps
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + NSLOT);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
 
-  // tile decode: n fastest, then m, then field
   int t = blockIdx.x;
   const int nt = t % p.n_tiles;
   t /= p.n_tiles;
@@ -198,12 +218,12 @@ __global__ void __launch_bounds__(THREADS, 1)
   int d, row_a0, row_b0;
   if (!OP_IS_A) {
     d = nt / p.n_half;
-    row_a0 = mt * BM;                    // data rows (y)
-    row_b0 = (nt % p.n_half) * BN;       // operator rows (u)
+    row_a0 = mt * BM;
+    row_b0 = (nt % p.n_half) * BN;
   } else {
     d = mt / p.m_half;
-    row_a0 = (mt % p.m_half) * BM;       // operator rows (v)
-    row_b0 = nt * BN;                    // data rows (u)
+    row_a0 = (mt % p.m_half) * BM;
+    row_b0 = nt * BN;
   }
 
   if (threadIdx.x == 0) {
@@ -211,14 +231,17 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    for (int s = 0; s < NSLOT; ++s) {
+      mbar_init(&tfull[s], 1);
+      mbar_init(&tempty[s], DRAIN_WARPS);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
+                 "r"(512));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -228,131 +251,152 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   const int k_iters = p.n_terms * 2 * p.k_blocks;
 
-  if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
-    int stage = 0;
-    uint32_t phase = 0;
-    for (int it = 0; it < k_iters; ++it) {
-      if (it >= STAGES) {
-        if (!mbar_wait(&empty[stage], phase ^ 1)) {
+  if (warp == PRODUCER_WARP) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int it = 0; it < k_iters; ++it) {
+        if (it >= STAGES && !mbar_wait(&empty[stage], phase ^ 1)) {
           atomicExch(p.status, 1);
           *abort_flag = 1;
           break;
         }
-      }
-      if (*abort_flag) break;
-      const int kb = it % p.k_blocks;
-      const int c = (it / p.k_blocks) & 1;
-      const int term = it / (2 * p.k_blocks);
-      const int pa = p.term_a[term], pb = p.term_b[term];
-      int za, zb;
-      if (!OP_IS_A) {
-        za = (field * 3 + pa) * 2 + c;
-        zb = (slot * 3 + pb) * 3 + sel_plane(d, c);
-      } else {
-        za = (slot * 3 + pa) * 3 + sel_plane(d, c);
-        zb = (field * 3 + pb) * 2 + c;
-      }
-      mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
-      tma_load_3d(sA + stage * A_BYTES, &tmA, &full[stage], kb * BK, row_a0, za);
-      tma_load_3d(sB + stage * B_BYTES, &tmB, &full[stage], kb * BK, row_b0, zb);
-      if (++stage == STAGES) {
-        stage = 0;
-        phase ^= 1;
+        if (*abort_flag) break;
+        const int kb = it % p.k_blocks;
+        const int c = (it / p.k_blocks) & 1;
+        const int term = it / (2 * p.k_blocks);
+        const int pa = p.term_a[term], pb = p.term_b[term];
+        int za, zb;
+        if (!OP_IS_A) {
+          za = (field * 3 + pa) * 2 + c;
+          zb = (slot * 3 + pb) * 3 + sel_plane(d, c);
+        } else {
+          za = (slot * 3 + pa) * 3 + sel_plane(d, c);
+          zb = (field * 3 + pb) * 2 + c;
+        }
+        mbar_expect_tx(&full[stage], CF::A_BYTES + CF::B_BYTES);
+        tma_load_3d(sA + stage * CF::A_BYTES, &tmA, &full[stage], kb * BK, row_a0, za);
+        tma_load_3d(sB + stage * CF::B_BYTES, &tmB, &full[stage], kb * BK, row_b0, zb);
+        if (++stage == STAGES) {
+          stage = 0;
+          phase ^= 1;
+        }
       }
     }
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer
-    constexpr uint32_t idesc = instr_desc(BM, BN);
-    int stage = 0;
-    uint32_t phase = 0;
+    __syncwarp();
+  } else if (warp == MMA_WARP) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = instr_desc(BM, BN);
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int it = 0; it < k_iters; ++it) {
+        const int ts = it % NSLOT;
+        const uint32_t round = (uint32_t)(it / NSLOT);
+        bool ok = true;
+        if (it >= NSLOT) ok = mbar_wait(&tempty[ts], (round & 1u) ^ 1u);
+        if (ok) ok = mbar_wait(&full[stage], phase);
+        if (!ok || *abort_flag) {
+          atomicExch(p.status, 2);
+          *abort_flag = 1;
+          // release every drain wait so nobody waits for the full budget again
+          for (int s = 0; s < NSLOT; ++s)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tfull[s]))
+                         : "memory");
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(sA + stage * CF::A_BYTES);
+        const uint32_t b0 = smem_u32(sB + stage * CF::B_BYTES);
+        const uint32_t dcol = tmem + (uint32_t)(ts * BN);
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k)
+          umma(dcol, smem_desc(a0 + k * 32), smem_desc(b0 + k * 32), idesc, k > 0 ? 1u : 0u);
+        umma_commit(&empty[stage]);
+        umma_commit(&tfull[ts]);
+        if (++stage == STAGES) {
+          stage = 0;
+          phase ^= 1;
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- drain warps: quadrant q of the 128 rows, half h of the columns
+    const int q = warp & 3, h = warp >> 2;
+    const int row = q * 32 + lane;
+    float acc[CPW];
+#pragma unroll
+    for (int j = 0; j < CPW; ++j) acc[j] = 0.f;
     bool ok = true;
     for (int it = 0; it < k_iters; ++it) {
-      if (!mbar_wait(&full[stage], phase)) {
-        atomicExch(p.status, 2);
-        *abort_flag = 1;
-        ok = false;
-        break;
-      }
+      const int ts = it % NSLOT;
+      const uint32_t round = (uint32_t)(it / NSLOT);
+      ok = mbar_wait(&tfull[ts], round & 1u);
+      ok = __all_sync(0xffffffffu, ok && !*abort_flag);
+      if (!ok) break;
       tc_fence_after();
-      const uint32_t a0 = smem_u32(sA + stage * A_BYTES);
-      const uint32_t b0 = smem_u32(sB + stage * B_BYTES);
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(ts * BN + h * CPW);
 #pragma unroll
-      for (int k = 0; k < BK / 16; ++k) {
-        umma(tmem, smem_desc(a0 + k * 32), smem_desc(b0 + k * 32), idesc,
-             (it > 0 || k > 0) ? 1u : 0u);
+      for (int cb = 0; cb < CPW; cb += 32) {
+        uint32_t r[32];
+        tmem_ld32(taddr + cb, r);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc[cb + j] += __uint_as_float(r[j]);
       }
-      umma_commit(&empty[stage]);
-      if (++stage == STAGES) {
-        stage = 0;
-        phase ^= 1;
-      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[ts]))
+                     : "memory");
     }
-    // signal the epilogue (also on abort, so nobody waits forever)
-    if (ok) umma_commit(accum);
-    else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(accum)) : "memory");
-  }
-  __syncwarp();
-
-  // ---------------- epilogue: all four warps
-  bool ready = mbar_wait(accum, 0);
-  if (!ready) atomicExch(p.status, 3);
-  tc_fence_after();
-  const int row = warp * 32 + lane;  // tile row held by this thread
-  // tcgen05.ld is warp-collective: decide per warp
-  ready = __all_sync(0xffffffffu, ready && !*abort_flag);
-  if (ready) {
-    for (int cb = 0; cb < BN; cb += 32) {
-      uint32_t r[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb, r);
-      if (EPI == EPI_T_SPLIT) {
-        // C[y][u] -> T^T parts [field][part][d][u][y] (bf16), y = row
-        const int y = row_a0 + row;
-        const int u0 = row_b0 + cb;
-        if (y < p.out_cols) {
-          __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
-          const size_t plane = (size_t)p.out_rows * p.out_cols;
-#pragma unroll 4
-          for (int j = 0; j < 32; ++j) {
-            const int u = u0 + j;
-            if (u < p.cols_valid) {
-              __nv_bfloat16 h0, h1, h2;
-              split3(__uint_as_float(r[j]), h0, h1, h2);
-              const size_t off = (size_t)u * p.out_cols + y;
-              out[((size_t)(field * 3 + 0) * 2 + d) * plane + off] = h0;
-              out[((size_t)(field * 3 + 1) * 2 + d) * plane + off] = h1;
-              out[((size_t)(field * 3 + 2) * 2 + d) * plane + off] = h2;
-            }
+    if (!ok) {
+      atomicExch(p.status, 3);
+    } else if (EPI == EPI_T_SPLIT) {
+      // C[y][u] -> T^T parts [field][part][d][u][y] (bf16)
+      const int y = row_a0 + row;
+      if (y < p.out_cols) {
+        __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+        const size_t plane = (size_t)p.out_rows * p.out_cols;
+        const int u0 = row_b0 + h * CPW;
+#pragma unroll
+        for (int j = 0; j < CPW; ++j) {
+          const int u = u0 + j;
+          if (u < p.cols_valid) {
+            __nv_bfloat16 h0, h1, h2;
+            split3(acc[j], h0, h1, h2);
+            const size_t off = (size_t)u * p.out_cols + y;
+            out[((size_t)(field * 3 + 0) * 2 + d) * plane + off] = h0;
+            out[((size_t)(field * 3 + 1) * 2 + d) * plane + off] = h1;
+            out[((size_t)(field * 3 + 2) * 2 + d) * plane + off] = h2;
           }
         }
-      } else {
-        // C[v][u] -> out fp32 [field][d][v][u], v = row
-        const int v = row_a0 + row;
-        const int u0 = row_b0 + cb;
-        if (v < p.rows_valid) {
-          float* out = reinterpret_cast<float*>(p.out) +
-                       ((size_t)(field * 2 + d) * p.out_rows + v) * p.out_cols;
-          if (u0 + 32 <= p.cols_valid && (p.out_cols & 3) == 0) {
-            float4* o4 = reinterpret_cast<float4*>(out + u0);
+      }
+    } else {
+      // C[v][u] -> out fp32 [field][d][v][u]
+      const int v = row_a0 + row;
+      if (v < p.rows_valid) {
+        float* out = reinterpret_cast<float*>(p.out) +
+                     ((size_t)(field * 2 + d) * p.out_rows + v) * p.out_cols;
+        const int u0 = row_b0 + h * CPW;
+        if (u0 + CPW <= p.cols_valid && (p.out_cols & 3) == 0) {
+          float4* o4 = reinterpret_cast<float4*>(out + u0);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              float4 val = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
-                                       __uint_as_float(r[4 * j + 2]),
-                                       __uint_as_float(r[4 * j + 3]));
-              if (p.accumulate) {
-                const float4 old = o4[j];
-                val.x += old.x; val.y += old.y; val.z += old.z; val.w += old.w;
-              }
-              o4[j] = val;
+          for (int j = 0; j < CPW / 4; ++j) {
+            float4 val = make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]);
+            if (p.accumulate) {
+              const float4 old = o4[j];
+              val.x += old.x; val.y += old.y; val.z += old.z; val.w += old.w;
             }
-          } else {
-            for (int j = 0; j < 32; ++j) {
-              const int u = u0 + j;
-              if (u < p.cols_valid) {
-                float val = __uint_as_float(r[j]);
-                if (p.accumulate) val += out[u];
-                out[u] = val;
-              }
+            o4[j] = val;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < CPW; ++j) {
+            const int u = u0 + j;
+            if (u < p.cols_valid) {
+              float val = acc[j];
+              if (p.accumulate) val += out[u];
+              out[u] = val;
             }
           }
         }
@@ -363,8 +407,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
   }
 }
 

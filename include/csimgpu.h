@@ -65,7 +65,8 @@ const char* csg_last_error(void);
 /* Wait for the context's stream and report CSG_E_TIMEOUT if a kernel gave up
  * on a bounded wait since the last call. */
 int csg_sync(csg_ctx* ctx);
-/* Run subsequent work on an external stream (cudaStream_t, NULL = own). */
+/* Run subsequent work on an external stream (a cudaStream_t; NULL is CUDA's
+ * default stream). A new context runs on its own non-blocking stream. */
 int csg_set_stream(csg_ctx* ctx, void* stream);
 void* csg_get_stream(csg_ctx* ctx);
 /* Context-owned device memory (freed at csg_destroy if not freed before). */
