@@ -62,7 +62,21 @@ SIGNATURES = {
     "csg_mft_execute": ([P, P, P, P, I, P, I, P, P], None),
     "csg_mft_workspace_bytes": ([P, I], SZ),
     "csg_hex_mask": ([P, P, P, I, I, P, I, I, P, P, D, I, D, I, P], None),
-    "csg_hex_tables": ([P, P, P, I, I, I, D, D, I, I, D, D, P, P], None),
+    "csg_hex_tables": ([P, P, P, I, I, I, D, D, D, I, I, D, D, P, P, P], None),
+    "csg_chain_create": ([P, C.POINTER(P), I, D, I, P, I], None),
+    "csg_chain_destroy": ([P], None),
+    "csg_chain_add_mask": ([P, P, I, I], None),
+    "csg_chain_add_mirror": ([P, P, D], None),
+    "csg_chain_add_fresnel": ([P, D, D], None),
+    "csg_chain_add_complex_mask": ([P, P, P, I, I, I], None),
+    "csg_chain_add_fpm_hex": ([P, P, P, I, I, I, D, D, D, D, D, D, I], None),
+    "csg_chain_add_fraunhofer": ([P, I, D, D], None),
+    "csg_chain_set_batch": ([P, I, P, P, P, P, P], None),
+    "csg_chain_sags": ([P, I, I, C.POINTER(P)], None),
+    "csg_chain_execute": ([P, I, I], None),
+    "csg_chain_image": ([P, C.POINTER(P), C.POINTER(I)], None),
+    "csg_chain_field": ([P, C.POINTER(P)], None),
+    "csg_mft_reserve": ([P, I], None),
     "csg_region_reduce": ([P, P, I, I, I, I, P, I, I, D, P], None),
     "csg_intensity": ([P, P, I, I, I, P, P], None),
     "csg_respobj_create": ([P, C.POINTER(P), P, I, I, I, P, D, D, I], None),

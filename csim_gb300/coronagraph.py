@@ -1,0 +1,271 @@
+"""Host-side mirror of the reference's coronagraph API, driving the native
+chain executor through the C ABI.
+
+Names follow the reference: a ``Telescope`` (telescope.cpp), an ``EField``
+description (efield.cpp), element classes named after the reference's
+elements (mask, mirror, fresnelPropagator, complexMask, fpmPupToLyot with the
+interpolated-hex adapter, fraunhoferFocal), a ``Coronagraph`` that walks them
+(coronagraph.cpp:175-200) for a whole batch of (wavelength, source,
+candidate) fields at once, and ``RegionContrast`` (regionContrast.cpp).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from ._lib import CSG_PREC_BF16X6, call
+from .runtime import Context, dvec, ptr
+
+
+@dataclass
+class Telescope:
+    """telescope.cpp:21-60."""
+    primaryDiameter: float
+    primaryfRatio: float
+    magnification: float = 1.0
+
+    @property
+    def primaryfLength(self) -> float:
+        return self.primaryfRatio * self.primaryDiameter
+
+    def compute_loD(self, lam: float) -> float:
+        return self.magnification * self.primaryfLength * lam / self.primaryDiameter
+
+
+@dataclass
+class PointSource:
+    """efield pointSource: flux (amplitude sqrt(flux)), tip/tilt in the
+    reference's units (multiplied by the telescope magnification)."""
+    flux: float = 1.0
+    tip: float = 0.0
+    tilt: float = 0.0
+
+
+@dataclass
+class EField:
+    """efield.cpp: square N x N array, beam radius and pixel scale (metres)."""
+    n: int
+    beamRadiusPhysical: float
+    pixelScale: float
+    wavelengths: np.ndarray
+    sources: list = field(default_factory=lambda: [PointSource()])
+
+    @property
+    def arrayRadiusPhysical(self) -> float:
+        beam_px = math.ceil(2 * self.beamRadiusPhysical / self.pixelScale)
+        return self.beamRadiusPhysical * self.n / beam_px
+
+    def pixel_centres(self) -> np.ndarray:
+        d = self.pixelScale
+        return -(d * self.n - d) / 2.0 + np.arange(self.n) * d
+
+
+# ------------------------------------------------------------- elements
+@dataclass
+class Mask:
+    """mask element (mask.cpp): real mask, multiplied as (m + i m) when
+    ref_quirk is set, exactly as the reference does."""
+    mask: np.ndarray
+    ref_quirk: bool = True
+    disableForCalibration: bool = False
+
+
+@dataclass
+class Mirror:
+    """mirror element (mirror.cpp): sag in metres, phase -sign 4 pi sag / lambda."""
+    sag: np.ndarray
+    mirrorSign: float = 1.0
+
+
+@dataclass
+class FresnelPropagator:
+    """fresnelPropagator (fresnelPropagator.cpp): signed distance z."""
+    z: float
+
+
+@dataclass
+class ComplexMask:
+    """complexMask (complexMask.cpp): centred amp exp(-i ph)."""
+    amp: np.ndarray
+    ph: np.ndarray
+    disableForCalibration: bool = False
+
+
+@dataclass
+class FpmPupToLyotHex:
+    """fpmPupToLyot + fpmIntHexCMCForPupToLyot + complexHexMaskFPM: hex tables
+    [3][S][S] (ids, counts), nSubPix, hex count, mask pixel scale (metres),
+    focalRatio, fRatioSign, zoomFftSign, phaseSign."""
+    hex_id: np.ndarray
+    count: np.ndarray
+    n_sub: int
+    n_hex: int
+    pixelScale: float
+    focalRatio: float
+    fRatioSign: float = -1.0
+    zoomFftSign: float = -1.0
+    phaseSign: float = 1.0
+    disableForCalibration: bool = True
+
+
+@dataclass
+class FraunhoferFocal:
+    """fraunhoferFocal (fraunhoferFocal.cpp:65-72): ceil(FOV spl)^2 pixels at
+    loD(referenceLambda) / spl."""
+    referenceLambda: float
+    samplesPerflD: float
+    FOVflD: float
+
+    def n_out(self) -> int:
+        return math.ceil(self.FOVflD * self.samplesPerflD)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Coronagraph:
+    """Batched coronagraph (coronagraph.cpp). ``set_batch`` chooses the fields;
+    ``execute`` runs every element once over the batch and returns the final
+    image fields as a planar fp32 tensor [F, 2, n_out, n_out]."""
+
+    def __init__(self, ctx: Context, tel: Telescope, ef: EField, elements: list,
+                 precision: int = CSG_PREC_BF16X6):
+        self.ctx, self.tel, self.ef, self.elements = ctx, tel, ef, elements
+        lam = np.ascontiguousarray(ef.wavelengths, dtype=np.float64)
+        h = C.c_void_p()
+        call("csg_chain_create", ctx.h, C.byref(h), ef.n, ef.pixelScale, lam.size,
+             lam.ctypes.data_as(C.c_void_p), precision)
+        self.h = h
+        self.n_hex = None
+        self.n_out = None
+        self.out_pixel = None
+        for e in elements:
+            self._add(e)
+
+    def _add(self, e):
+        if isinstance(e, Mask):
+            m = _f32(e.mask)
+            call("csg_chain_add_mask", self.h, m.ctypes.data_as(C.c_void_p), int(e.ref_quirk),
+                 int(e.disableForCalibration))
+        elif isinstance(e, Mirror):
+            s = _f32(e.sag)
+            call("csg_chain_add_mirror", self.h, s.ctypes.data_as(C.c_void_p), e.mirrorSign)
+        elif isinstance(e, FresnelPropagator):
+            call("csg_chain_add_fresnel", self.h, e.z, self.ef.arrayRadiusPhysical)
+        elif isinstance(e, ComplexMask):
+            a, p = _f32(e.amp), _f32(e.ph)
+            call("csg_chain_add_complex_mask", self.h, a.ctypes.data_as(C.c_void_p),
+                 p.ctypes.data_as(C.c_void_p), a.shape[0], a.shape[1],
+                 int(e.disableForCalibration))
+        elif isinstance(e, FpmPupToLyotHex):
+            ids = np.ascontiguousarray(e.hex_id, np.int16)
+            cnt = np.ascontiguousarray(e.count, np.uint16)
+            call("csg_chain_add_fpm_hex", self.h, ids.ctypes.data_as(C.c_void_p),
+                 cnt.ctypes.data_as(C.c_void_p), ids.shape[-1], e.n_sub, e.n_hex, e.pixelScale,
+                 e.focalRatio, self.ef.beamRadiusPhysical, e.fRatioSign, e.zoomFftSign,
+                 e.phaseSign, int(e.disableForCalibration))
+            self.n_hex = e.n_hex
+        elif isinstance(e, FraunhoferFocal):
+            self.n_out = e.n_out()
+            self.out_pixel = self.tel.compute_loD(e.referenceLambda) / e.samplesPerflD
+            call("csg_chain_add_fraunhofer", self.h, self.n_out, self.out_pixel,
+                 2 * self.ef.beamRadiusPhysical * self.tel.primaryfRatio)
+        else:
+            raise TypeError(f"unsupported element {type(e).__name__}")
+
+    def set_batch(self, lambda_idx, amp, tip, tilt, cand):
+        arrs = [np.ascontiguousarray(lambda_idx, np.int32), np.ascontiguousarray(amp, np.float64),
+                np.ascontiguousarray(tip, np.float64), np.ascontiguousarray(tilt, np.float64),
+                np.ascontiguousarray(cand, np.int32)]
+        self.n_fields = arrs[0].size
+        self._batch = arrs
+        call("csg_chain_set_batch", self.h, self.n_fields,
+             *[a.ctypes.data_as(C.c_void_p) for a in arrs])
+
+    def batch_all(self, n_cand: int = 1):
+        """Every (candidate, source, wavelength) combination, candidate-major."""
+        L = len(self.ef.wavelengths)
+        li, amp, tip, tilt, cand = [], [], [], [], []
+        for c in range(n_cand):
+            for s in self.ef.sources:
+                for l in range(L):
+                    li.append(l)
+                    amp.append(math.sqrt(s.flux))
+                    tip.append(s.tip * self.tel.magnification)
+                    tilt.append(s.tilt * self.tel.magnification)
+                    cand.append(c)
+        self.set_batch(li, amp, tip, tilt, cand)
+        return len(li)
+
+    def sags(self, n_cand: int) -> torch.Tensor:
+        """The device sag buffer [n_cand, n_hex] (a torch view, written in place)."""
+        p = C.c_void_p()
+        call("csg_chain_sags", self.h, n_cand, self.n_hex, C.byref(p))
+        self._sag_ptr = p.value
+        return _tensor_from_ptr(p.value, (n_cand, self.n_hex), torch.float64)
+
+    def execute(self, calibrating: bool = False, use_graph: bool = False) -> torch.Tensor:
+        call("csg_chain_execute", self.h, int(calibrating), int(use_graph))
+        p = C.c_void_p()
+        n = C.c_int()
+        call("csg_chain_image", self.h, C.byref(p), C.byref(n))
+        return _tensor_from_ptr(p.value, (self.n_fields, 2, n.value, n.value), torch.float32)
+
+    def close(self):
+        if self.h:
+            call("csg_chain_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _tensor_from_ptr(addr: int, shape, dtype) -> torch.Tensor:
+    """Zero-copy torch view of library-owned device memory (valid while the
+    owning object lives)."""
+    n = int(np.prod(shape))
+    elem = torch.tensor([], dtype=dtype).element_size()
+
+    class _Holder:
+        __cuda_array_interface__ = {
+            "shape": tuple(shape), "typestr": {torch.float32: "<f4", torch.float64: "<f8"}[dtype],
+            "data": (addr, False), "version": 3, "strides": None,
+        }
+    del n, elem
+    return torch.as_tensor(_Holder(), device="cuda")
+
+
+class RegionContrast:
+    """regionContrast (regionContrast.cpp:89-205): region pixels of the output
+    geometry, mean (or max) of sum_{s,lambda} |E|^2 over the region divided by
+    the calibration maximum."""
+
+    def __init__(self, ctx: Context, n_out: int, out_pixel: float, loD: float, radius1: float,
+                 radius2: float, angle1: float = -180.0, angle2: float = 180.0,
+                 xlim1: float = -1e300, xlim2: float = 1e300):
+        x = -(out_pixel * n_out - out_pixel) / 2.0 + np.arange(n_out) * out_pixel
+        xx = np.broadcast_to(x[None, :], (n_out, n_out))
+        yy = np.broadcast_to(x[:, None], (n_out, n_out))
+        rr = np.sqrt(xx ** 2 + yy ** 2)
+        tt = np.arctan2(yy, xx)
+        sel = ((xx / loD >= xlim1) & (xx / loD <= xlim2) & (rr / loD >= radius1)
+               & (rr / loD <= radius2) & (tt > angle1 * math.pi / 180) & (tt < angle2 * math.pi / 180))
+        self.mask = sel
+        self.pix = dvec(np.flatnonzero(sel.ravel()).astype(np.int32), torch.int32)
+        self.ctx = ctx
+
+    def calibration_max(self, image: torch.Tensor) -> float:
+        _, mx = self.ctx.intensity(image)
+        self.ctx.sync()
+        return float(mx.item())
+
+    def contrast(self, image: torch.Tensor, per_group: int, calib_max: float, mode: int = 0):
+        return self.ctx.region_reduce(image, per_group, self.pix, mode=mode, scale=1.0 / calib_max)

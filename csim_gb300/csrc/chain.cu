@@ -1,0 +1,506 @@
+// Batched coronagraph executor: the reference's element walk
+// (coronagraph::execute, coronagraph.cpp:175-200) over a batch of fields,
+// each field one (wavelength, source, candidate) triple. Elements are added in
+// optical order; execute() launches each element once for the whole batch on
+// the context's stream, so the walk can be captured into a CUDA graph and
+// replayed (csg_chain_capture / csg_chain_replay).
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+
+extern "C" {
+int csg_mft_create(csg_ctx*, csg_mft**, int, int, int, int, const double*, const double*,
+                   const double*, const double*, int, const double*, const double*, double, int);
+int csg_mft_destroy(csg_mft*);
+int csg_mft_execute(csg_ctx*, csg_mft*, const float*, float*, int, const int*, int, const float*,
+                    const int*);
+int csg_mft_reserve(csg_mft*, int);
+int csg_mask_real(csg_ctx*, float*, int, int, int, const float*, int);
+int csg_phase_screen(csg_ctx*, float*, int, int, int, const float*, const double*, double);
+int csg_complex_mask(csg_ctx*, float*, int, int, int, const float*, const float*, int, int);
+int csg_fresnel(csg_ctx*, float*, int, int, const double*, double, double);
+int csg_point_source(csg_ctx*, float*, int, int, int, double, double, const double*,
+                     const double*, const double*);
+}
+
+namespace csg {
+int hex_mask_with_phasor_buffer(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S,
+                                int n_sub, const double* sags, int n_hex, int n_out,
+                                const int* cand, const double* lambda, double phase_sign, int flip,
+                                double subtract, int use_only_hex, float* out, float2* phasors);
+
+enum ElemKind { E_MASK, E_MIRROR, E_FRESNEL, E_CMASK, E_FPM_HEX, E_FRAUNHOFER };
+
+template <typename T>
+static T* dev_copy(const T* h, size_t n, cudaStream_t st) {
+  T* d = nullptr;
+  if (cudaMalloc(&d, n * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (h) cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, st);
+  return d;
+}
+
+static std::vector<double> pixel_centres(int n, double d, double shift = 0.0) {
+  // set_xy: -(n d - d)/2 + i d - origin (csim_geom.cpp:113-142)
+  std::vector<double> v(n);
+  for (int i = 0; i < n; ++i) v[i] = -(d * n - d) / 2.0 + i * d + shift;
+  return v;
+}
+
+struct Elem {
+  ElemKind kind;
+  std::string name;
+  int disable_for_calibration = 0;
+  // mask / mirror / complex mask
+  float* a = nullptr;
+  float* b = nullptr;
+  int mrows = 0, mcols = 0;
+  int quirk = 0;
+  double sign = 1.0;
+  // fresnel
+  double z = 0, ap_rad = 0;
+  // hex FPM
+  int16_t* hex_id = nullptr;
+  uint16_t* count = nullptr;
+  int S = 0, n_sub = 0, n_hex = 0;
+  double phase_sign = 1.0;
+  csg_mft* mft1 = nullptr;
+  csg_mft* mft2 = nullptr;
+  // fraunhofer
+  csg_mft* mft = nullptr;
+  int n_out = 0;
+};
+
+}  // namespace csg
+
+using namespace csg;
+
+struct csg_chain {
+  csg_ctx* ctx = nullptr;
+  int n = 0;
+  double dx = 0;
+  int n_lambda = 0;
+  std::vector<double> lambda;
+  int precision = 6;
+  std::vector<Elem> elems;
+  // batch description (device)
+  int n_fields = 0, cap_fields = 0;
+  int* slot = nullptr;          // wavelength index per field
+  double* lam_f = nullptr;      // wavelength per field
+  double* amp = nullptr;
+  double* tip = nullptr;
+  double* tilt = nullptr;
+  int* cand = nullptr;          // candidate per field
+  int* ident = nullptr;         // 0..F-1
+  // buffers
+  float* field = nullptr;       // [F][2][n][n]
+  float* fpm = nullptr;         // [F][2][S][S]
+  float* fpm_mask = nullptr;    // [F][2][S][S]
+  float2* phasors = nullptr;    // [F][n_hex+1]
+  float* image = nullptr;       // [F][2][n_out][n_out]
+  double* sags = nullptr;       // [n_cand][n_hex]
+  int n_cand = 0, sag_hex = 0;
+  size_t fpm_cap = 0, img_cap = 0, ph_cap = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graph_calib = -1;
+};
+
+static int ensure_buf(float** p, size_t& cap, size_t need) {
+  if (need <= cap) return CSG_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  cap = 0;
+  if (cudaMalloc(p, need) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("chain buffer allocation failed");
+    return CSG_E_NOMEM;
+  }
+  cap = need;
+  return CSG_OK;
+}
+
+static void drop_graph(csg_chain* c) {
+  if (c->exec) cudaGraphExecDestroy(c->exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->exec = nullptr;
+  c->graph = nullptr;
+  c->graph_calib = -1;
+}
+
+extern "C" {
+
+int csg_chain_create(csg_ctx* ctx, csg_chain** out, int n, double pixel_scale, int n_lambda,
+                     const double* lambda, int precision) {
+  CSG_CHECK(ctx && out && lambda, CSG_E_ARG, "csg_chain_create: null argument");
+  CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
+            "csg_chain_create: the field must be N x N with N a power of two in [64, 4096]");
+  CSG_CHECK(n_lambda > 0 && pixel_scale > 0, CSG_E_ARG, "csg_chain_create: bad parameters");
+  csg_chain* c = new csg_chain();
+  c->ctx = ctx;
+  c->n = n;
+  c->dx = pixel_scale;
+  c->n_lambda = n_lambda;
+  c->lambda.assign(lambda, lambda + n_lambda);
+  c->precision = precision;
+  *out = c;
+  return CSG_OK;
+}
+
+int csg_chain_destroy(csg_chain* c) {
+  if (!c) return CSG_OK;
+  DeviceGuard g(c->ctx->device);
+  cudaStreamSynchronize(c->ctx->stream);
+  drop_graph(c);
+  for (auto& e : c->elems) {
+    cudaFree(e.a);
+    cudaFree(e.b);
+    cudaFree(e.hex_id);
+    cudaFree(e.count);
+    csg_mft_destroy(e.mft1);
+    csg_mft_destroy(e.mft2);
+    csg_mft_destroy(e.mft);
+  }
+  for (void* p : {(void*)c->slot, (void*)c->lam_f, (void*)c->amp, (void*)c->tip, (void*)c->tilt,
+                  (void*)c->cand, (void*)c->ident, (void*)c->field, (void*)c->fpm,
+                  (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->sags})
+    cudaFree(p);
+  delete c;
+  return CSG_OK;
+}
+
+// mask element (mask.cpp:23-58): real mask N x N (host fp32), ref_quirk as
+// csg_mask_real.
+int csg_chain_add_mask(csg_chain* c, const float* mask, int ref_quirk, int disable_for_calibration) {
+  CSG_CHECK(c && mask, CSG_E_ARG, "csg_chain_add_mask: null argument");
+  DeviceGuard g(c->ctx->device);
+  Elem e;
+  e.kind = E_MASK;
+  e.quirk = ref_quirk;
+  e.disable_for_calibration = disable_for_calibration;
+  e.a = dev_copy(mask, (size_t)c->n * c->n, c->ctx->stream);
+  CSG_CHECK(e.a, CSG_E_NOMEM, "csg_chain_add_mask: allocation failed");
+  c->elems.push_back(e);
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// mirror element (mirror.cpp:23-72): sag N x N (host fp32, metres).
+int csg_chain_add_mirror(csg_chain* c, const float* sag, double sign) {
+  CSG_CHECK(c && sag, CSG_E_ARG, "csg_chain_add_mirror: null argument");
+  DeviceGuard g(c->ctx->device);
+  Elem e;
+  e.kind = E_MIRROR;
+  e.sign = sign;
+  e.a = dev_copy(sag, (size_t)c->n * c->n, c->ctx->stream);
+  CSG_CHECK(e.a, CSG_E_NOMEM, "csg_chain_add_mirror: allocation failed");
+  c->elems.push_back(e);
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// fresnelPropagator (fresnelPropagator.cpp:23-61, pad factor 1): z is the
+// signed distance, ap_rad the efield's arrayRadiusPhysical.
+int csg_chain_add_fresnel(csg_chain* c, double z, double ap_rad) {
+  CSG_CHECK(c && ap_rad > 0, CSG_E_ARG, "csg_chain_add_fresnel: bad argument");
+  Elem e;
+  e.kind = E_FRESNEL;
+  e.z = z;
+  e.ap_rad = ap_rad;
+  c->elems.push_back(e);
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// complexMask (complexMask.cpp:24-66): centred amp exp(-i ph), host fp32.
+int csg_chain_add_complex_mask(csg_chain* c, const float* amp, const float* ph, int mrows,
+                               int mcols, int disable_for_calibration) {
+  CSG_CHECK(c && amp && ph && mrows > 0 && mcols > 0 && mrows <= c->n && mcols <= c->n, CSG_E_ARG,
+            "csg_chain_add_complex_mask: bad argument");
+  DeviceGuard g(c->ctx->device);
+  Elem e;
+  e.kind = E_CMASK;
+  e.mrows = mrows;
+  e.mcols = mcols;
+  e.disable_for_calibration = disable_for_calibration;
+  e.a = dev_copy(amp, (size_t)mrows * mcols, c->ctx->stream);
+  e.b = dev_copy(ph, (size_t)mrows * mcols, c->ctx->stream);
+  CSG_CHECK(e.a && e.b, CSG_E_NOMEM, "csg_chain_add_complex_mask: allocation failed");
+  c->elems.push_back(e);
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// fpmPupToLyot with fpmIntHexCMCForPupToLyot (fpmPupToLyot.cpp:24-167,
+// 419-455) in matrix-Fourier form:
+//   E <- E + c MFT2[(fliplr(M) - 1) . MFT1[E]]
+// MFT1: pupil -> mask grid, kernel e^{+2 pi i xm x / lf'};
+// MFT2: mask grid -> pupil grid shifted by +dx/2, kernel e^{-2 pi i ...};
+// lf' = fRatioSign lambda focalRatio 2 beamRadius,
+// c = zoomFftSign dm^2 / (i lf') * dx^2 / (-i fRatioSign lf').
+// This is the reference's 2N circular-convolution operator exactly (the
+// convolution never wraps and fft_shift by N puts the kernel origin at +dx/2).
+// hex_id/count: host [3][S][S] tables; dm: mask pixel size (metres).
+int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* count, int S,
+                          int n_sub, int n_hex, double dm, double focal_ratio, double beam_radius,
+                          double f_ratio_sign, double zoom_fft_sign, double phase_sign,
+                          int disable_for_calibration) {
+  CSG_CHECK(c && hex_id && count, CSG_E_ARG, "csg_chain_add_fpm_hex: null argument");
+  CSG_CHECK(S >= 8 && S % 8 == 0 && n_sub > 0 && n_hex > 0, CSG_E_SHAPE,
+            "csg_chain_add_fpm_hex: S must be a multiple of 8");
+  DeviceGuard g(c->ctx->device);
+  cudaStream_t st = c->ctx->stream;
+  Elem e;
+  e.kind = E_FPM_HEX;
+  e.S = S;
+  e.n_sub = n_sub;
+  e.n_hex = n_hex;
+  e.phase_sign = phase_sign;
+  e.disable_for_calibration = disable_for_calibration;
+  e.hex_id = dev_copy(hex_id, (size_t)3 * S * S, st);
+  e.count = dev_copy(count, (size_t)3 * S * S, st);
+  CSG_CHECK(e.hex_id && e.count, CSG_E_NOMEM, "csg_chain_add_fpm_hex: allocation failed");
+  const int n = c->n, L = c->n_lambda;
+  std::vector<double> lf(L), pref1(2 * L), pref2(2 * L);
+  for (int l = 0; l < L; ++l) {
+    lf[l] = f_ratio_sign * c->lambda[l] * focal_ratio * 2.0 * beam_radius;
+    pref1[2 * l] = 1.0;
+    pref1[2 * l + 1] = 0.0;
+    // c = s dm^2/(i lf) * dx^2/(-i fr lf) = s dm^2 dx^2 / (fr lf^2)   (i * -i = 1)
+    pref2[2 * l] = zoom_fft_sign * dm * dm * c->dx * c->dx / (f_ratio_sign * lf[l] * lf[l]);
+    pref2[2 * l + 1] = 0.0;
+  }
+  std::vector<double> xp = pixel_centres(n, c->dx), xm = pixel_centres(S, dm);
+  std::vector<double> xps = pixel_centres(n, c->dx, c->dx / 2.0);
+  int rc = csg_mft_create(c->ctx, &e.mft1, n, n, S, S, xp.data(), xp.data(), xm.data(),
+                          xm.data(), L, lf.data(), pref1.data(), +1.0, c->precision);
+  if (rc) return rc;
+  rc = csg_mft_create(c->ctx, &e.mft2, S, S, n, n, xm.data(), xm.data(), xps.data(), xps.data(), L,
+                      lf.data(), pref2.data(), -1.0, c->precision);
+  if (rc) return rc;
+  c->elems.push_back(e);
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// fraunhoferFocal (fraunhoferFocal.cpp:23-72): zoomFft to n_out x n_out at
+// out_pixel, lambda f = lambda * lf_scale (lf_scale = 2 beamRadius
+// primaryfRatio), prefactor dx^2 / (i lambda f).
+int csg_chain_add_fraunhofer(csg_chain* c, int n_out, double out_pixel, double lf_scale) {
+  CSG_CHECK(c && n_out > 0 && out_pixel > 0 && lf_scale != 0, CSG_E_ARG,
+            "csg_chain_add_fraunhofer: bad argument");
+  DeviceGuard g(c->ctx->device);
+  Elem e;
+  e.kind = E_FRAUNHOFER;
+  e.n_out = n_out;
+  const int n = c->n, L = c->n_lambda;
+  std::vector<double> lf(L), pref(2 * L);
+  for (int l = 0; l < L; ++l) {
+    lf[l] = c->lambda[l] * lf_scale;
+    // dx dy / (i lf) = -i dx^2 / lf
+    pref[2 * l] = 0.0;
+    pref[2 * l + 1] = -c->dx * c->dx / lf[l];
+  }
+  std::vector<double> xi = pixel_centres(n, c->dx), xo = pixel_centres(n_out, out_pixel);
+  int rc = csg_mft_create(c->ctx, &e.mft, n, n, n_out, n_out, xi.data(), xi.data(), xo.data(),
+                          xo.data(), L, lf.data(), pref.data(), -1.0, c->precision);
+  if (rc) return rc;
+  c->elems.push_back(e);
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// Batch of n_fields fields: wavelength index, point-source amplitude
+// (sqrt(flux)) and tip/tilt (already times magnification), and the candidate
+// whose sags drive the hex FPM (efield.cpp:179-206, :295-304).
+int csg_chain_set_batch(csg_chain* c, int n_fields, const int* lambda_idx, const double* amp,
+                        const double* tip, const double* tilt, const int* cand) {
+  CSG_CHECK(c && lambda_idx && amp && tip && tilt && cand, CSG_E_ARG,
+            "csg_chain_set_batch: null argument");
+  CSG_CHECK(n_fields > 0 && n_fields < 65536, CSG_E_SHAPE, "csg_chain_set_batch: bad batch size");
+  for (int f = 0; f < n_fields; ++f)
+    CSG_CHECK(lambda_idx[f] >= 0 && lambda_idx[f] < c->n_lambda && cand[f] >= 0, CSG_E_ARG,
+              "csg_chain_set_batch: wavelength index or candidate out of range");
+  DeviceGuard g(c->ctx->device);
+  cudaStream_t st = c->ctx->stream;
+  CSG_CUDA(cudaStreamSynchronize(st));
+  if (n_fields > c->cap_fields) {
+    for (void* p : {(void*)c->slot, (void*)c->lam_f, (void*)c->amp, (void*)c->tip,
+                    (void*)c->tilt, (void*)c->cand, (void*)c->ident, (void*)c->field})
+      cudaFree(p);
+    c->slot = dev_copy<int>(nullptr, n_fields, st);
+    c->lam_f = dev_copy<double>(nullptr, n_fields, st);
+    c->amp = dev_copy<double>(nullptr, n_fields, st);
+    c->tip = dev_copy<double>(nullptr, n_fields, st);
+    c->tilt = dev_copy<double>(nullptr, n_fields, st);
+    c->cand = dev_copy<int>(nullptr, n_fields, st);
+    c->ident = dev_copy<int>(nullptr, n_fields, st);
+    c->field = dev_copy<float>(nullptr, (size_t)n_fields * 2 * c->n * c->n, st);
+    CSG_CHECK(c->slot && c->lam_f && c->amp && c->tip && c->tilt && c->cand && c->ident &&
+                  c->field,
+              CSG_E_NOMEM, "csg_chain_set_batch: allocation failed");
+    c->cap_fields = n_fields;
+  }
+  std::vector<double> lam(n_fields);
+  std::vector<int> id(n_fields);
+  for (int f = 0; f < n_fields; ++f) {
+    lam[f] = c->lambda[lambda_idx[f]];
+    id[f] = f;
+  }
+  CSG_CUDA(cudaMemcpyAsync(c->slot, lambda_idx, n_fields * sizeof(int), cudaMemcpyHostToDevice, st));
+  CSG_CUDA(cudaMemcpyAsync(c->lam_f, lam.data(), n_fields * sizeof(double), cudaMemcpyHostToDevice, st));
+  CSG_CUDA(cudaMemcpyAsync(c->amp, amp, n_fields * sizeof(double), cudaMemcpyHostToDevice, st));
+  CSG_CUDA(cudaMemcpyAsync(c->tip, tip, n_fields * sizeof(double), cudaMemcpyHostToDevice, st));
+  CSG_CUDA(cudaMemcpyAsync(c->tilt, tilt, n_fields * sizeof(double), cudaMemcpyHostToDevice, st));
+  CSG_CUDA(cudaMemcpyAsync(c->cand, cand, n_fields * sizeof(int), cudaMemcpyHostToDevice, st));
+  CSG_CUDA(cudaMemcpyAsync(c->ident, id.data(), n_fields * sizeof(int), cudaMemcpyHostToDevice, st));
+  CSG_CUDA(cudaStreamSynchronize(st));
+  c->n_fields = n_fields;
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// Device buffer of candidate sags [n_cand][n_hex] (FP64 metres), allocated on
+// first use; the caller (or the DE kernels) writes it in place.
+int csg_chain_sags(csg_chain* c, int n_cand, int n_hex, double** dev_sags) {
+  CSG_CHECK(c && dev_sags && n_cand > 0 && n_hex > 0, CSG_E_ARG, "csg_chain_sags: bad argument");
+  DeviceGuard g(c->ctx->device);
+  if (!c->sags || n_cand != c->n_cand || n_hex != c->sag_hex) {
+    cudaStreamSynchronize(c->ctx->stream);
+    cudaFree(c->sags);
+    c->sags = dev_copy<double>(nullptr, (size_t)n_cand * n_hex, c->ctx->stream);
+    CSG_CHECK(c->sags, CSG_E_NOMEM, "csg_chain_sags: allocation failed");
+    CSG_CUDA(cudaMemsetAsync(c->sags, 0, sizeof(double) * n_cand * n_hex, c->ctx->stream));
+    c->n_cand = n_cand;
+    c->sag_hex = n_hex;
+    drop_graph(c);
+  }
+  *dev_sags = c->sags;
+  return CSG_OK;
+}
+
+static int prepare(csg_chain* c) {
+  const size_t F = (size_t)c->n_fields;
+  size_t fpm_need = 0, ph_need = 0, img_need = 0;
+  for (auto& e : c->elems) {
+    if (e.kind == E_FPM_HEX) {
+      fpm_need = std::max(fpm_need, F * 2 * e.S * e.S * sizeof(float));
+      ph_need = std::max(ph_need, F * (e.n_hex + 1) * sizeof(float2));
+      int rc = csg_mft_reserve(e.mft1, c->n_fields);
+      if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
+      if (rc) return rc;
+    } else if (e.kind == E_FRAUNHOFER) {
+      img_need = std::max(img_need, F * 2 * e.n_out * e.n_out * sizeof(float));
+      int rc = csg_mft_reserve(e.mft, c->n_fields);
+      if (rc) return rc;
+    }
+  }
+  size_t mask_cap = c->fpm_cap;
+  int rc = ensure_buf(&c->fpm, c->fpm_cap, fpm_need);
+  if (!rc) rc = ensure_buf(&c->fpm_mask, mask_cap, fpm_need);
+  if (!rc) rc = ensure_buf(reinterpret_cast<float**>(&c->phasors), c->ph_cap, ph_need);
+  if (!rc) rc = ensure_buf(&c->image, c->img_cap, img_need);
+  return rc;
+}
+
+static int run_walk(csg_chain* c, int calibrating) {
+  csg_ctx* ctx = c->ctx;
+  const int F = c->n_fields, n = c->n;
+  int rc = csg_point_source(ctx, c->field, F, n, n, c->dx, c->dx, c->amp, c->tip, c->tilt);
+  if (rc) return rc;
+  for (auto& e : c->elems) {
+    if (calibrating && e.disable_for_calibration) continue;
+    switch (e.kind) {
+      case E_MASK:
+        rc = csg_mask_real(ctx, c->field, F, n, n, e.a, e.quirk);
+        break;
+      case E_MIRROR:
+        rc = csg_phase_screen(ctx, c->field, F, n, n, e.a, c->lam_f, e.sign);
+        break;
+      case E_FRESNEL:
+        rc = csg_fresnel(ctx, c->field, F, n, c->lam_f, e.ap_rad, e.z);
+        break;
+      case E_CMASK:
+        rc = csg_complex_mask(ctx, c->field, F, n, n, e.a, e.b, e.mrows, e.mcols);
+        break;
+      case E_FPM_HEX:
+        CSG_CHECK(c->sags && c->sag_hex == e.n_hex, CSG_E_STATE,
+                  "hex FPM: candidate sags not set (csg_chain_sags) or wrong hex count");
+        // (fliplr(M) - 1) for each field's (candidate, wavelength)
+        rc = hex_mask_with_phasor_buffer(ctx, e.hex_id, e.count, e.S, e.n_sub, c->sags, e.n_hex,
+                                         F, c->cand, c->lam_f, e.phase_sign, 1, 1.0, -1,
+                                         c->fpm_mask, c->phasors);
+        if (!rc) rc = csg_mft_execute(ctx, e.mft1, c->field, c->fpm, F, c->slot, 0, nullptr,
+                                      nullptr);
+        if (!rc) rc = csg_mft_execute(ctx, e.mft2, c->fpm, c->field, F, c->slot, 1, c->fpm_mask,
+                                      c->ident);
+        break;
+      case E_FRAUNHOFER:
+        rc = csg_mft_execute(ctx, e.mft, c->field, c->image, F, c->slot, 0, nullptr, nullptr);
+        break;
+    }
+    if (rc) return rc;
+  }
+  return CSG_OK;
+}
+
+// Run the element walk on the current batch. calibrating != 0 skips every
+// element added with disable_for_calibration (the reference's calibration
+// propagation, regionContrast.cpp:124-143). use_graph != 0 captures the walk
+// into a CUDA graph on first use and replays it afterwards.
+int csg_chain_execute(csg_chain* c, int calibrating, int use_graph) {
+  CSG_CHECK(c, CSG_E_ARG, "csg_chain_execute: null chain");
+  CSG_CHECK(c->n_fields > 0, CSG_E_STATE, "csg_chain_execute: no batch (csg_chain_set_batch)");
+  DeviceGuard g(c->ctx->device);
+  int rc = prepare(c);
+  if (rc) return rc;
+  if (!use_graph) return run_walk(c, calibrating);
+  CSG_CHECK(c->ctx->stream != nullptr, CSG_E_STATE,
+            "csg_chain_execute: graph capture needs a non-default stream");
+  if (c->exec && c->graph_calib != calibrating) drop_graph(c);
+  if (!c->exec) {
+    rc = run_walk(c, calibrating);  // warm-up: first-use allocations happen outside capture
+    if (rc) return rc;
+    CSG_CUDA(cudaStreamSynchronize(c->ctx->stream));
+    CSG_CUDA(cudaStreamBeginCapture(c->ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = run_walk(c, calibrating);
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->ctx->stream, &gr);
+    if (rc) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    CSG_CHECK(e == cudaSuccess, CSG_E_CUDA,
+              std::string("graph capture: ") + cudaGetErrorString(e));
+    c->graph = gr;
+    CSG_CUDA(cudaGraphInstantiate(&c->exec, gr, 0));
+    c->graph_calib = calibrating;
+  }
+  CSG_CUDA(cudaGraphLaunch(c->exec, c->ctx->stream));
+  return CSG_OK;
+}
+
+// Final-plane field of the batch: [F][2][n_out][n_out] fp32 on the device.
+int csg_chain_image(csg_chain* c, float** dev_image, int* n_out) {
+  CSG_CHECK(c && dev_image && n_out, CSG_E_ARG, "csg_chain_image: null argument");
+  *dev_image = c->image;
+  *n_out = 0;
+  for (auto& e : c->elems)
+    if (e.kind == E_FRAUNHOFER) *n_out = e.n_out;
+  return CSG_OK;
+}
+
+// Pupil-plane working field [F][2][n][n] (the field before the final MFT).
+int csg_chain_field(csg_chain* c, float** dev_field) {
+  CSG_CHECK(c && dev_field, CSG_E_ARG, "csg_chain_field: null argument");
+  *dev_field = c->field;
+  return CSG_OK;
+}
+
+}  // extern "C"

@@ -234,6 +234,23 @@ __global__ void k_intensity(const float* __restrict__ field, long long plane, in
   if (threadIdx.x == 0 && out_max) atomicMax(out_max, (unsigned long long)__double_as_longlong(m));
 }
 
+// Hex mask with a caller-provided phasor buffer [n_out][n_hex + 1] (used by
+// the chain executor, which owns that buffer).
+int hex_mask_with_phasor_buffer(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S,
+                                int n_sub, const double* sags, int n_hex, int n_out,
+                                const int* cand, const double* lambda, double phase_sign, int flip,
+                                double subtract, int use_only_hex, float* out, float2* phasors) {
+  cudaStream_t st = ctx->stream;
+  k_hex_phasors<<<grid_for((long long)n_out * (n_hex + 1), 256), 256, 0, st>>>(
+      phasors, sags, n_hex, n_out, cand, lambda, phase_sign);
+  CSG_LAUNCH_CHECK();
+  k_hex_mask<<<grid_for((long long)S * S * n_out, 256), 256, 0, st>>>(
+      hex_id, count, S, 1.f / (float)(n_sub * n_sub), phasors, n_hex, n_out, flip,
+      (float)subtract, use_only_hex, out);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
 }  // namespace csg
 
 using namespace csg;
@@ -288,21 +305,6 @@ int csg_complex_mask(csg_ctx* ctx, float* field, int n_fields, int rows, int col
   DeviceGuard g(ctx->device);
   k_complex_mask<<<grid_for((long long)mrows * mcols * n_fields, 256), 256, 0, ctx->stream>>>(
       field, n_fields, rows, cols, amp, ph, mrows, mcols);
-  CSG_LAUNCH_CHECK();
-  return CSG_OK;
-}
-
-int hex_mask_with_phasor_buffer(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S,
-                                int n_sub, const double* sags, int n_hex, int n_out,
-                                const int* cand, const double* lambda, double phase_sign, int flip,
-                                double subtract, int use_only_hex, float* out, float2* phasors) {
-  cudaStream_t st = ctx->stream;
-  k_hex_phasors<<<grid_for((long long)n_out * (n_hex + 1), 256), 256, 0, st>>>(
-      phasors, sags, n_hex, n_out, cand, lambda, phase_sign);
-  CSG_LAUNCH_CHECK();
-  k_hex_mask<<<grid_for((long long)S * S * n_out, 256), 256, 0, st>>>(
-      hex_id, count, S, 1.f / (float)(n_sub * n_sub), phasors, n_hex, n_out, flip,
-      (float)subtract, use_only_hex, out);
   CSG_LAUNCH_CHECK();
   return CSG_OK;
 }

@@ -254,6 +254,14 @@ int csg_mft_destroy(csg_mft* m) {
   return CSG_OK;
 }
 
+int csg_mft_reserve(csg_mft* m, int n_fields) {
+  CSG_CHECK(m && n_fields > 0, CSG_E_ARG, "csg_mft_reserve: bad argument");
+  DeviceGuard g(m->ctx->device);
+  int rc = m->split_in.ensure((size_t)n_fields * 12 * m->ny * m->nx);
+  if (!rc) rc = m->tt.ensure((size_t)n_fields * 12 * m->no * m->ny);
+  return rc;
+}
+
 size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
   if (!m) return 0;
   return (size_t)n_fields * 12 * ((size_t)m->ny * m->nx + (size_t)m->no * m->ny);

@@ -169,12 +169,78 @@ int csg_hex_mask(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int
                  const double* sags, int n_hex, int n_out, const int* cand, const double* lambda,
                  double phase_sign, int flip, double subtract, int use_only_hex, float* out);
 /* Build the interpolation tables on the GPU (complexHexMaskFPM.cpp:317-469,
- * make_hex_array + make_interpolation_data). centres in hex-step units
- * (hex_x, hex_y), design array A x A, mask S x S at pixel_scale. */
+ * make_hex_array + make_interpolation_data). Hex centres (hex_x, hex_y,
+ * device FP64) are in hex-step units; `pitch` is the centre distance of
+ * neighbouring hexes in those units (sqrt(3) for the reference's own
+ * layout, complexHexMaskFPM.cpp:236-315, which reproduces its hexRadius
+ * formula exactly). Design array A x A, mask S x S at pixel_scale, n_sub^2
+ * samples per mask pixel. Where hexes overlap the highest index wins; a
+ * fourth distinct hex in one pixel is counted as outside and reported in
+ * *n_overflow (the reference asserts). Synchronous. */
 int csg_hex_tables(csg_ctx* ctx, const double* hex_x, const double* hex_y, int n_hex,
                    int n_rings, int design_size, double fpm_scale_factor, double hex_gap,
-                   int S, int n_sub, double pixel_scale, double fpm_radius, int16_t* hex_id,
-                   uint16_t* count);
+                   double pitch, int S, int n_sub, double pixel_scale, double fpm_radius,
+                   int16_t* hex_id, uint16_t* count, int* n_overflow);
+
+/* ------------------------------------------------- coronagraph chain */
+/* Batched element walk: coronagraph::init (coronagraph.cpp:50-168) builds the
+ * element list; coronagraph::execute (coronagraph.cpp:175-200) runs it. Here
+ * the list is built with the csg_chain_add_* calls (in optical order) and one
+ * csg_chain_execute runs every element once over a whole batch of fields,
+ * each field one (wavelength, source, candidate) triple. The field is
+ * N x N (N a power of two) at pixel_scale metres; lambda[n_lambda] are the
+ * efield's wavelengths (efield.cpp:351-417). `precision` is CSG_PREC_*. */
+int csg_chain_create(csg_ctx* ctx, csg_chain** chain, int n, double pixel_scale, int n_lambda,
+                     const double* lambda, int precision);
+int csg_chain_destroy(csg_chain* chain);
+/* mask (mask.cpp:23-58): host fp32 N x N; ref_quirk as csg_mask_real.
+ * disable_for_calibration as celem's flag (celem.cpp:63-130). */
+int csg_chain_add_mask(csg_chain* chain, const float* mask, int ref_quirk,
+                       int disable_for_calibration);
+/* mirror (mirror.cpp:23-72): host fp32 sag N x N in metres, mirrorSign. */
+int csg_chain_add_mirror(csg_chain* chain, const float* sag, double sign);
+/* fresnelPropagator (fresnelPropagator.cpp:23-61, no padding): z =
+ * propagationSign |next.position - prev.position|, ap_rad = the efield's
+ * arrayRadiusPhysical (efield.cpp:419-430). */
+int csg_chain_add_fresnel(csg_chain* chain, double z, double ap_rad);
+/* complexMask (complexMask.cpp:24-66): centred amp exp(-i ph), host fp32. */
+int csg_chain_add_complex_mask(csg_chain* chain, const float* amp, const float* ph, int mrows,
+                               int mcols, int disable_for_calibration);
+/* fpmPupToLyot + fpmIntHexCMCForPupToLyot + complexHexMaskFPM
+ * (fpmPupToLyot.cpp:24-167, 419-455; complexHexMaskFPM.cpp:44-99) in
+ * matrix-Fourier Babinet form, algebraically identical to the reference's
+ * 2N circular convolution:
+ *   E <- E + c MFT2[(fliplr(M_cand,lambda) - 1) MFT1[E]]
+ * lf' = fRatioSign lambda focalRatio 2 beamRadius, mask pixel dm (the hex
+ * mask's pixelScale), c = zoomFftSign dm^2 dx^2 / (fRatioSign lf'^2).
+ * Tables (host) as csg_hex_mask; candidate sags come from csg_chain_sags. */
+int csg_chain_add_fpm_hex(csg_chain* chain, const int16_t* hex_id, const uint16_t* count, int S,
+                          int n_sub, int n_hex, double dm, double focal_ratio, double beam_radius,
+                          double f_ratio_sign, double zoom_fft_sign, double phase_sign,
+                          int disable_for_calibration);
+/* fraunhoferFocal (fraunhoferFocal.cpp:23-72): zoomFft to n_out x n_out at
+ * out_pixel (= loD / samplesPerflD), lambda f = lambda lf_scale with
+ * lf_scale = 2 beamRadius primaryfRatio. Must be the last element. */
+int csg_chain_add_fraunhofer(csg_chain* chain, int n_out, double out_pixel, double lf_scale);
+/* The batch: per field the wavelength index, point-source amplitude
+ * (sqrt(flux)), tip and tilt (times magnification), and candidate index. */
+int csg_chain_set_batch(csg_chain* chain, int n_fields, const int* lambda_idx, const double* amp,
+                        const double* tip, const double* tilt, const int* cand);
+/* Device FP64 buffer [n_cand][n_hex] of candidate FPM sags, written in place
+ * by the caller or the DE kernels (complexHexMaskFPM set_optimization_data,
+ * complexHexMaskFPM.cpp:176-191). */
+int csg_chain_sags(csg_chain* chain, int n_cand, int n_hex, double** dev_sags);
+/* Run the walk (calibrating != 0 skips disable_for_calibration elements, the
+ * calibration propagation of regionContrast.cpp:124-143); use_graph != 0
+ * captures a CUDA graph on first use and replays it on later calls. */
+int csg_chain_execute(csg_chain* chain, int calibrating, int use_graph);
+/* Device pointers to the final image fields [F][2][n_out][n_out] and to the
+ * working pupil-plane fields [F][2][N][N]. */
+int csg_chain_image(csg_chain* chain, float** dev_image, int* n_out);
+int csg_chain_field(csg_chain* chain, float** dev_field);
+/* Pre-size an MFT plan's scratch for n_fields (so graph capture allocates
+ * nothing). */
+int csg_mft_reserve(csg_mft* plan, int n_fields);
 
 /* ---------------------------------------------------- intensity / contrast */
 /* regionContrast::compute_intensity (regionContrast.cpp:124-143) and the
