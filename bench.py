@@ -1,0 +1,339 @@
+"""Field-propagation throughput of the PIAACMC-style 1024^2 chain on GB300.
+
+One step = one batch of B fields (default 64 FPM candidates, lambda = 650 nm,
+on-axis source), each propagated through the full element walk
+(pupil mask -> PIAA M1 -> Fresnel 1 m -> PIAA M2 -> 217-hex FPM via
+512^2 MFT at 1/16 lambda/D (Babinet) -> Lyot 0.95 -> 256^2 MFT at
+0.25 lambda/D) and reduced to the 2-8 lambda/D dark-hole contrast of every
+candidate. Metric: field propagations per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun each rank runs its own batch (candidates are independent:
+weak scaling, no data-path collective); timing is the max over ranks.
+`--impl reference` times the reference-semantics CPU restatement of the same
+path (the reference itself needs FFTW/Armadillo/cfitsio, absent here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("piaacmc-1024: pupil + PIAA M1/M2 (even poly, PV 2um) + Fresnel 1.0 m + "
+            "217-hex FPM (8 rings, U(+-0.5um)) via 512^2 MFT at 1/16 lambda/D, Babinet + "
+            "Lyot 0.95 + 256^2 MFT at 0.25 lambda/D + 2-8 lambda/D contrast")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops_sustained"]), "measured"
+    except Exception:
+        return 6800.0, 1700.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [l.strip().split(", ") for l in open(self.path) if l.strip()]
+        os.unlink(self.path)
+        if not rows:
+            return None
+        def mhz(v):
+            try:
+                return float(v.split()[0])
+            except Exception:
+                return float("nan")
+        sm = [mhz(r[1]) for r in rows if len(r) > 8]
+        mx = [mhz(r[2]) for r in rows if len(r) > 8]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ CPU
+def cpu_fields_per_s(spec, inp, sags, budget_s: float, max_fields: int):
+    """Reference-semantics CPU restatement (FP64, scipy/pocketfft + BLAS, all
+    host threads) of the same per-field path: the reference's own
+    fpmPupToLyot algorithm (mask hat by chirp-Z zoom + 2N x 2N FFT
+    convolution, recomputed for every candidate's mask)."""
+    from oracle import chain as oc
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_fields and (time.perf_counter() - t0) < budget_s:
+        oc.piaacmc_field(inp, spec, float(inp["lam"][0]), 1.0, 0.0, 0.0, sags[n % len(sags)],
+                         conv_form=True, czt=True)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt
+
+
+def reference_arm(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    from csim_gb300.synth import PiaacmcSpec
+    from oracle.chain import host_inputs
+    spec = PiaacmcSpec()
+    inp = host_inputs(spec)
+    rng = np.random.default_rng(7)
+    sags = rng.uniform(-spec.sag_range, spec.sag_range, (8, spec.n_hex))
+    per_step = 2
+    for _ in range(args.warmup):
+        cpu_fields_per_s(spec, inp, sags, 1e9, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_fields_per_s(spec, inp, sags, 1e9, per_step)
+    dt = time.perf_counter() - t0
+    v = per_step * args.steps / dt
+    cores = os.cpu_count()
+    line = {"metric": "field propagations/s", "value": v, "unit": "fields/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "fields_per_step": per_step},
+            "cpu_baseline": {"value": v, "unit": "fields/s", "cores": cores, "kind": "port",
+                             "sample": f"{per_step} fields per step x {args.steps} steps"},
+            "e2e": {"value": v, "unit": "fields/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--fields", type=int, default=64)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    import ctypes as C
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from csim_gb300 import _lib
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import workloads as W
+    from csim_gb300.runtime import Context, ptr
+
+    ctx = Context(local)
+    stream = torch.cuda.Stream(local)
+    ctx.bind_stream(stream)
+    spec = W.PiaacmcSpec()
+    B = args.fields
+    with torch.cuda.stream(stream):
+        cor, inp = W.build_piaacmc(ctx, spec, precision=args.precision)
+        rng = np.random.default_rng(100 + rank)
+        sags_h = W.random_sags(rng, B, spec.n_hex, spec.sag_range)
+        sags_d = cor.sags(B)
+        sags_d.copy_(torch.as_tensor(sags_h))
+        # calibration (FPM removed) for the contrast normaliser
+        cor.batch_all(1)
+        cal = cor.execute(calibrating=True)
+        reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 2.0, 8.0)
+        cmax = reg.calibration_max(cal)
+        cor.batch_all(B)
+        contrast = torch.empty(B, dtype=torch.float64, device="cuda")
+
+        def step():
+            img = cor.execute(calibrating=False, use_graph=True)
+            ctx.region_reduce(img, 1, reg.pix, mode=0, scale=1.0 / cmax, out=contrast)
+            return img
+
+        # kernels per step (graph replays launch the same kernels)
+        n0 = _lib.api["csg_launch_count"]()
+        cor.execute(calibrating=False, use_graph=False)
+        ctx.region_reduce(cor.execute(use_graph=False), 1, reg.pix, mode=0, scale=1.0 / cmax,
+                          out=contrast)
+        n1 = _lib.api["csg_launch_count"]()
+        launches_per_step = (n1 - n0) // 2
+        for _ in range(args.warmup):
+            step()
+        ctx.sync()
+
+    hbm_peak, tc_peak, peak_kind = peaks()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ctx.sync()
+    value = B * args.steps * ws / (ms / 1e3)
+
+    # ---- e2e through the C ABI with host buffers (pinned), every step:
+    # H2D of the candidates' sags, the walk, the contrast, D2H of the final
+    # image fields and the contrasts.
+    img0 = cor.execute(use_graph=True)
+    host_sags = torch.as_tensor(sags_h).pin_memory()
+    host_img = torch.empty(img0.shape, dtype=torch.float32).pin_memory()
+    host_con = torch.empty(B, dtype=torch.float64).pin_memory()
+    h2d = host_sags.numel() * 8
+    d2h = host_img.numel() * 4 + B * 8
+    with torch.cuda.stream(stream):
+        def e2e_step():
+            _lib.call("csg_memcpy_h2d", ctx.h, C.c_void_p(sags_d.data_ptr()),
+                      C.c_void_p(host_sags.data_ptr()), h2d)
+            img = step()
+            _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_img.data_ptr()),
+                      C.c_void_p(img.data_ptr()), host_img.numel() * 4)
+            _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_con.data_ptr()),
+                      C.c_void_p(contrast.data_ptr()), B * 8)
+        for _ in range(3):
+            e2e_step()
+        ctx.sync()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        ctx.sync()
+        e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = B * args.steps * ws / e2e_s
+
+    # ---- dominant kernel, timed live with CUDA events on its stream
+    with torch.cuda.stream(stream):
+        _lib.call("csg_profile", ctx.h, 1)
+        for _ in range(3):
+            cor.execute(use_graph=False)
+        buf = C.create_string_buffer(1 << 16)
+        _lib.call("csg_profile_report", ctx.h, buf, len(buf))
+        _lib.call("csg_profile", ctx.h, 0)
+    prof = json.loads(buf.value.decode())
+    g = prof.get("mft_gemm", {"count": 1, "ms": float("nan"), "flops": 0.0})
+    gemm_tflops = g["flops"] / (g["ms"] / 1e3) / 1e12
+    total_ms = sum(v["ms"] for v in prof.values())
+    split_terms = args.precision
+    roofline = {"bound": "tensor", "kernel": "k_split_gemm (tcgen05 split-bf16 MFT)",
+                "achieved": gemm_tflops, "peak": tc_peak, "unit": "TFLOP/s",
+                "frac": gemm_tflops / tc_peak, "peak_kind": f"{peak_kind} bf16 sustained",
+                "traffic": TRAFFIC.get(B),
+                "algorithmic_flops_per_launch": g["flops"] / g["count"],
+                "avg_launch_ms": g["ms"] / g["count"],
+                "executed_bf16_tflops": gemm_tflops * split_terms,
+                "share_of_step": g["ms"] / total_ms if total_ms else None,
+                "kernels": {k: {"count": v["count"], "ms": round(v["ms"], 4)} for k, v in prof.items()}}
+    if "fresnel_3pass" in prof:
+        fz = prof["fresnel_3pass"]
+        roofline["fresnel_gbs"] = fz["bytes"] / (fz["ms"] / 1e3) / 1e9
+        roofline["fresnel_frac_hbm"] = roofline["fresnel_gbs"] / hbm_peak
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        v, n, dt = cpu_fields_per_s(spec, inp, sags_h, 15.0, 32)
+        cpu = {"value": v, "unit": "fields/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n} fields of the same workload in {dt:.1f} s (FP64, reference "
+                         "algorithm: chirp-Z mask hat + 2048^2 FFT convolution)"}
+
+    line = {"metric": "field propagations/s", "value": value, "unit": "fields/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 fields, bf16x%d-split tensor-core MFT, f64 phases" % args.precision,
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "fields_per_step": B, "n": spec.n, "fpm_grid": spec.S,
+                       "n_hex": spec.n_hex, "image": cor.n_out, "precision": f"bf16x{args.precision}",
+                       "l2": "working set > L2 (fields + MFT operands ~1.5 GB per step)",
+                       "parallelism": f"candidates sharded over {ws} rank(s)"},
+            "e2e": {"value": e2e_value, "unit": "fields/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": roofline, "clocks": clk, "cpu_baseline": cpu,
+            "contrast_sample": float(contrast[0].item())}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum per k_split_gemm launch from the
+# committed ncu capture (see profiles/), keyed by fields per step; None until
+# captured.
+TRAFFIC: dict = {}
+
+if __name__ == "__main__":
+    sys.exit(main())

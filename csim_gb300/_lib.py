@@ -49,6 +49,9 @@ SIGNATURES = {
     "csg_memcpy_d2h": ([P, P, P, SZ], None),
     "csg_memset": ([P, P, I, SZ], None),
     "csg_version": ([], C.c_char_p),
+    "csg_launch_count": ([], C.c_ulonglong),
+    "csg_profile": ([P, I], None),
+    "csg_profile_report": ([P, C.c_char_p, SZ], None),
     "csg_field_upload": ([P, P, I, I, I, I, P, P], None),
     "csg_field_download": ([P, P, I, I, I, P, P, I], None),
     "csg_point_source": ([P, P, I, I, I, D, D, P, P, P], None),

@@ -21,47 +21,7 @@ from ._lib import CSG_PREC_BF16X6, call
 from .runtime import Context, dvec, ptr
 
 
-@dataclass
-class Telescope:
-    """telescope.cpp:21-60."""
-    primaryDiameter: float
-    primaryfRatio: float
-    magnification: float = 1.0
-
-    @property
-    def primaryfLength(self) -> float:
-        return self.primaryfRatio * self.primaryDiameter
-
-    def compute_loD(self, lam: float) -> float:
-        return self.magnification * self.primaryfLength * lam / self.primaryDiameter
-
-
-@dataclass
-class PointSource:
-    """efield pointSource: flux (amplitude sqrt(flux)), tip/tilt in the
-    reference's units (multiplied by the telescope magnification)."""
-    flux: float = 1.0
-    tip: float = 0.0
-    tilt: float = 0.0
-
-
-@dataclass
-class EField:
-    """efield.cpp: square N x N array, beam radius and pixel scale (metres)."""
-    n: int
-    beamRadiusPhysical: float
-    pixelScale: float
-    wavelengths: np.ndarray
-    sources: list = field(default_factory=lambda: [PointSource()])
-
-    @property
-    def arrayRadiusPhysical(self) -> float:
-        beam_px = math.ceil(2 * self.beamRadiusPhysical / self.pixelScale)
-        return self.beamRadiusPhysical * self.n / beam_px
-
-    def pixel_centres(self) -> np.ndarray:
-        d = self.pixelScale
-        return -(d * self.n - d) / 2.0 + np.arange(self.n) * d
+from .synth import EField, PointSource, Telescope  # noqa: E402,F401
 
 
 # ------------------------------------------------------------- elements

@@ -11,6 +11,9 @@ static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
 const char* get_error() { return g_last_error.c_str(); }
 
+std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 // Convert host complex<double> (interleaved, staged on device) to planar fp32.
 // src: FP64 interleaved; colmajor: element (r, c, f) at r + c R + f R C.
 __global__ void k_c128_to_c32p(const double2* __restrict__ src, float* __restrict__ dst, int R,
@@ -53,6 +56,54 @@ using namespace csg;
 extern "C" {
 
 const char* csg_version(void) { return "csim_gb300 0.1 (sm_103a)"; }
+
+unsigned long long csg_launch_count(void) { return g_launches.load(); }
+
+int csg_profile(csg_ctx* c, int enable) {
+  CSG_CHECK(c != nullptr, CSG_E_ARG, "csg_profile: null context");
+  c->prof = enable != 0;
+  if (enable) {
+    c->acc.clear();
+    for (auto& p : c->pending) {
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+    c->pending.clear();
+  }
+  return CSG_OK;
+}
+
+int csg_profile_report(csg_ctx* c, char* buf, size_t len) {
+  CSG_CHECK(c && buf && len > 0, CSG_E_ARG, "csg_profile_report: bad argument");
+  DeviceGuard g(c->device);
+  CSG_CUDA(cudaStreamSynchronize(c->stream));
+  for (auto& p : c->pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    auto& a = c->acc[p.name];
+    a.count += 1;
+    a.ms += ms;
+    a.flops += p.flops;
+    a.bytes += p.bytes;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  c->pending.clear();
+  std::string s = "{";
+  bool first = true;
+  for (auto& kv : c->acc) {
+    char tmp[256];
+    snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"count\": %lld, \"ms\": %.6f, \"flops\": %.6e, \"bytes\": %.6e}",
+             first ? "" : ", ", kv.first.c_str(), kv.second.count, kv.second.ms, kv.second.flops,
+             kv.second.bytes);
+    s += tmp;
+    first = false;
+  }
+  s += "}";
+  CSG_CHECK(s.size() + 1 <= len, CSG_E_ARG, "csg_profile_report: buffer too small");
+  memcpy(buf, s.c_str(), s.size() + 1);
+  return CSG_OK;
+}
 
 const char* csg_last_error(void) { return get_error(); }
 

@@ -34,6 +34,7 @@ const char* get_error();
 
 #define CSG_LAUNCH_CHECK()                                                      \
   do {                                                                          \
+    ::csg::count_launch();                                                      \
     cudaError_t e_ = cudaGetLastError();                                        \
     if (e_ != cudaSuccess) {                                                    \
       ::csg::set_error(std::string("kernel launch: ") + cudaGetErrorString(e_)); \
@@ -41,9 +42,8 @@ const char* get_error();
     }                                                                           \
   } while (0)
 
-// Device status word: kernels that give up on a bounded wait record a code
-// here; csg_sync() reads it back and reports CSG_E_TIMEOUT.
-int* device_status(int device);
+// Counts kernel launches made by the library (csg_launch_count).
+void count_launch();
 
 // ~1 s at 2 GHz: no legitimate wait inside a kernel comes close.
 constexpr long long kWaitBudgetCycles = 2000000000LL;

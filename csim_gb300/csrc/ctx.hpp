@@ -7,6 +7,25 @@
 
 #include "common.cuh"
 
+#include <atomic>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace csg {
+struct ProfPending {
+  std::string name;
+  cudaEvent_t a, b;
+  double flops, bytes;
+};
+struct ProfAcc {
+  long long count = 0;
+  double ms = 0, flops = 0, bytes = 0;
+};
+// Kernel launches made by the library's host code (all contexts).
+extern std::atomic<unsigned long long> g_launches;
+}  // namespace csg
+
 struct csg_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
@@ -14,9 +33,42 @@ struct csg_ctx {
   int* status = nullptr;            // device int, 0 = ok
   std::set<void*> allocations;
   int sm_count = 0;
+  // opt-in per-kernel timing (CUDA events on the launching stream)
+  bool prof = false;
+  std::vector<csg::ProfPending> pending;
+  std::map<std::string, csg::ProfAcc> acc;
 };
 
 namespace csg {
+
+// Records CUDA events around the launches inside its scope when profiling is
+// on (never inside graph capture: csg_profile refuses while capturing).
+struct ProfScope {
+  csg_ctx* c;
+  ProfPending p;
+  bool on;
+  ProfScope(csg_ctx* ctx, const char* name, double flops = 0, double bytes = 0)
+      : c(ctx), on(ctx && ctx->prof) {
+    if (!on) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(ctx->stream, &cs);
+    if (cs != cudaStreamCaptureStatusNone) {
+      on = false;
+      return;
+    }
+    p.name = name;
+    p.flops = flops;
+    p.bytes = bytes;
+    cudaEventCreate(&p.a);
+    cudaEventCreate(&p.b);
+    cudaEventRecord(p.a, ctx->stream);
+  }
+  ~ProfScope() {
+    if (!on) return;
+    cudaEventRecord(p.b, c->stream);
+    c->pending.push_back(p);
+  }
+};
 
 // RAII guard that makes the context's device current for the call.
 struct DeviceGuard {

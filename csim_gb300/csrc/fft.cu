@@ -268,6 +268,10 @@ int fft2d_launch(csg_ctx* ctx, float* field, int F, int n, int direction, const 
   int rc;
   const bool inv = direction > 0;
   const float inv_scale = 1.f / ((float)n * (float)n);
+  // one compulsory read + write of the planar fp32 field per pass
+  const double pass_bytes = (double)F * n * n * 16.0;
+  ProfScope ps(ctx, fresnel ? "fresnel_3pass" : "fft2d_2pass", 0,
+               pass_bytes * (fresnel ? 3.0 : 2.0));
   if (!fresnel) {
     if (!inv) {
       if ((rc = prep_smem(k_fft_rows<false>, rsm))) return rc;

@@ -280,9 +280,13 @@ int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n
   auto* sin = static_cast<__nv_bfloat16*>(m->split_in.ptr);
   auto* tt = static_cast<__nv_bfloat16*>(m->tt.ptr);
 
-  k_split_field<<<grid_for((long long)n_fields * m->ny * m->nx, 256), 256, 0, st>>>(
-      in, sin, m->ny, m->nx, n_fields, in_mul, mul_idx);
-  CSG_LAUNCH_CHECK();
+  const double F = n_fields;
+  {
+    ProfScope ps(ctx, "mft_split", 0, F * m->ny * m->nx * (8.0 + 12.0 + (in_mul ? 8.0 : 0.0)));
+    k_split_field<<<grid_for((long long)n_fields * m->ny * m->nx, 256), 256, 0, st>>>(
+        in, sin, m->ny, m->nx, n_fields, in_mul, mul_idx);
+    CSG_LAUNCH_CHECK();
+  }
 
   const int bn1 = m->no >= 256 ? 256 : 128;
   // ---- stage 1: T^T = split(in . B_x^T)^T
@@ -307,6 +311,8 @@ int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n
     p.accumulate = 0;
     p.status = ctx->status;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
+    // algorithmic work: 8 flops per complex multiply-add of the contraction
+    ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->ny * m->no * m->nx);
     rc = bn1 == 256 ? launch_gemm<256, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
                     : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
     if (rc) return rc;
@@ -333,6 +339,7 @@ int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n
     p.accumulate = accumulate;
     p.status = ctx->status;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
+    ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->mo * m->no * m->ny);
     rc = bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st)
                     : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st);
     if (rc) return rc;

@@ -1,0 +1,153 @@
+"""Seeded synthetic inputs (pure numpy) with the shapes of the benchmark
+configurations, and the plain descriptions of telescope, field and sources.
+
+The reference's own example data (pupils, PIAA sags, hex tables, response
+matrices) are not available, so every workload is generated from a seed:
+apertures, PIAA even-polynomial sags, standard hex layouts and uniform hex
+sags. This module has no GPU dependency; the hex interpolation tables are
+built on the GPU by workloads.hex_tables.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Telescope:
+    """telescope.cpp:21-60."""
+    primaryDiameter: float
+    primaryfRatio: float
+    magnification: float = 1.0
+
+    @property
+    def primaryfLength(self) -> float:
+        return self.primaryfRatio * self.primaryDiameter
+
+    def compute_loD(self, lam: float) -> float:
+        return self.magnification * self.primaryfLength * lam / self.primaryDiameter
+
+
+@dataclass
+class PointSource:
+    """efield pointSource: flux (amplitude sqrt(flux)), tip/tilt in the
+    reference's units (multiplied by the telescope magnification)."""
+    flux: float = 1.0
+    tip: float = 0.0
+    tilt: float = 0.0
+
+
+@dataclass
+class EField:
+    """efield.cpp: square N x N array, beam radius and pixel scale (metres)."""
+    n: int
+    beamRadiusPhysical: float
+    pixelScale: float
+    wavelengths: np.ndarray
+    sources: list = field(default_factory=lambda: [PointSource()])
+
+    @property
+    def arrayRadiusPhysical(self) -> float:
+        beam_px = math.ceil(2 * self.beamRadiusPhysical / self.pixelScale)
+        return self.beamRadiusPhysical * self.n / beam_px
+
+    def pixel_centres(self) -> np.ndarray:
+        d = self.pixelScale
+        return -(d * self.n - d) / 2.0 + np.arange(self.n) * d
+
+
+def circle_mask(n: int, radius_px: float, obstruction: float = 0.0) -> np.ndarray:
+    """Pixel-centred disk (optionally annular) on an n x n grid."""
+    c = (n - 1) / 2.0
+    yy, xx = np.mgrid[:n, :n]
+    r = np.hypot(xx - c, yy - c)
+    m = (r <= radius_px).astype(np.float64)
+    if obstruction > 0:
+        m[r < obstruction * radius_px] = 0.0
+    return m
+
+
+def piaa_sag(n: int, dx: float, radius: float, rng: np.random.Generator, pv: float = 2e-6,
+             order: int = 10) -> np.ndarray:
+    """Radially symmetric even polynomial sum_{k=1..order/2} c_k (r/R)^{2k},
+    clamped at r = R, scaled to the given peak-to-valley inside the beam."""
+    x = -(dx * n - dx) / 2.0 + np.arange(n) * dx
+    rr = np.minimum(np.hypot(x[None, :], x[:, None]) / radius, 1.0)
+    coef = rng.standard_normal(order // 2)
+    sag = sum(c * rr ** (2 * (k + 1)) for k, c in enumerate(coef))
+    inside = rr < 1.0
+    span = sag[inside].max() - sag[inside].min()
+    return sag * (pv / span)
+
+
+def hex_layout_standard(n_rings: int):
+    """Standard hexagonal rings (3 n (n+1) + 1 cells), unit neighbour pitch,
+    numbered ring by ring (counter-clockwise from +x)."""
+    pts = []
+    for q in range(-n_rings, n_rings + 1):
+        for r in range(max(-n_rings, -q - n_rings), min(n_rings, -q + n_rings) + 1):
+            x = 1.5 * q / math.sqrt(3.0)
+            y = (r + q / 2.0)
+            ring = max(abs(q), abs(r), abs(-q - r))
+            pts.append((ring, math.atan2(y, x) % (2 * math.pi), x, y))
+    pts.sort(key=lambda p: (p[0], p[1]))
+    return np.array([p[2] for p in pts]), np.array([p[3] for p in pts])
+
+
+@dataclass
+class PiaacmcSpec:
+    """PIAACMC-style chain (the 1024^2 PIAA + hex-FPM benchmark): PIAA M1 and
+    M2 even-polynomial sags (PV 2 um) separated by 1.0 m of Fresnel
+    propagation, a hex-tiled phase FPM (standard rings) applied through the
+    Babinet matrix-Fourier form on an S x S grid at 1/16 lambda/D, a 0.95
+    Lyot stop and a final 256^2 MFT at 0.25 lambda/D."""
+    n: int = 1024
+    beam_px: int = 800
+    beam_radius: float = 0.022
+    wavelengths: tuple = (650e-9,)
+    f_ratio: float = 15.1           # telescope primary f-ratio
+    diameter: float = 2.4
+    z: float = 1.0
+    fpm_focal_ratio: float = 80.0
+    S: int = 512
+    fpm_sampling: float = 16.0      # mask pixels per lambda/D
+    n_rings: int = 8
+    n_sub: int = 64
+    design_size: int = 2048
+    fpm_scale_factor: float = 0.9
+    hex_gap: float = 0.01
+    fpm_radius_lod: float = 2.0
+    sag_range: float = 0.5e-6
+    lyot: float = 0.95
+    n_out_fov: float = 64.0
+    spl: float = 4.0
+    seed: int = 2
+
+    @property
+    def n_hex(self) -> int:
+        return 3 * self.n_rings * (self.n_rings + 1) + 1
+
+
+def piaacmc_arrays(spec: PiaacmcSpec, sources=None) -> dict:
+    """Every seeded host-side input of the PIAACMC chain except the hex
+    interpolation tables (pupil, Lyot stop, PIAA sags, hex centres, mask
+    geometry, telescope and efield descriptions)."""
+    rng = np.random.default_rng(spec.seed)
+    dx = 2 * spec.beam_radius / spec.beam_px
+    lam = np.asarray(spec.wavelengths, dtype=np.float64)
+    tel = Telescope(spec.diameter, spec.f_ratio)
+    ef = EField(spec.n, spec.beam_radius, dx, lam, sources or [PointSource()])
+    lam_ref = float(lam.mean())
+    lod_fpm = lam_ref * spec.fpm_focal_ratio           # lambda/D at the FPM (metres)
+    hx, hy = hex_layout_standard(spec.n_rings)
+    return dict(pupil=circle_mask(spec.n, spec.beam_px / 2.0),
+                lyot=circle_mask(spec.n, spec.lyot * spec.beam_px / 2.0),
+                sag1=piaa_sag(spec.n, dx, spec.beam_radius, rng).astype(np.float32),
+                sag2=piaa_sag(spec.n, dx, spec.beam_radius, rng).astype(np.float32),
+                dm=lod_fpm / spec.fpm_sampling, fpm_radius=spec.fpm_radius_lod * lod_fpm,
+                dx=dx, lam=lam, tel=tel, ef=ef, hex_x=hx, hex_y=hy, lam_ref=lam_ref,
+                lod_image=tel.compute_loD(lam_ref))
+
+

@@ -77,6 +77,17 @@ int csg_memcpy_d2h(csg_ctx* ctx, void* dst, const void* src, size_t bytes);
 int csg_memset(csg_ctx* ctx, void* dst, int value, size_t bytes);
 /* Version string of the library build. */
 const char* csg_version(void);
+/* Number of kernels the library has launched from host code (all contexts);
+ * graph replays launch kernels without host code and are not counted. */
+unsigned long long csg_launch_count(void);
+/* Per-kernel timing, the device-side counterpart of the reference's
+ * per-element wall-clock timers (coronagraph.cpp:183-198, csim -t): when
+ * enabled, CUDA events bracket every instrumented launch on the context's
+ * stream (never inside graph capture). csg_profile_report writes
+ * {"kernel": {"count", "ms", "flops", "bytes"}} JSON, flops/bytes being the
+ * algorithmic work of those launches. */
+int csg_profile(csg_ctx* ctx, int enable);
+int csg_profile_report(csg_ctx* ctx, char* buf, size_t len);
 
 /* ---------------------------------------------------- field transfer */
 /* Upload n_fields complex<double> fields (host, interleaved) of rows x cols

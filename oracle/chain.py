@@ -11,10 +11,28 @@ from . import csim_fft as of
 from . import elements as oe
 
 
+def host_inputs(spec, sources=None) -> dict:
+    """The PIAACMC inputs built entirely on the CPU: the seeded arrays plus
+    hex tables from the C restatement of the reference's table builder."""
+    from csim_gb300.synth import piaacmc_arrays  # seeded input generators (numpy only)
+    from . import native
+    a = piaacmc_arrays(spec, sources)
+    d = native.hex_design_array(a["hex_x"], a["hex_y"], spec.n_rings, spec.design_size,
+                                spec.fpm_scale_factor, spec.hex_gap, 1.0)
+    ids, cnt, over = native.interpolation_tables(d, spec.S, spec.n_sub, a["dm"], a["fpm_radius"],
+                                                 spec.fpm_scale_factor)
+    a.update(hex_id=ids, count=cnt, overflow=over)
+    return a
+
+
 def piaacmc_field(inp: dict, spec, lam: float, amp: float, tip: float, tilt: float,
-                  sags: np.ndarray | None, calibrating: bool = False, conv_form: bool = False):
+                  sags: np.ndarray | None, calibrating: bool = False, conv_form: bool = False,
+                  czt: bool = False):
     """One (wavelength, source, candidate) field through mask -> mirror ->
     fresnel -> mirror -> fpmPupToLyot(hex, Babinet) -> mask -> fraunhoferFocal.
+    conv_form runs the reference's fpmPupToLyot algorithm (mask hat + 2N FFT
+    convolution); czt evaluates every zoom FFT by the reference's Bluestein
+    chirp-Z algorithm instead of the direct matrix product.
     Returns the final image field [n_out][n_out]."""
     ef, tel = inp["ef"], inp["tel"]
     n, dx = ef.n, inp["dx"]
@@ -31,9 +49,12 @@ def piaacmc_field(inp: dict, spec, lam: float, amp: float, tip: float, tilt: flo
         m1 = (np.fliplr(m) - 1.0)[None]
         fr, zs = -1.0, -1.0
         lfl = np.array([fr * lam * spec.fpm_focal_ratio * 2 * ef.beamRadiusPhysical])
-        f = oe.pup_to_lyot_conv if conv_form else oe.pup_to_lyot_mft
-        e = f(e, [lam], geom, mgeom, m1, lfl, fr, zs)
+        if conv_form:
+            e = oe.pup_to_lyot_conv(e, [lam], geom, mgeom, m1, lfl, fr, zs, use_czt=czt)
+        else:
+            e = oe.pup_to_lyot_mft(e, [lam], geom, mgeom, m1, lfl, fr, zs)
     e = oe.mask_apply(e, inp["lyot"])
     n_out = int(np.ceil(spec.n_out_fov * spec.spl))
     gout = of.ArrayGeom.set_xy(n_out, n_out, inp["lod_image"] / spec.spl)
-    return oe.fraunhofer_focal(e, geom, gout, [lam], ef.beamRadiusPhysical, tel.primaryfRatio)[0]
+    return oe.fraunhofer_focal(e, geom, gout, [lam], ef.beamRadiusPhysical, tel.primaryfRatio,
+                               use_czt=czt)[0]

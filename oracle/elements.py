@@ -223,7 +223,8 @@ def hex_mask_pixel_scale(beam_radius: float, pixel_scale: float, mask_size: int,
 
 # -------------------------------------------------- fpmPupToLyot (Babinet) --
 def pup_to_lyot_conv(cube, lambdas, egeom: ArrayGeom, mask_geom: ArrayGeom, mask_m1,
-                     lfl, f_ratio_sign: float, zoom_fft_sign: float, babinet: bool = True):
+                     lfl, f_ratio_sign: float, zoom_fft_sign: float, babinet: bool = True,
+                     use_czt: bool = False):
     """fpmPupToLyot.cpp:24-167, reference algorithm: per lambda the mask hat
     FFT(fft_shift(zoomFftSign zoomFft(maskGeom -> paddedGeom)(M - 1))) is built
     (:76-99); per field: embed E at [N/2, 3N/2) in 2N x 2N, FFT, multiply by the
@@ -235,7 +236,7 @@ def pup_to_lyot_conv(cube, lambdas, egeom: ArrayGeom, mask_geom: ArrayGeom, mask
     out = np.empty_like(cube)
     for sl, lam in enumerate(lambdas):
         z = ZoomFft(mask_geom, pgeom, lfl)
-        hat = zoom_fft_sign * z.mft(mask_m1[sl], sl)
+        hat = zoom_fft_sign * (z.execute if use_czt else z.mft)(mask_m1[sl], sl)
         fhat = fft2(fft_shift(hat))
         scale = pgeom.pixelSizeX ** 2 / (-1j * f_ratio_sign * lfl[sl])
         p = np.zeros((2 * nr, 2 * nc), dtype=np.complex128)

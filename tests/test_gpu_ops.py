@@ -37,6 +37,15 @@ RMS_TOL = 1e-6
 RANDOM_PEAK_TOL = 1e-5
 
 
+def c64_rms(gin, gout, lf, pref, e, ref):
+    """Relative rms error of the same MFT evaluated in complex64 (fp32) on the
+    CPU: the conditioning of the product sets what an fp32-class result can
+    reach (some random inputs cancel heavily)."""
+    a, b = of.mft_matrices(gin.pixelX, gin.pixelY, gout.pixelX, gout.pixelY, lf)
+    out = (np.complex64(pref) * a.astype(np.complex64)) @ e.astype(np.complex64) @ b.T.astype(np.complex64)
+    return rms_err(out.astype(np.complex128), ref)
+
+
 def rand_field(rng, f, r, c):
     return rng.standard_normal((f, r, c)) + 1j * rng.standard_normal((f, r, c))
 
@@ -60,7 +69,8 @@ def test_mft_zoomfft_semantics(ctx, n_in, n_out):
     for f in range(3):
         z = of.ZoomFft(gin, gout, lf)
         ref = z.mft(e[f], int(slots[f]))
-        assert rms_err(got[f], ref) < RMS_TOL
+        assert rms_err(got[f], ref) < max(RMS_TOL, 1.5 * c64_rms(gin, gout, lf[slots[f]],
+                                                                 pref[slots[f]], e[f], ref))
         assert peak_err(got[f], ref) < RANDOM_PEAK_TOL
 
 
