@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "ctx.hpp"
+#include "pixops.cuh"
 
 extern "C" {
 int csg_mft_create(csg_ctx*, csg_mft**, int, int, int, int, const double*, const double*,
@@ -409,27 +410,99 @@ static int prepare(csg_chain* c) {
   return rc;
 }
 
+// The walk as fused passes: elementwise elements (the point source, masks,
+// mirrors, complex masks) never get a pass of their own when a transform can
+// carry them. Ops before a Fresnel propagation ride in its first row pass,
+// ops right after it in its last row pass, ops before the final MFT in its
+// operand split; only ops with no such neighbour get one standalone pass.
+struct Step {
+  enum Kind { PIX, FRESNEL, FPM, FINAL } kind;
+  PixOps pro, epi;
+  const Elem* e = nullptr;
+};
+
+static bool push_op(PixOps& o, int kind, const float* a, const float* b, float param, int mr,
+                    int mc) {
+  if (o.n >= MAX_PIXOPS) return false;
+  o.kind[o.n] = kind;
+  o.a[o.n] = a;
+  o.b[o.n] = b;
+  o.param[o.n] = param;
+  o.mr[o.n] = mr;
+  o.mc[o.n] = mc;
+  ++o.n;
+  return true;
+}
+
+static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
+  std::vector<Step> prog;
+  PixOps pend;
+  push_op(pend, OP_SOURCE, nullptr, nullptr, 0.f, 0, 0);
+  bool epi_open = false;  // the last step is a Fresnel that can still take ops
+  for (const auto& e : c->elems) {
+    if (calibrating && e.disable_for_calibration) continue;
+    int kind = 0;
+    float param = 0.f;
+    if (e.kind == E_MASK) {
+      kind = OP_MASK;
+      param = e.quirk ? 1.f : 0.f;
+    } else if (e.kind == E_MIRROR) {
+      kind = OP_PHASE;
+      param = (float)e.sign;
+    } else if (e.kind == E_CMASK) {
+      kind = OP_CMASK;
+    }
+    if (kind) {
+      if (epi_open && push_op(prog.back().epi, kind, e.a, e.b, param, e.mrows, e.mcols)) continue;
+      epi_open = false;
+      if (!push_op(pend, kind, e.a, e.b, param, e.mrows, e.mcols)) {
+        Step s{Step::PIX, pend, PixOps(), nullptr};
+        prog.push_back(s);
+        pend = PixOps();
+        push_op(pend, kind, e.a, e.b, param, e.mrows, e.mcols);
+      }
+      continue;
+    }
+    if (e.kind == E_FRESNEL) {
+      prog.push_back(Step{Step::FRESNEL, pend, PixOps(), &e});
+      pend = PixOps();
+      epi_open = true;
+    } else if (e.kind == E_FPM_HEX) {
+      if (pend.n) prog.push_back(Step{Step::PIX, pend, PixOps(), nullptr});
+      pend = PixOps();
+      prog.push_back(Step{Step::FPM, PixOps(), PixOps(), &e});
+      epi_open = false;
+    } else if (e.kind == E_FRAUNHOFER) {
+      prog.push_back(Step{Step::FINAL, pend, PixOps(), &e});
+      pend = PixOps();
+      epi_open = false;
+    }
+  }
+  if (pend.n) prog.push_back(Step{Step::PIX, pend, PixOps(), nullptr});
+  return prog;
+}
+
 static int run_walk(csg_chain* c, int calibrating) {
   csg_ctx* ctx = c->ctx;
   const int F = c->n_fields, n = c->n;
-  int rc = csg_point_source(ctx, c->field, F, n, n, c->dx, c->dx, c->amp, c->tip, c->tilt);
-  if (rc) return rc;
-  for (auto& e : c->elems) {
-    if (calibrating && e.disable_for_calibration) continue;
-    switch (e.kind) {
-      case E_MASK:
-        rc = csg_mask_real(ctx, c->field, F, n, n, e.a, e.quirk);
+  FieldInfo fi;
+  fi.lam = c->lam_f;
+  fi.amp = c->amp;
+  fi.tip = c->tip;
+  fi.tilt = c->tilt;
+  int rc = CSG_OK;
+  for (const Step& s : plan_walk(c, calibrating)) {
+    switch (s.kind) {
+      case Step::PIX:
+        rc = pixops_pass(ctx->stream, c->field, F, n, n, s.pro, fi);
         break;
-      case E_MIRROR:
-        rc = csg_phase_screen(ctx, c->field, F, n, n, e.a, c->lam_f, e.sign);
+      case Step::FRESNEL: {
+        FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad};
+        rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi);
         break;
-      case E_FRESNEL:
-        rc = csg_fresnel(ctx, c->field, F, n, c->lam_f, e.ap_rad, e.z);
-        break;
-      case E_CMASK:
-        rc = csg_complex_mask(ctx, c->field, F, n, n, e.a, e.b, e.mrows, e.mcols);
-        break;
-      case E_FPM_HEX:
+      }
+      case Step::FPM: {
+        const Elem& e = *s.e;
         CSG_CHECK(c->sags && c->sag_hex == e.n_hex, CSG_E_STATE,
                   "hex FPM: candidate sags not set (csg_chain_sags) or wrong hex count");
         // (fliplr(M) - 1) for each field's (candidate, wavelength)
@@ -441,8 +514,10 @@ static int run_walk(csg_chain* c, int calibrating) {
         if (!rc) rc = csg_mft_execute(ctx, e.mft2, c->fpm, c->field, F, c->slot, 1, c->fpm_mask,
                                       c->ident);
         break;
-      case E_FRAUNHOFER:
-        rc = csg_mft_execute(ctx, e.mft, c->field, c->image, F, c->slot, 0, nullptr, nullptr);
+      }
+      case Step::FINAL:
+        rc = mft_execute_ops(ctx, s.e->mft, c->field, c->image, F, c->slot, 0, nullptr, nullptr,
+                             s.pro, fi);
         break;
     }
     if (rc) return rc;

@@ -1,21 +1,28 @@
 // Shared-memory Stockham FFTs for square N x N planar fp32 fields and the
 // fused angular-spectrum Fresnel pipeline.
 //
-// A 2-D transform is two HBM passes: a row pass (rows per CTA, coalesced
+// A 2-D transform is two HBM passes: a row pass (4096/N rows per CTA, float4
 // row loads) and a column pass (a [N][COLS] tile per CTA, coalesced row
-// segments). Each pass reads and writes the field once; every butterfly stage
-// runs in shared memory with the stage's inputs held in registers so the
-// transform is done in place (one buffer). Stages are radix 4 (one radix-2
-// stage first when log2 N is odd). Twiddles come from an FP64-generated
-// table of N entries.
+// segments). Each pass reads and writes the field once. Inside a pass every
+// thread owns 16 elements of one transform in registers; stages are radix 16
+// (one radix 2/4/8 stage first when log2 N is not a multiple of 4), so a
+// 1024-point transform is 3 shared-memory exchanges. The radix-R butterflies
+// are unrolled radix-2 decimation-in-frequency networks with exact W16
+// constants; inter-stage twiddles come from an FP64-generated table. Row
+// transforms are padded in shared memory (one float per 16) so the
+// stride-16 stores of the first stage are conflict-free.
 //
-// Fresnel (csim_fft.cpp:371-392) runs as: row FFT | column FFT x H x column
-// IFFT | row IFFT / N^2, i.e. three passes instead of four, with H generated
-// in-kernel from the integer frequency index (no N^2 exp table).
+// Element ops (point source, masks, mirrors) ride along in the row passes'
+// prologue and epilogue (pixops.cuh), so they cost no extra HBM pass.
+//
+// Fresnel (csim_fft.cpp:371-392) is row FFT | column FFT x H x column IFFT |
+// row IFFT / N^2: three passes, H generated in-kernel from the integer
+// frequency index.
 #include <map>
 #include <mutex>
 
 #include "ctx.hpp"
+#include "pixops.cuh"
 
 namespace csg {
 
@@ -47,202 +54,268 @@ static const float2* twiddles(int device, int n, cudaStream_t st) {
   return p;
 }
 
-// ------------------------------------------------------- in-smem FFT
-// ntr transforms of length N; element m of transform t at t*ts + m*es.
-// Requires blockDim.x == ntr * N / 16. TF: transform index fastest across
-// threads (columns) or butterfly index fastest (rows).
-template <bool INV, bool TF>
-__device__ void smem_fft(float* __restrict__ re, float* __restrict__ im, int N, int log2n, int ntr,
-                         int es, int ts, const float2* __restrict__ tw) {
-  const int T = blockDim.x;
-  const int tid = threadIdx.x;
-  const float sg = INV ? 1.f : -1.f;
-  float vr[16], vi[16];
-  int L = 1;
-  int first = 1;
-  while (L < N) {
-    const int R = (first && (log2n & 1)) ? 2 : 4;
-    first = 0;
-    const int nbf = N / R;          // butterflies per transform
-    const int per = (ntr * nbf) / T;  // butterflies per thread (4 or 8)
-    const int stride_in = nbf;      // N / R
-    const int twstep = N / (L * R);
-    // gather + compute into registers
-    for (int i = 0; i < per; ++i) {
-      const int b = tid + i * T;
-      int t, j;
-      if (TF) { t = b % ntr; j = b / ntr; }
-      else    { j = b % nbf; t = b / nbf; }
-      const int k = j % L, g = j / L;
-      const int src = t * ts + (g * L + k) * es;
-      if (R == 4) {
-        float ar[4], ai[4];
+// ------------------------------------------------ in-register butterflies
+// cos and sin of 2 pi m / 16.
+__device__ __forceinline__ float w16c(int m) {
+  constexpr float c[16] = {1.0f, 0.92387953251128674f, 0.70710678118654752f, 0.38268343236508977f,
+                           0.0f, -0.38268343236508977f, -0.70710678118654752f, -0.92387953251128674f,
+                           -1.0f, -0.92387953251128674f, -0.70710678118654752f, -0.38268343236508977f,
+                           0.0f, 0.38268343236508977f, 0.70710678118654752f, 0.92387953251128674f};
+  return c[m];
+}
+__device__ __forceinline__ float w16s(int m) { return w16c((m + 12) & 15); }  // sin = cos(. - pi/2)
+
+constexpr int bitrev(int q, int bits) {
+  int r = 0;
+  for (int i = 0; i < bits; ++i) r |= ((q >> i) & 1) << (bits - 1 - i);
+  return r;
+}
+constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+// Radix-2 decimation-in-frequency network on R register values (natural
+// order in, bit-reversed order out). sg = -1 forward, +1 inverse.
+template <int R, int HALF, bool INV>
+__device__ __forceinline__ void dif_stage(float* xr, float* xi) {
+  if constexpr (HALF >= 1) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int idx = src + q * stride_in * es;
-          float xr = re[idx], xi = im[idx];
-          if (q) {
-            const float2 w = __ldg(&tw[k * q * twstep]);
-            const float wi = sg * w.y;
-            const float tr = xr * w.x - xi * wi;
-            xi = xr * wi + xi * w.x;
-            xr = tr;
-          }
-          ar[q] = xr; ai[q] = xi;
+    for (int base = 0; base < R; base += 2 * HALF) {
+#pragma unroll
+      for (int k = 0; k < HALF; ++k) {
+        const float ar = xr[base + k], ai = xi[base + k];
+        const float br = xr[base + k + HALF], bi = xi[base + k + HALF];
+        xr[base + k] = ar + br;
+        xi[base + k] = ai + bi;
+        const float dr = ar - br, di = ai - bi;
+        constexpr int step = 16 / (2 * HALF);
+        const int m = k * step;
+        if (m == 0) {
+          xr[base + k + HALF] = dr;
+          xi[base + k + HALF] = di;
+        } else {
+          const float c = w16c(m), s = INV ? w16s(m) : -w16s(m);
+          xr[base + k + HALF] = dr * c - di * s;
+          xi[base + k + HALF] = dr * s + di * c;
         }
-        const float s02r = ar[0] + ar[2], s02i = ai[0] + ai[2];
-        const float d02r = ar[0] - ar[2], d02i = ai[0] - ai[2];
-        const float s13r = ar[1] + ar[3], s13i = ai[1] + ai[3];
-        const float d13r = ar[1] - ar[3], d13i = ai[1] - ai[3];
-        // y1 = d02 + sg*i*d13, y3 = d02 - sg*i*d13
-        vr[4 * i + 0] = s02r + s13r;        vi[4 * i + 0] = s02i + s13i;
-        vr[4 * i + 1] = d02r - sg * d13i;   vi[4 * i + 1] = d02i + sg * d13r;
-        vr[4 * i + 2] = s02r - s13r;        vi[4 * i + 2] = s02i - s13i;
-        vr[4 * i + 3] = d02r + sg * d13i;   vi[4 * i + 3] = d02i - sg * d13r;
-      } else {
-        const int i0 = src, i1 = src + stride_in * es;
-        float xr = re[i1], xi = im[i1];
-        const float2 w = __ldg(&tw[k * twstep]);
-        const float wi = sg * w.y;
-        const float tr = xr * w.x - xi * wi;
-        xi = xr * wi + xi * w.x;
-        xr = tr;
-        const float ar = re[i0], ai = im[i0];
-        vr[2 * i + 0] = ar + xr; vi[2 * i + 0] = ai + xi;
-        vr[2 * i + 1] = ar - xr; vi[2 * i + 1] = ai - xi;
       }
     }
-    __syncthreads();
-    for (int i = 0; i < per; ++i) {
-      const int b = tid + i * T;
-      int t, j;
-      if (TF) { t = b % ntr; j = b / ntr; }
-      else    { j = b % nbf; t = b / nbf; }
-      const int k = j % L, g = j / L;
-      const int dst = t * ts + (g * L * R + k) * es;
-      for (int q = 0; q < R; ++q) {
-        re[dst + q * L * es] = vr[R * i + q];
-        im[dst + q * L * es] = vi[R * i + q];
-      }
-    }
-    __syncthreads();
-    L *= R;
+    dif_stage<R, HALF / 2, INV>(xr, xi);
   }
 }
 
-// Row pass: blockDim = rows * N / 16; each CTA transforms `rows` rows.
-template <bool INV>
-__global__ void k_fft_rows(float* __restrict__ field, int F, int N, int log2n, int rows,
-                           float scale, const float2* __restrict__ tw) {
-  extern __shared__ float sm[];
-  float* re = sm;
-  float* im = sm + rows * N;
-  const int ctas_per_field = N / rows;
-  const int f = blockIdx.x / ctas_per_field;
-  const int r0 = (blockIdx.x % ctas_per_field) * rows;
-  const long long plane = (long long)N * N;
-  float* fre = field + (long long)f * 2 * plane + (long long)r0 * N;
-  float* fim = fre + plane;
-  const int n = rows * N;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    re[i] = fre[i];
-    im[i] = fim[i];
-  }
-  __syncthreads();
-  smem_fft<INV, false>(re, im, N, log2n, rows, 1, N, tw);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    fre[i] = re[i] * scale;
-    fim[i] = im[i] * scale;
-  }
-}
-
-struct FresnelArgs {
-  const double* lambda;  // per field, nullptr = plain column pass
-  double z;
-  double ap_rad;
+// Row layout: transform t at t * NP, element m padded by m / 16.
+template <int N>
+struct RowAddr {
+  static constexpr int NP = N + N / 16;
+  __device__ __forceinline__ static int at(int t, int m) { return t * NP + m + (m >> 4); }
+};
+// Column layout: element m of column t at m * COLS + t.
+template <int COLS>
+struct ColAddr {
+  __device__ __forceinline__ static int at(int t, int m) { return m * COLS + t; }
 };
 
-__device__ __forceinline__ float frac_mul(float a, float khi, float klo) {
-  // a * (khi + klo) modulo 1, with the product error folded back in
-  const float p = a * khi;
-  float e = fmaf(a, khi, -p);
-  e = fmaf(a, klo, e);
-  return (p - rintf(p)) + e;
-}
-
-// Column pass: blockDim = cols * N / 16; tile [N][cols] of one field.
-// MODE 0: forward, 1: inverse, 2: forward * H(lambda_f) * inverse.
-template <int MODE>
-__global__ void k_fft_cols(float* __restrict__ field, int F, int N, int log2n, int cols,
-                           const float2* __restrict__ tw, FresnelArgs fa) {
-  extern __shared__ float sm[];
-  float* re = sm;
-  float* im = sm + cols * N;
-  const int ctas_per_field = N / cols;
-  const int f = blockIdx.x / ctas_per_field;
-  const int c0 = (blockIdx.x % ctas_per_field) * cols;
-  const long long plane = (long long)N * N;
-  float* fre = field + (long long)f * 2 * plane + c0;
-  float* fim = fre + plane;
-  const int n = cols * N;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int r = i / cols, c = i % cols;
-    re[i] = fre[(long long)r * N + c];
-    im[i] = fim[(long long)r * N + c];
+// One Stockham stage of radix R at sub-length L; each thread owns 16 / R
+// butterflies j = u + i N / 16.
+template <int N, int R, int L, bool INV, class A>
+__device__ __forceinline__ void stockham_stage(float* __restrict__ re, float* __restrict__ im,
+                                               int t, int u, const float2* __restrict__ tw) {
+  constexpr int TPT = N / 16;
+  constexpr int BPT = 16 / R;
+  constexpr int STRIDE = N / R;
+  constexpr int TWSTEP = N / (L * R);
+  float xr[16], xi[16];
+#pragma unroll
+  for (int i = 0; i < BPT; ++i) {
+    const int j = u + i * TPT;
+    const int k = j % L, g = j / L;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int m = g * L + k + q * STRIDE;
+      float a = re[A::at(t, m)], b = im[A::at(t, m)];
+      if (L > 1 && q > 0) {
+        const float2 w = __ldg(&tw[k * q * TWSTEP]);
+        const float ws = INV ? w.y : -w.y;
+        const float tr = a * w.x - b * ws;
+        b = a * ws + b * w.x;
+        a = tr;
+      }
+      xr[i * R + q] = a;
+      xi[i * R + q] = b;
+    }
   }
   __syncthreads();
-  if (MODE == 1) {
-    smem_fft<true, true>(re, im, N, log2n, cols, cols, 1, tw);
-  } else {
-    smem_fft<false, true>(re, im, N, log2n, cols, cols, 1, tw);
+#pragma unroll
+  for (int i = 0; i < BPT; ++i) {
+    dif_stage<R, R / 2, INV>(&xr[i * R], &xi[i * R]);
+    const int j = u + i * TPT;
+    const int k = j % L, g = j / L;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int m = g * L * R + k + q * L;
+      constexpr int bits = ilog2c(R);
+      re[A::at(t, m)] = xr[i * R + bitrev(q, bits)];
+      im[A::at(t, m)] = xi[i * R + bitrev(q, bits)];
+    }
   }
+  __syncthreads();
+}
+
+// Full transform: a first stage of radix 2^(log2 N mod 4) if needed, then
+// radix-16 stages.
+template <int N, int L, bool INV, class A>
+__device__ __forceinline__ void stockham_rest(float* re, float* im, int t, int u,
+                                              const float2* tw) {
+  if constexpr (L < N) {
+    stockham_stage<N, 16, L, INV, A>(re, im, t, u, tw);
+    stockham_rest<N, L * 16, INV, A>(re, im, t, u, tw);
+  }
+}
+
+template <int N, bool INV, class A>
+__device__ __forceinline__ void smem_fft(float* re, float* im, int t, int u, const float2* tw) {
+  constexpr int REM = ilog2c(N) % 4;
+  if constexpr (REM == 0) {
+    stockham_rest<N, 1, INV, A>(re, im, t, u, tw);
+  } else {
+    constexpr int R0 = 1 << REM;
+    stockham_stage<N, R0, 1, INV, A>(re, im, t, u, tw);
+    stockham_rest<N, R0, INV, A>(re, im, t, u, tw);
+  }
+}
+
+template <int N>
+struct RowCfg {
+  static constexpr int TPT = N / 16;
+  static constexpr int ROWS = 4096 / N > 0 ? 4096 / N : 1;  // 256 threads per CTA
+  static constexpr int THREADS = ROWS * TPT;
+  static constexpr size_t SMEM = (size_t)ROWS * RowAddr<N>::NP * 8;
+};
+template <int N>
+struct ColCfg {
+  static constexpr int TPT = N / 16;
+  static constexpr int COLS = N >= 2048 ? 16 * 1024 / N : 16;
+  static constexpr int THREADS = COLS * TPT;
+  static constexpr size_t SMEM = (size_t)COLS * N * 8;
+};
+
+// Row pass with fused element prologue / epilogue.
+template <int N, bool INV>
+__global__ void __launch_bounds__(RowCfg<N>::THREADS)
+    k_fft_rows(float* __restrict__ field, float scale, const float2* __restrict__ tw, PixOps pro,
+               PixOps epi, FieldInfo fi) {
+  using CF = RowCfg<N>;
+  using A = RowAddr<N>;
+  extern __shared__ float sm[];
+  float* re = sm;
+  float* im = sm + CF::ROWS * A::NP;
+  constexpr int CPF = N / CF::ROWS;  // CTAs per field
+  const int f = blockIdx.x / CPF;
+  const int r0 = (blockIdx.x % CPF) * CF::ROWS;
+  const size_t plane = (size_t)N * N;
+  float* fre = field + (size_t)f * 2 * plane + (size_t)r0 * N;
+  float* fim = fre + plane;
+  PixConsts kp, ke;
+  if (pro.n) pix_consts(pro, fi, f, N, N, kp);
+  if (epi.n) pix_consts(epi, fi, f, N, N, ke);
+  const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // source overwrites: skip the read
+  constexpr int NV = CF::ROWS * N / 4;
+#pragma unroll 2
+  for (int v = threadIdx.x; v < NV; v += CF::THREADS) {
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (!gen) {
+      a = reinterpret_cast<const float4*>(fre)[v];
+      b = reinterpret_cast<const float4*>(fim)[v];
+    }
+    const int e0 = 4 * v, t = e0 / N, m = e0 % N;
+    float xr[4] = {a.x, a.y, a.z, a.w}, xi[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (pro.n) pix_apply(pro, kp, r0 + t, m + q, N, N, xr[q], xi[q]);
+      re[A::at(t, m + q)] = xr[q];
+      im[A::at(t, m + q)] = xi[q];
+    }
+  }
+  __syncthreads();
+  const int t = threadIdx.x / CF::TPT, u = threadIdx.x % CF::TPT;
+  smem_fft<N, INV, A>(re, im, t, u, tw);
+#pragma unroll 2
+  for (int v = threadIdx.x; v < NV; v += CF::THREADS) {
+    const int e0 = 4 * v, tt = e0 / N, m = e0 % N;
+    float xr[4], xi[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      xr[q] = re[A::at(tt, m + q)] * scale;
+      xi[q] = im[A::at(tt, m + q)] * scale;
+      if (epi.n) pix_apply(epi, ke, r0 + tt, m + q, N, N, xr[q], xi[q]);
+    }
+    reinterpret_cast<float4*>(fre)[v] = make_float4(xr[0], xr[1], xr[2], xr[3]);
+    reinterpret_cast<float4*>(fim)[v] = make_float4(xi[0], xi[1], xi[2], xi[3]);
+  }
+}
+
+// Column pass; MODE 0: forward, 1: inverse, 2: forward * H(lambda_f) * inverse.
+template <int N, int MODE>
+__global__ void __launch_bounds__(ColCfg<N>::THREADS)
+    k_fft_cols(float* __restrict__ field, const float2* __restrict__ tw, FresnelArgs fa) {
+  using CF = ColCfg<N>;
+  using A = ColAddr<CF::COLS>;
+  extern __shared__ float sm[];
+  float* re = sm;
+  float* im = sm + CF::COLS * N;
+  constexpr int CPF = N / CF::COLS;
+  const int f = blockIdx.x / CPF;
+  const int c0 = (blockIdx.x % CPF) * CF::COLS;
+  const size_t plane = (size_t)N * N;
+  float* fre = field + (size_t)f * 2 * plane + c0;
+  float* fim = fre + plane;
+  constexpr int NE = CF::COLS * N;
+  for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
+    const int r = i / CF::COLS, c = i % CF::COLS;
+    re[i] = fre[(size_t)r * N + c];
+    im[i] = fim[(size_t)r * N + c];
+  }
+  __syncthreads();
+  const int t = threadIdx.x % CF::COLS, u = threadIdx.x / CF::COLS;
+  smem_fft<N, MODE == 1, A>(re, im, t, u, tw);
   if (MODE == 2) {
     // H = exp(2 pi i [z/lambda sqrt(1 - eps)]), eps = (lambda/apRad)^2 f^2 / 4
     //   turns = z/lambda - K f^2 / 2 - K f^2 h,  K = z lambda / (4 apRad^2),
     //   h = eps / (2 (1 + sqrt(1 - eps))^2)
+    // eps > 1 (evanescent) gives NaN like the reference's real sqrt.
     const double lam = fa.lambda[f];
     double t0 = fa.z / lam;
     t0 -= rint(t0);
     const double K = fa.z * lam / (4.0 * fa.ap_rad * fa.ap_rad);
-    const double kh = 0.5 * K;
-    const float khi = (float)kh, klo = (float)(kh - (double)khi);
+    float khi, klo;
+    split_f64_pair(0.5 * K, khi, klo);
     const float Kf = (float)K;
     const float c_eps = (float)(0.25 * (lam / fa.ap_rad) * (lam / fa.ap_rad));
     const float t0f = (float)t0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const int r = i / cols, c = c0 + i % cols;
+    for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
+      const int r = i / CF::COLS, c = c0 + i % CF::COLS;
       const int fr = r < N / 2 ? r : r - N;
       const int fc = c < N / 2 ? c : c - N;
       const float f2 = (float)(fr * fr + fc * fc);  // exact: < 2^24
       const float eps = c_eps * f2;
       const float s = sqrtf(1.f - eps);
       const float h = eps / (2.f * (1.f + s) * (1.f + s));
-      float t = t0f - frac_mul(f2, khi, klo) - Kf * f2 * h;
-      t -= rintf(t);
+      float tt = t0f - frac_prod(f2, khi, klo) - Kf * f2 * h;
+      tt -= rintf(tt);
       float sn, cs;
-      sincospif(2.f * t, &sn, &cs);
+      sincospif(2.f * tt, &sn, &cs);
       const float xr = re[i], xi = im[i];
       re[i] = xr * cs - xi * sn;
       im[i] = xr * sn + xi * cs;
     }
     __syncthreads();
-    smem_fft<true, true>(re, im, N, log2n, cols, cols, 1, tw);
+    smem_fft<N, true, A>(re, im, t, u, tw);
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int r = i / cols, c = i % cols;
-    fre[(long long)r * N + c] = re[i];
-    fim[(long long)r * N + c] = im[i];
+  for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
+    const int r = i / CF::COLS, c = i % CF::COLS;
+    fre[(size_t)r * N + c] = re[i];
+    fim[(size_t)r * N + c] = im[i];
   }
 }
-
-static int ilog2(int n) {
-  int l = 0;
-  while ((1 << l) < n) ++l;
-  return l;
-}
-
-static int rows_for(int n) { return n >= 4096 ? 1 : (4096 / n > 16 ? 16 : 4096 / n); }
-static int cols_for(int n) { return n >= 2048 ? 8 * 2048 / n : (n >= 64 ? 16 : 16); }
 
 template <typename K>
 static int prep_smem(K kern, size_t bytes) {
@@ -250,56 +323,66 @@ static int prep_smem(K kern, size_t bytes) {
   return CSG_OK;
 }
 
-int fft2d_launch(csg_ctx* ctx, float* field, int F, int n, int direction, const double* lambda,
-                 double ap_rad, double z, bool fresnel) {
-  CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
-            "FFT size must be a power of two in [64, 4096]");
-  CSG_CHECK(F > 0, CSG_E_SHAPE, "FFT needs at least one field");
-  cudaStream_t st = ctx->stream;
-  const float2* tw = twiddles(ctx->device, n, st);
-  CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
-  const int lg = ilog2(n);
-  const int rows = rows_for(n), cols = cols_for(n);
-  const size_t rsm = (size_t)rows * n * 8, csm = (size_t)cols * n * 8;
-  const int rthreads = rows * n / 16, cthreads = cols * n / 16;
-  const long long rgrid = (long long)F * (n / rows), cgrid = (long long)F * (n / cols);
-  CSG_CHECK(rgrid < (1LL << 31) && cgrid < (1LL << 31), CSG_E_SHAPE, "too many fields");
-  FresnelArgs fa{lambda, z, ap_rad};
+template <int N>
+static int run_fft(cudaStream_t st, float* field, int F, int direction, const FresnelArgs* fa,
+                   const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw) {
+  using RC = RowCfg<N>;
+  using CC = ColCfg<N>;
+  const int rgrid = F * (N / RC::ROWS), cgrid = F * (N / CC::COLS);
+  const float inv_scale = 1.f / ((float)N * (float)N);
+  const PixOps none;
   int rc;
-  const bool inv = direction > 0;
-  const float inv_scale = 1.f / ((float)n * (float)n);
-  // one compulsory read + write of the planar fp32 field per pass
-  const double pass_bytes = (double)F * n * n * 16.0;
-  ProfScope ps(ctx, fresnel ? "fresnel_3pass" : "fft2d_2pass", 0,
-               pass_bytes * (fresnel ? 3.0 : 2.0));
-  if (!fresnel) {
-    if (!inv) {
-      if ((rc = prep_smem(k_fft_rows<false>, rsm))) return rc;
-      k_fft_rows<false><<<(int)rgrid, rthreads, rsm, st>>>(field, F, n, lg, rows, 1.f, tw);
-      CSG_LAUNCH_CHECK();
-      if ((rc = prep_smem(k_fft_cols<0>, csm))) return rc;
-      k_fft_cols<0><<<(int)cgrid, cthreads, csm, st>>>(field, F, n, lg, cols, tw, fa);
-      CSG_LAUNCH_CHECK();
-    } else {
-      if ((rc = prep_smem(k_fft_cols<1>, csm))) return rc;
-      k_fft_cols<1><<<(int)cgrid, cthreads, csm, st>>>(field, F, n, lg, cols, tw, fa);
-      CSG_LAUNCH_CHECK();
-      if ((rc = prep_smem(k_fft_rows<true>, rsm))) return rc;
-      k_fft_rows<true><<<(int)rgrid, rthreads, rsm, st>>>(field, F, n, lg, rows, inv_scale, tw);
-      CSG_LAUNCH_CHECK();
-    }
+  if (fa) {
+    if ((rc = prep_smem(k_fft_rows<N, false>, RC::SMEM))) return rc;
+    k_fft_rows<N, false><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, 1.f, tw, pro, none, fi);
+    CSG_LAUNCH_CHECK();
+    if ((rc = prep_smem(k_fft_cols<N, 2>, CC::SMEM))) return rc;
+    k_fft_cols<N, 2><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
+    CSG_LAUNCH_CHECK();
+    if ((rc = prep_smem(k_fft_rows<N, true>, RC::SMEM))) return rc;
+    k_fft_rows<N, true><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, inv_scale, tw, none, epi, fi);
+    CSG_LAUNCH_CHECK();
+  } else if (direction < 0) {
+    if ((rc = prep_smem(k_fft_rows<N, false>, RC::SMEM))) return rc;
+    k_fft_rows<N, false><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, 1.f, tw, pro, none, fi);
+    CSG_LAUNCH_CHECK();
+    if ((rc = prep_smem(k_fft_cols<N, 0>, CC::SMEM))) return rc;
+    k_fft_cols<N, 0><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    CSG_LAUNCH_CHECK();
+    if (epi.n) return pixops_pass(st, field, F, N, N, epi, fi);
   } else {
-    if ((rc = prep_smem(k_fft_rows<false>, rsm))) return rc;
-    k_fft_rows<false><<<(int)rgrid, rthreads, rsm, st>>>(field, F, n, lg, rows, 1.f, tw);
+    if (pro.n && (rc = pixops_pass(st, field, F, N, N, pro, fi))) return rc;
+    if ((rc = prep_smem(k_fft_cols<N, 1>, CC::SMEM))) return rc;
+    k_fft_cols<N, 1><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
     CSG_LAUNCH_CHECK();
-    if ((rc = prep_smem(k_fft_cols<2>, csm))) return rc;
-    k_fft_cols<2><<<(int)cgrid, cthreads, csm, st>>>(field, F, n, lg, cols, tw, fa);
-    CSG_LAUNCH_CHECK();
-    if ((rc = prep_smem(k_fft_rows<true>, rsm))) return rc;
-    k_fft_rows<true><<<(int)rgrid, rthreads, rsm, st>>>(field, F, n, lg, rows, inv_scale, tw);
+    if ((rc = prep_smem(k_fft_rows<N, true>, RC::SMEM))) return rc;
+    k_fft_rows<N, true><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, inv_scale, tw, none, epi, fi);
     CSG_LAUNCH_CHECK();
   }
   return CSG_OK;
+}
+
+// 2-D FFT or Fresnel propagation of F square N x N fields with fused element
+// ops (pro before the transform, epi after it).
+int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
+                const PixOps& pro, const PixOps& epi, const FieldInfo& fi) {
+  CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
+            "FFT size must be a power of two in [64, 4096]");
+  CSG_CHECK(F > 0 && (long long)F * n < (1LL << 31), CSG_E_SHAPE, "FFT: bad field count");
+  cudaStream_t st = ctx->stream;
+  const float2* tw = twiddles(ctx->device, n, st);
+  CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
+  const double pass_bytes = (double)F * n * n * 16.0;
+  ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0, pass_bytes * (fa ? 3.0 : 2.0));
+  switch (n) {
+    case 64: return run_fft<64>(st, field, F, direction, fa, pro, epi, fi, tw);
+    case 128: return run_fft<128>(st, field, F, direction, fa, pro, epi, fi, tw);
+    case 256: return run_fft<256>(st, field, F, direction, fa, pro, epi, fi, tw);
+    case 512: return run_fft<512>(st, field, F, direction, fa, pro, epi, fi, tw);
+    case 1024: return run_fft<1024>(st, field, F, direction, fa, pro, epi, fi, tw);
+    case 2048: return run_fft<2048>(st, field, F, direction, fa, pro, epi, fi, tw);
+    default: return run_fft<4096>(st, field, F, direction, fa, pro, epi, fi, tw);
+  }
 }
 
 }  // namespace csg
@@ -312,7 +395,7 @@ int csg_fft2d(csg_ctx* ctx, float* field, int n_fields, int n, int direction) {
   CSG_CHECK(ctx && field, CSG_E_ARG, "csg_fft2d: null argument");
   CSG_CHECK(direction == -1 || direction == 1, CSG_E_ARG, "csg_fft2d: direction must be -1 or +1");
   DeviceGuard g(ctx->device);
-  return fft2d_launch(ctx, field, n_fields, n, direction, nullptr, 0, 0, false);
+  return fft2d_fused(ctx, field, n_fields, n, direction, nullptr, PixOps(), PixOps(), FieldInfo());
 }
 
 int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
@@ -320,7 +403,8 @@ int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* l
   CSG_CHECK(ctx && field && lambda, CSG_E_ARG, "csg_fresnel: null argument");
   CSG_CHECK(ap_rad > 0, CSG_E_ARG, "csg_fresnel: apRad must be positive");
   DeviceGuard g(ctx->device);
-  return fft2d_launch(ctx, field, n_fields, n, -1, lambda, ap_rad, z, true);
+  FresnelArgs fa{lambda, z, ap_rad};
+  return fft2d_fused(ctx, field, n_fields, n, -1, &fa, PixOps(), PixOps(), FieldInfo());
 }
 
 }  // extern "C"

@@ -1,116 +1,58 @@
 // Element field operations (HBM-bound elementwise / gather kernels) and the
 // intensity / dark-hole reductions.
 //
-// Phases: a per-pixel phase is the product of an fp32 datum (sag, pixel
-// offset) and an FP64 constant. The constant is carried as an fp32 pair
-// (hi + lo) and the product is reduced modulo one turn with the rounding
-// error of the leading product folded back (fmaf), which keeps ~2^-40 turns
-// of accuracy without FP64 arithmetic per pixel.
+// The single-element calls (point source, mask, mirror phase, complex mask)
+// are one standalone pass of the fused element machinery (pixops.cuh); the
+// chain executor instead folds them into the FFT and MFT passes.
 #include "ctx.hpp"
+#include "pixops.cuh"
 
 namespace csg {
 
-__device__ __forceinline__ float frac_mul2(float a, float khi, float klo) {
-  const float p = a * khi;
-  float e = fmaf(a, khi, -p);
-  e = fmaf(a, klo, e);
-  return (p - rintf(p)) + e;
-}
-
-__device__ __forceinline__ void split_f64(double v, float& hi, float& lo) {
-  hi = (float)v;
-  lo = (float)(v - (double)hi);
-}
-
-// ------------------------------------------------------------ point source
-__global__ void k_point_source(float* __restrict__ field, int F, int R, int C, double dx, double dy,
-                               const double* __restrict__ amp, const double* __restrict__ tip,
-                               const double* __restrict__ tilt) {
-  const long long plane = (long long)R * C;
+// ----------------------------------------------------- standalone element pass
+// 4 consecutive pixels per thread (float4 when the row length allows).
+__global__ void k_pixops(float* __restrict__ field, int R, int C, PixOps ops, FieldInfo fi) {
   const int f = blockIdx.y;
-  if (f >= F) return;
-  // turns = 2 x tip / Lx + 2 y tilt / Ly, x = (c - (C-1)/2) dx, Lx = C dx
-  float kxh, kxl, kyh, kyl;
-  split_f64(2.0 * tip[f] / (double)C, kxh, kxl);
-  split_f64(2.0 * tilt[f] / (double)R, kyh, kyl);
-  const float a = (float)amp[f];
-  float* re = field + (long long)f * 2 * plane;
+  const int plane = R * C;
+  PixConsts k;
+  pix_consts(ops, fi, f, R, C, k);
+  float* re = field + (size_t)f * 2 * plane;
   float* im = re + plane;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C), r = (int)(i / C);
-    const float xc = (float)c - 0.5f * (float)(C - 1);  // exact half-integers
-    const float yr = (float)r - 0.5f * (float)(R - 1);
-    float t = frac_mul2(xc, kxh, kxl) + frac_mul2(yr, kyh, kyl);
-    t -= rintf(t);
-    float s, co;
-    sincospif(2.f * t, &s, &co);
-    re[i] = a * co;
-    im[i] = a * s;
-  }
-}
-
-// -------------------------------------------------------------- masks
-__global__ void k_mask_real(float* __restrict__ field, int F, long long plane,
-                            const float* __restrict__ mask, int quirk) {
-  const long long n = plane * F;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long f = i / plane, o = i % plane;
-    float* re = field + f * 2 * plane + o;
-    float* im = re + plane;
-    const float m = mask[o];
-    const float xr = *re, xi = *im;
-    if (quirk) {  // (xr + i xi)(m + i m)
-      *re = m * (xr - xi);
-      *im = m * (xr + xi);
-    } else {
-      *re = xr * m;
-      *im = xi * m;
+  const bool gen = ops.n && ops.kind[0] == OP_SOURCE;
+  if ((C & 3) == 0) {
+    const int nv = plane / 4;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+      if (!gen) {
+        a = reinterpret_cast<const float4*>(re)[v];
+        b = reinterpret_cast<const float4*>(im)[v];
+      }
+      const int e0 = 4 * v, r = e0 / C, c = e0 % C;
+      float xr[4] = {a.x, a.y, a.z, a.w}, xi[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) pix_apply(ops, k, r, c + q, R, C, xr[q], xi[q]);
+      reinterpret_cast<float4*>(re)[v] = make_float4(xr[0], xr[1], xr[2], xr[3]);
+      reinterpret_cast<float4*>(im)[v] = make_float4(xi[0], xi[1], xi[2], xi[3]);
+    }
+  } else {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x) {
+      float xr = gen ? 0.f : re[i], xi = gen ? 0.f : im[i];
+      pix_apply(ops, k, i / C, i % C, R, C, xr, xi);
+      re[i] = xr;
+      im[i] = xi;
     }
   }
 }
 
-__global__ void k_phase_screen(float* __restrict__ field, int F, long long plane,
-                               const float* __restrict__ sag, const double* __restrict__ lambda,
-                               double sign) {
-  const int f = blockIdx.y;
-  if (f >= F) return;
-  float kh, kl;  // turns per metre of sag: -sign * 2 / lambda
-  split_f64(-sign * 2.0 / lambda[f], kh, kl);
-  float* re = field + (long long)f * 2 * plane;
-  float* im = re + plane;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane;
-       i += (long long)gridDim.x * blockDim.x) {
-    float t = frac_mul2(sag[i], kh, kl);
-    float s, c;
-    sincospif(2.f * t, &s, &c);
-    const float xr = re[i], xi = im[i];
-    re[i] = xr * c - xi * s;
-    im[i] = xr * s + xi * c;
-  }
-}
-
-__global__ void k_complex_mask(float* __restrict__ field, int F, int R, int C,
-                               const float* __restrict__ amp, const float* __restrict__ ph,
-                               int mr, int mc) {
-  const long long plane = (long long)R * C;
-  const long long mplane = (long long)mr * mc;
-  const int r0 = R / 2 - mr / 2, c0 = C / 2 - mc / 2;
-  const long long n = mplane * F;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long f = i / mplane, o = i % mplane;
-    const int r = (int)(o / mc), c = (int)(o % mc);
-    float s, co;
-    sincosf(-ph[o], &s, &co);
-    const float a = amp[o];
-    float* re = field + f * 2 * plane + (long long)(r0 + r) * C + (c0 + c);
-    float* im = re + plane;
-    const float xr = *re, xi = *im;
-    *re = a * (xr * co - xi * s);
-    *im = a * (xr * s + xi * co);
-  }
+int pixops_pass(cudaStream_t st, float* field, int F, int R, int C, const PixOps& ops,
+                const FieldInfo& fi) {
+  if (!ops.n) return CSG_OK;
+  CSG_CHECK(F > 0 && F < 65536 && (long long)R * C < (1LL << 31), CSG_E_SHAPE,
+            "element pass: bad shape");
+  dim3 grid(grid_for((long long)R * C / 4 + 1, 256, 1024), F);
+  k_pixops<<<grid, 256, 0, st>>>(field, R, C, ops, fi);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
 }
 
 // ------------------------------------------------------------- hex FPM
@@ -260,16 +202,18 @@ extern "C" {
 int csg_point_source(csg_ctx* ctx, float* field, int n_fields, int rows, int cols, double dx,
                      double dy, const double* amp, const double* tip, const double* tilt) {
   CSG_CHECK(ctx && field && amp && tip && tilt, CSG_E_ARG, "csg_point_source: null argument");
-  CSG_CHECK(n_fields > 0 && n_fields < 65536 && rows > 0 && cols > 0, CSG_E_SHAPE,
-            "csg_point_source: bad shape");
+  CSG_CHECK(n_fields > 0 && rows > 0 && cols > 0, CSG_E_SHAPE, "csg_point_source: bad shape");
   (void)dx;
-  (void)dy;  // the phase only depends on the pixel index (x / Lx = index / C)
+  (void)dy;  // the phase depends on the pixel index only (x / Lx = index / C)
   DeviceGuard g(ctx->device);
-  dim3 grid(grid_for((long long)rows * cols, 256, 512), n_fields);
-  k_point_source<<<grid, 256, 0, ctx->stream>>>(field, n_fields, rows, cols, dx, dy, amp, tip,
-                                                tilt);
-  CSG_LAUNCH_CHECK();
-  return CSG_OK;
+  PixOps ops;
+  ops.n = 1;
+  ops.kind[0] = OP_SOURCE;
+  FieldInfo fi;
+  fi.amp = amp;
+  fi.tip = tip;
+  fi.tilt = tilt;
+  return pixops_pass(ctx->stream, field, n_fields, rows, cols, ops, fi);
 }
 
 int csg_mask_real(csg_ctx* ctx, float* field, int n_fields, int rows, int cols, const float* mask,
@@ -277,24 +221,27 @@ int csg_mask_real(csg_ctx* ctx, float* field, int n_fields, int rows, int cols, 
   CSG_CHECK(ctx && field && mask, CSG_E_ARG, "csg_mask_real: null argument");
   CSG_CHECK(n_fields > 0 && rows > 0 && cols > 0, CSG_E_SHAPE, "csg_mask_real: bad shape");
   DeviceGuard g(ctx->device);
-  const long long plane = (long long)rows * cols;
-  k_mask_real<<<grid_for(plane * n_fields, 256), 256, 0, ctx->stream>>>(field, n_fields, plane,
-                                                                        mask, ref_quirk);
-  CSG_LAUNCH_CHECK();
-  return CSG_OK;
+  PixOps ops;
+  ops.n = 1;
+  ops.kind[0] = OP_MASK;
+  ops.a[0] = mask;
+  ops.param[0] = ref_quirk ? 1.f : 0.f;
+  return pixops_pass(ctx->stream, field, n_fields, rows, cols, ops, FieldInfo());
 }
 
 int csg_phase_screen(csg_ctx* ctx, float* field, int n_fields, int rows, int cols, const float* sag,
                      const double* lambda, double sign) {
   CSG_CHECK(ctx && field && sag && lambda, CSG_E_ARG, "csg_phase_screen: null argument");
-  CSG_CHECK(n_fields > 0 && n_fields < 65536 && rows > 0 && cols > 0, CSG_E_SHAPE,
-            "csg_phase_screen: bad shape");
+  CSG_CHECK(n_fields > 0 && rows > 0 && cols > 0, CSG_E_SHAPE, "csg_phase_screen: bad shape");
   DeviceGuard g(ctx->device);
-  const long long plane = (long long)rows * cols;
-  dim3 grid(grid_for(plane, 256, 512), n_fields);
-  k_phase_screen<<<grid, 256, 0, ctx->stream>>>(field, n_fields, plane, sag, lambda, sign);
-  CSG_LAUNCH_CHECK();
-  return CSG_OK;
+  PixOps ops;
+  ops.n = 1;
+  ops.kind[0] = OP_PHASE;
+  ops.a[0] = sag;
+  ops.param[0] = (float)sign;
+  FieldInfo fi;
+  fi.lam = lambda;
+  return pixops_pass(ctx->stream, field, n_fields, rows, cols, ops, fi);
 }
 
 int csg_complex_mask(csg_ctx* ctx, float* field, int n_fields, int rows, int cols,
@@ -303,10 +250,14 @@ int csg_complex_mask(csg_ctx* ctx, float* field, int n_fields, int rows, int col
   CSG_CHECK(n_fields > 0 && mrows > 0 && mcols > 0 && mrows <= rows && mcols <= cols,
             CSG_E_SHAPE, "csg_complex_mask: mask larger than field");
   DeviceGuard g(ctx->device);
-  k_complex_mask<<<grid_for((long long)mrows * mcols * n_fields, 256), 256, 0, ctx->stream>>>(
-      field, n_fields, rows, cols, amp, ph, mrows, mcols);
-  CSG_LAUNCH_CHECK();
-  return CSG_OK;
+  PixOps ops;
+  ops.n = 1;
+  ops.kind[0] = OP_CMASK;
+  ops.a[0] = amp;
+  ops.b[0] = ph;
+  ops.mr[0] = mrows;
+  ops.mc[0] = mcols;
+  return pixops_pass(ctx->stream, field, n_fields, rows, cols, ops, FieldInfo());
 }
 
 int csg_hex_mask(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S, int n_sub,

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "ctx.hpp"
+#include "pixops.cuh"
 #include "tc_gemm.cuh"
 
 namespace csg {
@@ -103,33 +104,57 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
   }
 }
 
-// Data split: planar fp32 [F][2][R][C] (optionally times a complex multiplier
-// [n_mul][2][R][C] chosen by mul_idx[f]) -> bf16 [F][3][2][R][C].
+// Data split: planar fp32 [F][2][R][C] -> (element ops `pre`) -> (times a
+// complex multiplier [n_mul][2][R][C] chosen by mul_idx[f]) -> bf16
+// [F][3][2][R][C]. Four pixels per thread (C is a multiple of 8); grid.y is
+// the field.
 __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int R,
-                              int C, int F, const float* __restrict__ mul,
-                              const int* __restrict__ mul_idx) {
-  const long long plane = (long long)R * C;
-  const long long n = plane * F;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int f = (int)(i / plane);
-    const long long o = i % plane;
-    float re = in[(long long)f * 2 * plane + o];
-    float im = in[(long long)f * 2 * plane + plane + o];
-    if (mul) {
-      const long long mb = (long long)mul_idx[f] * 2 * plane;
-      const float mr = mul[mb + o], mi = mul[mb + plane + o];
-      const float tr = re * mr - im * mi;
-      im = re * mi + im * mr;
-      re = tr;
-    }
-    __nv_bfloat16 a[3], b[3];
-    split3(re, a[0], a[1], a[2]);
-    split3(im, b[0], b[1], b[2]);
+                              int C, const float* __restrict__ mul,
+                              const int* __restrict__ mul_idx, PixOps pre, FieldInfo fi) {
+  const int f = blockIdx.y;
+  const int plane = R * C;
+  PixConsts k;
+  if (pre.n) pix_consts(pre, fi, f, R, C, k);
+  const float* ire = in + (size_t)f * 2 * plane;
+  const float* iim = ire + plane;
+  const float* mre = mul ? mul + (size_t)mul_idx[f] * 2 * plane : nullptr;
+  const int nv = plane / 4;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    const float4 a4 = reinterpret_cast<const float4*>(ire)[v];
+    const float4 b4 = reinterpret_cast<const float4*>(iim)[v];
+    float xr[4] = {a4.x, a4.y, a4.z, a4.w}, xi[4] = {b4.x, b4.y, b4.z, b4.w};
+    const int e0 = 4 * v;
+    if (pre.n) {
+      const int r = e0 / C, c = e0 % C;
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      out[((long long)(f * 3 + q) * 2 + 0) * plane + o] = a[q];
-      out[((long long)(f * 3 + q) * 2 + 1) * plane + o] = b[q];
+      for (int q = 0; q < 4; ++q) pix_apply(pre, k, r, c + q, R, C, xr[q], xi[q]);
+    }
+    if (mre) {
+      const float4 m4 = reinterpret_cast<const float4*>(mre)[v];
+      const float4 n4 = reinterpret_cast<const float4*>(mre + plane)[v];
+      const float mr[4] = {m4.x, m4.y, m4.z, m4.w}, mi[4] = {n4.x, n4.y, n4.z, n4.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float tr = xr[q] * mr[q] - xi[q] * mi[q];
+        xi[q] = xr[q] * mi[q] + xi[q] * mr[q];
+        xr[q] = tr;
+      }
+    }
+    __nv_bfloat16 a[3][4], b[3][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      split3(xr[q], a[0][q], a[1][q], a[2][q]);
+      split3(xi[q], b[0][q], b[1][q], b[2][q]);
+    }
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+      __nv_bfloat16* o = out + ((size_t)(f * 3 + p) * 2) * plane + e0;
+      *reinterpret_cast<uint2*>(o) = make_uint2(
+          (uint32_t)__bfloat16_as_ushort(a[p][0]) | ((uint32_t)__bfloat16_as_ushort(a[p][1]) << 16),
+          (uint32_t)__bfloat16_as_ushort(a[p][2]) | ((uint32_t)__bfloat16_as_ushort(a[p][3]) << 16));
+      *reinterpret_cast<uint2*>(o + plane) = make_uint2(
+          (uint32_t)__bfloat16_as_ushort(b[p][0]) | ((uint32_t)__bfloat16_as_ushort(b[p][1]) << 16),
+          (uint32_t)__bfloat16_as_ushort(b[p][2]) | ((uint32_t)__bfloat16_as_ushort(b[p][3]) << 16));
     }
   }
 }
@@ -267,8 +292,13 @@ size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
   return (size_t)n_fields * 12 * ((size_t)m->ny * m->nx + (size_t)m->no * m->ny);
 }
 
-int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
-                    const int* slot, int accumulate, const float* in_mul, const int* mul_idx) {
+}  // extern "C"
+
+// MFT with element ops applied to the input pixels in the operand split
+// (the chain executor fuses the elements before a transform here).
+int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
+                         const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
+                         const PixOps& pre, const FieldInfo& fi) {
   CSG_CHECK(ctx && m && in && out && slot, CSG_E_ARG, "csg_mft_execute: null argument");
   CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_mft_execute: n_fields must be positive");
   CSG_CHECK(!in_mul || mul_idx, CSG_E_ARG, "csg_mft_execute: in_mul needs mul_idx");
@@ -283,8 +313,9 @@ int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n
   const double F = n_fields;
   {
     ProfScope ps(ctx, "mft_split", 0, F * m->ny * m->nx * (8.0 + 12.0 + (in_mul ? 8.0 : 0.0)));
-    k_split_field<<<grid_for((long long)n_fields * m->ny * m->nx, 256), 256, 0, st>>>(
-        in, sin, m->ny, m->nx, n_fields, in_mul, mul_idx);
+    CSG_CHECK(n_fields < 65536, CSG_E_SHAPE, "csg_mft_execute: too many fields in one call");
+    dim3 grid(grid_for((long long)m->ny * m->nx / 4, 256, 1024), n_fields);
+    k_split_field<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, in_mul, mul_idx, pre, fi);
     CSG_LAUNCH_CHECK();
   }
 
@@ -347,4 +378,9 @@ int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n
   return CSG_OK;
 }
 
-}  // extern "C"
+extern "C" int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out,
+                               int n_fields, const int* slot, int accumulate, const float* in_mul,
+                               const int* mul_idx) {
+  return mft_execute_ops(ctx, m, in, out, n_fields, slot, accumulate, in_mul, mul_idx, PixOps(),
+                         FieldInfo());
+}

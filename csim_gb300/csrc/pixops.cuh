@@ -1,0 +1,140 @@
+// Per-pixel element operations fused into the prologue or epilogue of the
+// pass that already reads or writes the field (FFT passes, the MFT operand
+// split, or one standalone elementwise pass). Each op is one reference
+// element applied to one pixel:
+//   OP_SOURCE  efield::init_point_sources (efield.cpp:179-206): replaces the
+//              pixel by amp exp(2 pi i (2 x tip / Lx + 2 y tilt / Ly))
+//   OP_MASK    mask::execute (mask.cpp:38-46): * m, or * (m + i m)
+//   OP_PHASE   mirror / deformableMirror: * exp(-sign 4 pi i sag / lambda)
+//   OP_CMASK   complexMask (complexMask.cpp:24-55): centred amp exp(-i ph)
+// Phases are products of an fp32 datum and an FP64 per-field constant held
+// as an fp32 (hi, lo) pair, reduced modulo one turn with the product's
+// rounding error folded back (fmaf).
+#pragma once
+#include "common.cuh"
+
+namespace csg {
+
+enum PixOpKind { OP_SOURCE = 1, OP_MASK = 2, OP_PHASE = 3, OP_CMASK = 4 };
+constexpr int MAX_PIXOPS = 6;
+
+struct PixOps {
+  int n = 0;
+  int kind[MAX_PIXOPS] = {};
+  const float* a[MAX_PIXOPS] = {};  // mask, sag or amplitude
+  const float* b[MAX_PIXOPS] = {};  // phase of a complex mask
+  float param[MAX_PIXOPS] = {};     // OP_MASK: quirk flag; OP_PHASE: mirror sign
+  int mr[MAX_PIXOPS] = {}, mc[MAX_PIXOPS] = {};
+};
+
+// Per-field inputs the ops need (device arrays indexed by field).
+struct FieldInfo {
+  const double* lam = nullptr;
+  const double* amp = nullptr;
+  const double* tip = nullptr;
+  const double* tilt = nullptr;
+};
+
+// Per-field constants, computed once per CTA.
+struct PixConsts {
+  float khi[MAX_PIXOPS], klo[MAX_PIXOPS];  // OP_PHASE turns per metre
+  float sxh, sxl, syh, syl, amp;           // OP_SOURCE
+};
+
+__device__ __forceinline__ float frac_prod(float a, float khi, float klo) {
+  const float p = a * khi;
+  float e = fmaf(a, khi, -p);
+  e = fmaf(a, klo, e);
+  return (p - rintf(p)) + e;
+}
+
+__device__ __forceinline__ void split_f64_pair(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+__device__ __forceinline__ void pix_consts(const PixOps& ops, const FieldInfo& fi, int f, int R,
+                                           int C, PixConsts& k) {
+#pragma unroll
+  for (int i = 0; i < MAX_PIXOPS; ++i) {
+    if (i >= ops.n) break;
+    if (ops.kind[i] == OP_PHASE) {
+      split_f64_pair(-(double)ops.param[i] * 2.0 / fi.lam[f], k.khi[i], k.klo[i]);
+    } else if (ops.kind[i] == OP_SOURCE) {
+      split_f64_pair(2.0 * fi.tip[f] / (double)C, k.sxh, k.sxl);
+      split_f64_pair(2.0 * fi.tilt[f] / (double)R, k.syh, k.syl);
+      k.amp = (float)fi.amp[f];
+    }
+  }
+}
+
+// Apply the ops to pixel (r, c) of an R x C field.
+__device__ __forceinline__ void pix_apply(const PixOps& ops, const PixConsts& k, int r, int c,
+                                          int R, int C, float& re, float& im) {
+#pragma unroll
+  for (int i = 0; i < MAX_PIXOPS; ++i) {  // static indices keep k in registers
+    if (i >= ops.n) break;
+    const int kind = ops.kind[i];
+    if (kind == OP_SOURCE) {
+      const float xc = (float)c - 0.5f * (float)(C - 1);
+      const float yr = (float)r - 0.5f * (float)(R - 1);
+      float t = frac_prod(xc, k.sxh, k.sxl) + frac_prod(yr, k.syh, k.syl);
+      t -= rintf(t);
+      float s, co;
+      sincospif(2.f * t, &s, &co);
+      re = k.amp * co;
+      im = k.amp * s;
+    } else if (kind == OP_MASK) {
+      const float m = ops.a[i][(size_t)r * C + c];
+      if (ops.param[i] != 0.f) {
+        const float t = m * (re - im);
+        im = m * (re + im);
+        re = t;
+      } else {
+        re *= m;
+        im *= m;
+      }
+    } else if (kind == OP_PHASE) {
+      const float t = frac_prod(ops.a[i][(size_t)r * C + c], k.khi[i], k.klo[i]);
+      float s, co;
+      sincospif(2.f * t, &s, &co);
+      const float xr = re;
+      re = xr * co - im * s;
+      im = xr * s + im * co;
+    } else if (kind == OP_CMASK) {
+      const int r0 = R / 2 - ops.mr[i] / 2, c0 = C / 2 - ops.mc[i] / 2;
+      const int rr = r - r0, cc = c - c0;
+      if (rr >= 0 && rr < ops.mr[i] && cc >= 0 && cc < ops.mc[i]) {
+        const size_t o = (size_t)rr * ops.mc[i] + cc;
+        float s, co;
+        sincosf(-ops.b[i][o], &s, &co);
+        const float a = ops.a[i][o];
+        const float xr = re;
+        re = a * (xr * co - im * s);
+        im = a * (xr * s + im * co);
+      }
+    }
+  }
+}
+
+// Standalone pass: field [F][2][R][C] <- ops(field).
+int pixops_pass(cudaStream_t st, float* field, int F, int R, int C, const PixOps& ops,
+                const FieldInfo& fi);
+
+struct FresnelArgs {
+  const double* lambda;  // per field
+  double z;
+  double ap_rad;
+};
+
+// 2-D FFT (direction -1 / +1) or, with fa, Fresnel propagation of F square
+// N x N fields with element ops fused before (pro) and after (epi).
+int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
+                const PixOps& pro, const PixOps& epi, const FieldInfo& fi);
+
+// MFT with element ops applied to the input in the operand split.
+int mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
+                    const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
+                    const PixOps& pre, const FieldInfo& fi);
+
+}  // namespace csg
