@@ -91,6 +91,9 @@ __device__ __forceinline__ void dif_stage(float* xr, float* xi) {
         if (m == 0) {
           xr[base + k + HALF] = dr;
           xi[base + k + HALF] = di;
+        } else if (m == 4) {  // times -i (forward) or +i (inverse)
+          xr[base + k + HALF] = INV ? -di : di;
+          xi[base + k + HALF] = INV ? dr : -dr;
         } else {
           const float c = w16c(m), s = INV ? w16s(m) : -w16s(m);
           xr[base + k + HALF] = dr * c - di * s;
@@ -108,10 +111,12 @@ struct RowAddr {
   static constexpr int NP = N + N / 16;
   __device__ __forceinline__ static int at(int t, int m) { return t * NP + m + (m >> 4); }
 };
-// Column layout: element m of column t at m * COLS + t.
+// Column layout: element m of column t at m * (COLS + 1) + t (the odd row
+// pitch spreads stride-16 stores over all banks).
 template <int COLS>
 struct ColAddr {
-  __device__ __forceinline__ static int at(int t, int m) { return m * COLS + t; }
+  static constexpr int PITCH = COLS + 1;
+  __device__ __forceinline__ static int at(int t, int m) { return m * PITCH + t; }
 };
 
 // One Stockham stage of radix R at sub-length L; each thread owns 16 / R
@@ -160,27 +165,24 @@ __device__ __forceinline__ void stockham_stage(float* __restrict__ re, float* __
   __syncthreads();
 }
 
-// Full transform: a first stage of radix 2^(log2 N mod 4) if needed, then
-// radix-16 stages.
+// Full transform: radix-16 stages first, then one radix 2^(log2 N mod 4)
+// stage if needed. (Radix 16 first keeps every stage's stores either
+// contiguous or at stride 16, which the one-in-16 padding makes
+// conflict-free.)
 template <int N, int L, bool INV, class A>
-__device__ __forceinline__ void stockham_rest(float* re, float* im, int t, int u,
+__device__ __forceinline__ void stockham_from(float* re, float* im, int t, int u,
                                               const float2* tw) {
-  if constexpr (L < N) {
+  if constexpr (L * 16 <= N) {
     stockham_stage<N, 16, L, INV, A>(re, im, t, u, tw);
-    stockham_rest<N, L * 16, INV, A>(re, im, t, u, tw);
+    stockham_from<N, L * 16, INV, A>(re, im, t, u, tw);
+  } else if constexpr (L < N) {
+    stockham_stage<N, N / L, L, INV, A>(re, im, t, u, tw);
   }
 }
 
 template <int N, bool INV, class A>
 __device__ __forceinline__ void smem_fft(float* re, float* im, int t, int u, const float2* tw) {
-  constexpr int REM = ilog2c(N) % 4;
-  if constexpr (REM == 0) {
-    stockham_rest<N, 1, INV, A>(re, im, t, u, tw);
-  } else {
-    constexpr int R0 = 1 << REM;
-    stockham_stage<N, R0, 1, INV, A>(re, im, t, u, tw);
-    stockham_rest<N, R0, INV, A>(re, im, t, u, tw);
-  }
+  stockham_from<N, 1, INV, A>(re, im, t, u, tw);
 }
 
 template <int N>
@@ -195,7 +197,7 @@ struct ColCfg {
   static constexpr int TPT = N / 16;
   static constexpr int COLS = N >= 2048 ? 16 * 1024 / N : 16;
   static constexpr int THREADS = COLS * TPT;
-  static constexpr size_t SMEM = (size_t)COLS * N * 8;
+  static constexpr size_t SMEM = (size_t)(COLS + 1) * N * 8;
 };
 
 // Row pass with fused element prologue / epilogue.
@@ -218,38 +220,31 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS)
   if (pro.n) pix_consts(pro, fi, f, N, N, kp);
   if (epi.n) pix_consts(epi, fi, f, N, N, ke);
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // source overwrites: skip the read
-  constexpr int NV = CF::ROWS * N / 4;
-#pragma unroll 2
-  for (int v = threadIdx.x; v < NV; v += CF::THREADS) {
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+  // one element per thread per instruction: coalesced global access and
+  // consecutive (conflict-free) shared-memory addresses
+  constexpr int NE = CF::ROWS * N;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < NE; e += CF::THREADS) {
+    const int t = e / N, m = e % N;
+    float xr = 0.f, xi = 0.f;
     if (!gen) {
-      a = reinterpret_cast<const float4*>(fre)[v];
-      b = reinterpret_cast<const float4*>(fim)[v];
+      xr = fre[e];
+      xi = fim[e];
     }
-    const int e0 = 4 * v, t = e0 / N, m = e0 % N;
-    float xr[4] = {a.x, a.y, a.z, a.w}, xi[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (pro.n) pix_apply(pro, kp, r0 + t, m + q, N, N, xr[q], xi[q]);
-      re[A::at(t, m + q)] = xr[q];
-      im[A::at(t, m + q)] = xi[q];
-    }
+    if (pro.n) pix_apply(pro, kp, r0 + t, m, N, N, xr, xi);
+    re[A::at(t, m)] = xr;
+    im[A::at(t, m)] = xi;
   }
   __syncthreads();
   const int t = threadIdx.x / CF::TPT, u = threadIdx.x % CF::TPT;
   smem_fft<N, INV, A>(re, im, t, u, tw);
-#pragma unroll 2
-  for (int v = threadIdx.x; v < NV; v += CF::THREADS) {
-    const int e0 = 4 * v, tt = e0 / N, m = e0 % N;
-    float xr[4], xi[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      xr[q] = re[A::at(tt, m + q)] * scale;
-      xi[q] = im[A::at(tt, m + q)] * scale;
-      if (epi.n) pix_apply(epi, ke, r0 + tt, m + q, N, N, xr[q], xi[q]);
-    }
-    reinterpret_cast<float4*>(fre)[v] = make_float4(xr[0], xr[1], xr[2], xr[3]);
-    reinterpret_cast<float4*>(fim)[v] = make_float4(xi[0], xi[1], xi[2], xi[3]);
+#pragma unroll 4
+  for (int e = threadIdx.x; e < NE; e += CF::THREADS) {
+    const int tt = e / N, m = e % N;
+    float xr = re[A::at(tt, m)] * scale, xi = im[A::at(tt, m)] * scale;
+    if (epi.n) pix_apply(epi, ke, r0 + tt, m, N, N, xr, xi);
+    fre[e] = xr;
+    fim[e] = xi;
   }
 }
 
@@ -261,7 +256,7 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS)
   using A = ColAddr<CF::COLS>;
   extern __shared__ float sm[];
   float* re = sm;
-  float* im = sm + CF::COLS * N;
+  float* im = sm + A::PITCH * N;
   constexpr int CPF = N / CF::COLS;
   const int f = blockIdx.x / CPF;
   const int c0 = (blockIdx.x % CPF) * CF::COLS;
@@ -269,10 +264,11 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS)
   float* fre = field + (size_t)f * 2 * plane + c0;
   float* fim = fre + plane;
   constexpr int NE = CF::COLS * N;
+#pragma unroll 4
   for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
     const int r = i / CF::COLS, c = i % CF::COLS;
-    re[i] = fre[(size_t)r * N + c];
-    im[i] = fim[(size_t)r * N + c];
+    re[A::at(c, r)] = fre[(size_t)r * N + c];
+    im[A::at(c, r)] = fim[(size_t)r * N + c];
   }
   __syncthreads();
   const int t = threadIdx.x % CF::COLS, u = threadIdx.x / CF::COLS;
@@ -303,23 +299,27 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS)
       tt -= rintf(tt);
       float sn, cs;
       sincospif(2.f * tt, &sn, &cs);
-      const float xr = re[i], xi = im[i];
-      re[i] = xr * cs - xi * sn;
-      im[i] = xr * sn + xi * cs;
+      const int a = A::at(i % CF::COLS, r);
+      const float xr = re[a], xi = im[a];
+      re[a] = xr * cs - xi * sn;
+      im[a] = xr * sn + xi * cs;
     }
     __syncthreads();
     smem_fft<N, true, A>(re, im, t, u, tw);
   }
+#pragma unroll 4
   for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
     const int r = i / CF::COLS, c = i % CF::COLS;
-    fre[(size_t)r * N + c] = re[i];
-    fim[(size_t)r * N + c] = im[i];
+    fre[(size_t)r * N + c] = re[A::at(c, r)];
+    fim[(size_t)r * N + c] = im[A::at(c, r)];
   }
 }
 
 template <typename K>
 static int prep_smem(K kern, size_t bytes) {
   CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  // prefer the largest shared-memory carveout so several CTAs fit per SM
+  CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   return CSG_OK;
 }
 

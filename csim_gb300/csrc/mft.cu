@@ -196,7 +196,76 @@ struct csg_mft {
   __nv_bfloat16* op2 = nullptr;  // [slot][3][3][mo][ny]
   Scratch split_in;               // [F][3][2][ny][nx] bf16
   Scratch tt;                     // [F][3][2][no][ny] bf16
+  int bn = 0;                     // tile width chosen by the autotuner (0: default)
+  int tuned_fields = 0;           // batch size the choice was measured at
+  float tuned_ms[2] = {0, 0};     // measured time of BN = 128, 256
 };
+
+namespace {
+// Tile autotuner: times the transform with N-tile widths 128 and 256 at the
+// batch size it will run at (zero input, every field on slot 0) and keeps the
+// faster. Runs outside graph capture (csg_mft_reserve is called before).
+int autotune(csg_mft* m, int F) {
+  if (m->tuned_fields == F) return CSG_OK;
+  const char* env = getenv("CSG_MFT_AUTOTUNE");
+  if (env && env[0] == '0') {
+    m->bn = 0;
+    m->tuned_fields = F;
+    return CSG_OK;
+  }
+  cudaStream_t st = m->ctx->stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cs);
+  if (cs != cudaStreamCaptureStatusNone) return CSG_OK;
+  float *in = nullptr, *out = nullptr;
+  int* slot = nullptr;
+  const size_t in_b = (size_t)F * 2 * m->ny * m->nx * 4, out_b = (size_t)F * 2 * m->mo * m->no * 4;
+  if (cudaMalloc(&in, in_b) != cudaSuccess || cudaMalloc(&out, out_b) != cudaSuccess ||
+      cudaMalloc(&slot, (size_t)F * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(in);
+    cudaFree(out);
+    cudaFree(slot);
+    return CSG_OK;  // keep the default tile on allocation pressure
+  }
+  cudaMemsetAsync(in, 0, in_b, st);
+  cudaMemsetAsync(slot, 0, (size_t)F * sizeof(int), st);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int cand[2] = {128, 256};
+  float best = 1e30f;
+  int best_bn = 0, rc = CSG_OK;
+  const bool prof = m->ctx->prof;
+  m->ctx->prof = false;
+  for (int i = 0; i < 2 && !rc; ++i) {
+    m->bn = cand[i];
+    rc = mft_execute_ops(m->ctx, m, in, out, F, slot, 0, nullptr, nullptr, PixOps(), FieldInfo());
+    cudaEventRecord(a, st);
+    for (int r = 0; r < 2 && !rc; ++r)
+      rc = mft_execute_ops(m->ctx, m, in, out, F, slot, 0, nullptr, nullptr, PixOps(),
+                           FieldInfo());
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    m->tuned_ms[i] = ms / 2;
+    if (ms < best) {
+      best = ms;
+      best_bn = cand[i];
+    }
+  }
+  m->ctx->prof = prof;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(in);
+  cudaFree(out);
+  cudaFree(slot);
+  m->bn = best_bn;
+  m->tuned_fields = F;
+  return rc;
+}
+}  // namespace
 
 extern "C" {
 
@@ -284,7 +353,18 @@ int csg_mft_reserve(csg_mft* m, int n_fields) {
   DeviceGuard g(m->ctx->device);
   int rc = m->split_in.ensure((size_t)n_fields * 12 * m->ny * m->nx);
   if (!rc) rc = m->tt.ensure((size_t)n_fields * 12 * m->no * m->ny);
+  if (!rc) rc = autotune(m, n_fields);
   return rc;
+}
+
+// Tile width the autotuner chose for the last reserved batch size and the
+// times it measured (ms per transform for widths 128 and 256).
+int csg_mft_tuning(csg_mft* m, int* bn, float* ms128, float* ms256) {
+  CSG_CHECK(m && bn, CSG_E_ARG, "csg_mft_tuning: null argument");
+  *bn = m->bn;
+  if (ms128) *ms128 = m->tuned_ms[0];
+  if (ms256) *ms256 = m->tuned_ms[1];
+  return CSG_OK;
 }
 
 size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
@@ -319,7 +399,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     CSG_LAUNCH_CHECK();
   }
 
-  const int bn1 = m->no >= 256 ? 256 : 128;
+  const int bn1 = m->bn ? m->bn : (m->no >= 256 ? 256 : 128);
   // ---- stage 1: T^T = split(in . B_x^T)^T
   {
     CUtensorMap ta, tb;

@@ -75,7 +75,10 @@ __device__ __forceinline__ void pix_apply(const PixOps& ops, const PixConsts& k,
   for (int i = 0; i < MAX_PIXOPS; ++i) {  // static indices keep k in registers
     if (i >= ops.n) break;
     const int kind = ops.kind[i];
-    if (kind == OP_SOURCE) {
+    if (kind == OP_SOURCE && k.sxh == 0.f && k.syh == 0.f && k.sxl == 0.f && k.syl == 0.f) {
+      re = k.amp;  // on-axis source: flat phase
+      im = 0.f;
+    } else if (kind == OP_SOURCE) {
       const float xc = (float)c - 0.5f * (float)(C - 1);
       const float yr = (float)r - 0.5f * (float)(R - 1);
       float t = frac_prod(xc, k.sxh, k.sxl) + frac_prod(yr, k.syh, k.syl);

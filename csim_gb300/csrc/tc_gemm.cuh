@@ -133,7 +133,8 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
       : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+// 32 lanes x 32 columns of fp32 from tensor memory (no wait).
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
       "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -145,6 +146,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
         "=r"(r[31])
       : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
@@ -336,12 +339,15 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!ok) break;
       tc_fence_after();
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(ts * BN + h * CPW);
+      // two loads in flight per wait
 #pragma unroll
-      for (int cb = 0; cb < CPW; cb += 32) {
-        uint32_t r[32];
-        tmem_ld32(taddr + cb, r);
+      for (int cb = 0; cb < CPW; cb += 64) {
+        uint32_t r[64];
+        tmem_ld32_nowait(taddr + cb, r);
+        tmem_ld32_nowait(taddr + cb + 32, r + 32);
+        tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) acc[cb + j] += __uint_as_float(r[j]);
+        for (int j = 0; j < 64; ++j) acc[cb + j] += __uint_as_float(r[j]);
       }
       tc_fence_before();
       __syncwarp();

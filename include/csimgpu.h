@@ -250,8 +250,12 @@ int csg_chain_execute(csg_chain* chain, int calibrating, int use_graph);
 int csg_chain_image(csg_chain* chain, float** dev_image, int* n_out);
 int csg_chain_field(csg_chain* chain, float** dev_field);
 /* Pre-size an MFT plan's scratch for n_fields (so graph capture allocates
- * nothing). */
+ * nothing) and autotune its tensor-core tile width (128 or 256 output
+ * columns per tile) by timing both at that batch size. Set the environment
+ * variable CSG_MFT_AUTOTUNE=0 to keep the default width. */
 int csg_mft_reserve(csg_mft* plan, int n_fields);
+/* The chosen tile width and the measured ms per transform of each width. */
+int csg_mft_tuning(csg_mft* plan, int* bn, float* ms128, float* ms256);
 
 /* ---------------------------------------------------- intensity / contrast */
 /* regionContrast::compute_intensity (regionContrast.cpp:124-143) and the
