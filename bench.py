@@ -205,15 +205,15 @@ def main():
             ctx.region_reduce(img, 1, reg.pix, mode=0, scale=1.0 / cmax, out=contrast)
             return img
 
-        # kernels per step (graph replays launch the same kernels)
-        n0 = _lib.api["csg_launch_count"]()
-        cor.execute(calibrating=False, use_graph=False)
-        ctx.region_reduce(cor.execute(use_graph=False), 1, reg.pix, mode=0, scale=1.0 / cmax,
-                          out=contrast)
-        n1 = _lib.api["csg_launch_count"]()
-        launches_per_step = (n1 - n0) // 2
         for _ in range(args.warmup):
             step()
+        ctx.sync()
+        # kernels per step, counted on an eager (non-graph) step after the
+        # warm-up; graph replays launch exactly these kernels
+        n0 = _lib.api["csg_launch_count"]()
+        ctx.region_reduce(cor.execute(use_graph=False), 1, reg.pix, mode=0, scale=1.0 / cmax,
+                          out=contrast)
+        launches_per_step = _lib.api["csg_launch_count"]() - n0
         ctx.sync()
 
     hbm_peak, tc_peak, peak_kind = peaks()
@@ -284,6 +284,9 @@ def main():
         _lib.call("csg_profile_report", ctx.h, buf, len(buf))
         _lib.call("csg_profile", ctx.h, 0)
     prof = json.loads(buf.value.decode())
+    tbuf = C.create_string_buffer(1 << 16)
+    _lib.call("csg_mft_tuning_log", tbuf, len(tbuf))
+    tuning = json.loads(tbuf.value.decode())
     g = prof.get("mft_gemm", {"count": 1, "ms": float("nan"), "flops": 0.0})
     gemm_tflops = g["flops"] / (g["ms"] / 1e3) / 1e12
     total_ms = sum(v["ms"] for v in prof.values())
@@ -296,7 +299,10 @@ def main():
                 "avg_launch_ms": g["ms"] / g["count"],
                 "executed_bf16_tflops": gemm_tflops * split_terms,
                 "share_of_step": g["ms"] / total_ms if total_ms else None,
-                "kernels": {k: {"count": v["count"], "ms": round(v["ms"], 4)} for k, v in prof.items()}}
+                "kernels": {k: {"count": v["count"], "ms": round(v["ms"], 4),
+                                **({"gbs": round(v["bytes"] / v["ms"] / 1e6, 1)} if v["bytes"] else {})}
+                            for k, v in prof.items()},
+                "mft_tile_autotune": tuning}
     if "fresnel_3pass" in prof:
         fz = prof["fresnel_3pass"]
         roofline["fresnel_gbs"] = fz["bytes"] / (fz["ms"] / 1e3) / 1e9

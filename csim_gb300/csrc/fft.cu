@@ -318,46 +318,63 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS)
 template <typename K>
 static int prep_smem(K kern, size_t bytes) {
   CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  // prefer the largest shared-memory carveout so several CTAs fit per SM
-  CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  // optional shared-memory carveout preference (percent), for tuning
+  static const char* cv = getenv("CSG_FFT_CARVEOUT");
+  if (cv) CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, atoi(cv)));
   return CSG_OK;
 }
 
 template <int N>
-static int run_fft(cudaStream_t st, float* field, int F, int direction, const FresnelArgs* fa,
+static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const FresnelArgs* fa,
                    const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw) {
   using RC = RowCfg<N>;
   using CC = ColCfg<N>;
+  cudaStream_t st = ctx->stream;
   const int rgrid = F * (N / RC::ROWS), cgrid = F * (N / CC::COLS);
   const float inv_scale = 1.f / ((float)N * (float)N);
+  const double pass_bytes = (double)F * N * N * 16.0;
   const PixOps none;
   int rc;
+  auto rows = [&](bool inv, float scale, const PixOps& p, const PixOps& e) -> int {
+    const bool gen = p.n && p.kind[0] == OP_SOURCE;
+    ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, pass_bytes * (gen ? 0.5 : 1.0));
+    if (inv) {
+      if ((rc = prep_smem(k_fft_rows<N, true>, RC::SMEM))) return rc;
+      k_fft_rows<N, true><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
+    } else {
+      if ((rc = prep_smem(k_fft_rows<N, false>, RC::SMEM))) return rc;
+      k_fft_rows<N, false><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
+    }
+    CSG_LAUNCH_CHECK();
+    return CSG_OK;
+  };
+  auto cols = [&](int mode) -> int {
+    ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, pass_bytes);
+    if (mode == 2) {
+      if ((rc = prep_smem(k_fft_cols<N, 2>, CC::SMEM))) return rc;
+      k_fft_cols<N, 2><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
+    } else if (mode == 1) {
+      if ((rc = prep_smem(k_fft_cols<N, 1>, CC::SMEM))) return rc;
+      k_fft_cols<N, 1><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    } else {
+      if ((rc = prep_smem(k_fft_cols<N, 0>, CC::SMEM))) return rc;
+      k_fft_cols<N, 0><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    }
+    CSG_LAUNCH_CHECK();
+    return CSG_OK;
+  };
   if (fa) {
-    if ((rc = prep_smem(k_fft_rows<N, false>, RC::SMEM))) return rc;
-    k_fft_rows<N, false><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, 1.f, tw, pro, none, fi);
-    CSG_LAUNCH_CHECK();
-    if ((rc = prep_smem(k_fft_cols<N, 2>, CC::SMEM))) return rc;
-    k_fft_cols<N, 2><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
-    CSG_LAUNCH_CHECK();
-    if ((rc = prep_smem(k_fft_rows<N, true>, RC::SMEM))) return rc;
-    k_fft_rows<N, true><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, inv_scale, tw, none, epi, fi);
-    CSG_LAUNCH_CHECK();
+    if ((rc = rows(false, 1.f, pro, none))) return rc;
+    if ((rc = cols(2))) return rc;
+    return rows(true, inv_scale, none, epi);
   } else if (direction < 0) {
-    if ((rc = prep_smem(k_fft_rows<N, false>, RC::SMEM))) return rc;
-    k_fft_rows<N, false><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, 1.f, tw, pro, none, fi);
-    CSG_LAUNCH_CHECK();
-    if ((rc = prep_smem(k_fft_cols<N, 0>, CC::SMEM))) return rc;
-    k_fft_cols<N, 0><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
-    CSG_LAUNCH_CHECK();
+    if ((rc = rows(false, 1.f, pro, none))) return rc;
+    if ((rc = cols(0))) return rc;
     if (epi.n) return pixops_pass(st, field, F, N, N, epi, fi);
   } else {
     if (pro.n && (rc = pixops_pass(st, field, F, N, N, pro, fi))) return rc;
-    if ((rc = prep_smem(k_fft_cols<N, 1>, CC::SMEM))) return rc;
-    k_fft_cols<N, 1><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
-    CSG_LAUNCH_CHECK();
-    if ((rc = prep_smem(k_fft_rows<N, true>, RC::SMEM))) return rc;
-    k_fft_rows<N, true><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, inv_scale, tw, none, epi, fi);
-    CSG_LAUNCH_CHECK();
+    if ((rc = cols(1))) return rc;
+    return rows(true, inv_scale, none, epi);
   }
   return CSG_OK;
 }
@@ -373,15 +390,17 @@ int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const F
   const float2* tw = twiddles(ctx->device, n, st);
   CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
   const double pass_bytes = (double)F * n * n * 16.0;
-  ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0, pass_bytes * (fa ? 3.0 : 2.0));
+  const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // the first pass only writes
+  ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0,
+               pass_bytes * ((fa ? 3.0 : 2.0) - (gen ? 0.5 : 0.0)));
   switch (n) {
-    case 64: return run_fft<64>(st, field, F, direction, fa, pro, epi, fi, tw);
-    case 128: return run_fft<128>(st, field, F, direction, fa, pro, epi, fi, tw);
-    case 256: return run_fft<256>(st, field, F, direction, fa, pro, epi, fi, tw);
-    case 512: return run_fft<512>(st, field, F, direction, fa, pro, epi, fi, tw);
-    case 1024: return run_fft<1024>(st, field, F, direction, fa, pro, epi, fi, tw);
-    case 2048: return run_fft<2048>(st, field, F, direction, fa, pro, epi, fi, tw);
-    default: return run_fft<4096>(st, field, F, direction, fa, pro, epi, fi, tw);
+    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw);
+    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw);
+    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw);
+    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw);
+    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw);
+    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw);
+    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw);
   }
 }
 

@@ -202,6 +202,8 @@ struct csg_mft {
 };
 
 namespace {
+std::string g_tune_log;
+
 // Tile autotuner: times the transform with N-tile widths 128 and 256 at the
 // batch size it will run at (zero input, every field on slot 0) and keeps the
 // faster. Runs outside graph capture (csg_mft_reserve is called before).
@@ -263,9 +265,24 @@ int autotune(csg_mft* m, int F) {
   cudaFree(slot);
   m->bn = best_bn;
   m->tuned_fields = F;
+  char line[200];
+  snprintf(line, sizeof(line), "%s{\"in\": [%d, %d], \"out\": [%d, %d], \"fields\": %d, "
+           "\"bn\": %d, \"ms_bn128\": %.4f, \"ms_bn256\": %.4f}",
+           g_tune_log.empty() ? "" : ", ", m->ny, m->nx, m->mo, m->no, F, best_bn,
+           m->tuned_ms[0], m->tuned_ms[1]);
+  g_tune_log += line;
   return rc;
 }
 }  // namespace
+
+// JSON list of every autotuning decision made in this process.
+extern "C" int csg_mft_tuning_log(char* buf, size_t len) {
+  CSG_CHECK(buf && len > 0, CSG_E_ARG, "csg_mft_tuning_log: bad buffer");
+  const std::string s = "[" + g_tune_log + "]";
+  CSG_CHECK(s.size() + 1 <= len, CSG_E_ARG, "csg_mft_tuning_log: buffer too small");
+  memcpy(buf, s.c_str(), s.size() + 1);
+  return CSG_OK;
+}
 
 extern "C" {
 

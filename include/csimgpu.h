@@ -256,6 +256,8 @@ int csg_chain_field(csg_chain* chain, float** dev_field);
 int csg_mft_reserve(csg_mft* plan, int n_fields);
 /* The chosen tile width and the measured ms per transform of each width. */
 int csg_mft_tuning(csg_mft* plan, int* bn, float* ms128, float* ms256);
+/* Every autotuning decision of the process as a JSON list. */
+int csg_mft_tuning_log(char* buf, size_t len);
 
 /* ---------------------------------------------------- intensity / contrast */
 /* regionContrast::compute_intensity (regionContrast.cpp:124-143) and the
