@@ -179,6 +179,22 @@ size_t csg_mft_workspace_bytes(csg_mft* plan, int n_fields);
 int csg_hex_mask(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S, int n_sub,
                  const double* sags, int n_hex, int n_out, const int* cand, const double* lambda,
                  double phase_sign, int flip, double subtract, int use_only_hex, float* out);
+/* csg_hex_mask for callers that cannot let the library allocate device
+ * memory (no counterpart in the reference, which computes masks on the
+ * CPU). Same arguments and results as csg_hex_mask; its per-call scratch is a
+ * fixed device array of CSG_HEX_NOALLOC_MAX_PHASORS complex values (2 MiB,
+ * held by every GPU that loads the library until the process exits), so
+ * n_out * (n_hex + 1) must not exceed that, else CSG_E_SHAPE. It calls no
+ * cudaMalloc/cudaFree. The first call on a device looks up the array's
+ * device address (a one-time set-up); make that first call before any stream
+ * capture. All calls share the one array: calls whose work overlaps on the
+ * GPU (different streams or contexts on one device) race and must be
+ * ordered by the caller. */
+#define CSG_HEX_NOALLOC_MAX_PHASORS 262144
+int csg_hex_mask_noalloc(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S,
+                         int n_sub, const double* sags, int n_hex, int n_out, const int* cand,
+                         const double* lambda, double phase_sign, int flip, double subtract,
+                         int use_only_hex, float* out);
 /* Build the interpolation tables on the GPU (complexHexMaskFPM.cpp:317-469,
  * make_hex_array + make_interpolation_data). Hex centres (hex_x, hex_y,
  * device FP64) are in hex-step units; `pitch` is the centre distance of
