@@ -88,8 +88,16 @@ SIGNATURES = {
     "csg_respobj_create": ([P, C.POINTER(P), P, I, I, I, P, D, D, I], None),
     "csg_respobj_destroy": ([P], None),
     "csg_respobj_execute": ([P, P, I, P], None),
-    "csg_de_mutate": ([P, P, P, I, I, I, D, D, P, P, U64, U64, P, P], None),
-    "csg_de_select": ([P, P, P, P, P, I, I], None),
+    "csg_de_create": ([P, C.POINTER(P), I, I, U64], None),
+    "csg_de_destroy": ([P], None),
+    "csg_de_set_bounds": ([P, P, P, P, P], None),
+    "csg_de_init": ([P, P, D, I], None),
+    "csg_de_buffers": ([P, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P)], None),
+    "csg_de_set_trial_buffer": ([P, P], None),
+    "csg_de_generate": ([P, I, D, D], None),
+    "csg_de_select": ([P, I], None),
+    "csg_de_reset_best": ([P], None),
+    "csg_de_stats": ([P, P, P, P, P, P], None),
 }
 
 

@@ -43,8 +43,8 @@ static int get_encoder() {
 }
 
 // 3-D bf16 map: (k inner, rows, planes), box (64, box_rows, 1), 128B swizzle.
-static int make_map(CUtensorMap* m, const void* base, int k, int rows, long long planes,
-                    int box_rows) {
+int make_map(CUtensorMap* m, const void* base, int k, int rows, long long planes,
+             int box_rows) {
   int rc = get_encoder();
   if (rc) return rc;
   CSG_CHECK(((uintptr_t)base & 15) == 0, CSG_E_ARG, "TMA base not 16-byte aligned");
@@ -160,7 +160,7 @@ __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __res
 }
 
 // Product terms of the three-way split, largest first.
-static void terms_for(int precision, tc::Params& p) {
+void terms_for(int precision, tc::Params& p) {
   static const int a6[6] = {0, 0, 1, 0, 1, 2};
   static const int b6[6] = {0, 1, 0, 2, 1, 0};
   p.n_terms = precision == CSG_PREC_BF16X3 ? 3 : 6;
@@ -183,6 +183,14 @@ static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Par
   kern<<<grid, tc::THREADS, smem, st>>>(a, b, p);
   CSG_LAUNCH_CHECK();
   return CSG_OK;
+}
+
+// Data (A, rows of the fields) x operator (B) with an fp32 output
+// [field][re/im][rows][cols]: the response-matrix objective's product.
+int launch_gemm_data_op_f32(int bn, const CUtensorMap& a, const CUtensorMap& b,
+                            const tc::Params& p, int grid, cudaStream_t st) {
+  return bn == 256 ? launch_gemm<256, false, tc::EPI_F32>(a, b, p, grid, st)
+                   : launch_gemm<128, false, tc::EPI_F32>(a, b, p, grid, st);
 }
 
 }  // namespace csg

@@ -305,19 +305,37 @@ int csg_respobj_destroy(csg_respobj* obj);
 int csg_respobj_execute(csg_respobj* obj, const double* x, int pop, double* out);
 
 /* ------------------------------------------------ differential evolution */
-/* differentialEvolutionOptimizer generation step (differentialEvolution
- * Optimizer.cpp:261-281; deStrategy.cpp:23-158) on device FP64 populations
- * [pop][nvar]: strategy 0 = DE/rand/1, 1 = DE/local-to-best/1, 2 = either-or;
- * binomial crossover without a forced index (:360-369); bounce-back into
- * [lo, hi] (:395-434). Random numbers come from a counter-based generator
- * keyed by (seed, generation), so a generation is reproducible. */
-int csg_de_mutate(csg_ctx* ctx, const double* pop_x, const double* best, int pop, int nvar,
-                  int strategy, double f_weight, double cr, const double* lo, const double* hi,
-                  uint64_t seed, uint64_t generation, double* trial, double* origin);
-/* Greedy selection (differentialEvolutionOptimizer.cpp:436-453):
- * where f_trial < f, x <- trial, f <- f_trial. */
-int csg_de_select(csg_ctx* ctx, double* pop_x, double* f, const double* trial,
-                  const double* f_trial, int pop, int nvar);
+/* differentialEvolutionOptimizer (differentialEvolutionOptimizer.cpp:216-468;
+ * deStrategy.cpp:23-158) with its state on the device. Populations are FP64
+ * [pop][nvar] (candidate-major: the transpose of the reference's nvar x pop
+ * matrix). A generation is csg_de_generate (permutations, mutation, binomial
+ * crossover without a forced index, bounce-back into [mean + init bounds]
+ * clipped to the global bounds) -> the objective on the trial population,
+ * written to f_trial -> csg_de_select (greedy selection, best member,
+ * population statistics, generation + 1). Random numbers come from a
+ * counter-based generator keyed by (seed, generation, stream, index), so a
+ * generation is reproducible and can be captured in a CUDA graph. */
+int csg_de_create(csg_ctx* ctx, csg_de** de, int pop, int nvar, uint64_t seed);
+int csg_de_destroy(csg_de* de);
+/* globalBounds and initBounds per variable (host FP64 arrays of nvar). */
+int csg_de_set_bounds(csg_de* de, const double* global_lo, const double* global_hi,
+                      const double* init_lo, const double* init_hi);
+/* init_population (:336-358): origin + spread (u - 1/2) (initUB - initLB)
+ * (type 0) or origin + spread n (initUB - initLB) (type 1, normal). */
+int csg_de_init(csg_de* de, const double* origin_host, double spread, int type);
+/* Device buffers of the state: population, objective values, trial
+ * population and trial objective values. */
+int csg_de_buffers(csg_de* de, double** pop, double** f, double** trial, double** f_trial);
+/* Write trial vectors into a caller buffer instead (e.g. a chain's sags). */
+int csg_de_set_trial_buffer(csg_de* de, double* trial);
+/* strategy 0 = DE/rand/1, 1 = DE/local-to-best/1, 2 = either-or. */
+int csg_de_generate(csg_de* de, int strategy, double f_weight, double cr);
+/* initial != 0 after evaluating a fresh population (no selection). */
+int csg_de_select(csg_de* de, int initial);
+/* bestVal = huge, as on a re-initialisation (:249-258). */
+int csg_de_reset_best(csg_de* de);
+int csg_de_stats(csg_de* de, double* best_val, double* mean_dist, double* max_dist,
+                 unsigned long long* generation, double* best_vec);
 
 #ifdef __cplusplus
 }
