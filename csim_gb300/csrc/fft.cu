@@ -105,18 +105,25 @@ __device__ __forceinline__ void dif_stage(float* xr, float* xi) {
   }
 }
 
-// Row layout: transform t at t * NP, element m padded by m / 16.
+// Shared-memory swizzle: word address s is stored at s ^ ((s >> 4) & 31).
+// It permutes words within each aligned 32-word row, and it makes every
+// access of these transforms (32 consecutive elements, the stride-16 stores
+// of a radix-16 stage, the (g, k) scatter of the later stages, and the
+// column tile's 16-column rows) hit 32 distinct banks (checked exhaustively
+// for N = 256..4096).
+__device__ __forceinline__ int swz(int s) { return s ^ ((s >> 4) & 31); }
+
+// Row layout: transform t at t * N.
 template <int N>
 struct RowAddr {
-  static constexpr int NP = N + N / 16;
-  __device__ __forceinline__ static int at(int t, int m) { return t * NP + m + (m >> 4); }
+  static constexpr int NP = N;
+  __device__ __forceinline__ static int at(int t, int m) { return t * N + swz(m); }
 };
-// Column layout: element m of column t at m * (COLS + 1) + t (the odd row
-// pitch spreads stride-16 stores over all banks).
+// Column layout: element m of column t at m * COLS + t.
 template <int COLS>
 struct ColAddr {
-  static constexpr int PITCH = COLS + 1;
-  __device__ __forceinline__ static int at(int t, int m) { return m * PITCH + t; }
+  static constexpr int PITCH = COLS;
+  __device__ __forceinline__ static int at(int t, int m) { return swz(m * COLS + t); }
 };
 
 // One Stockham stage of radix R at sub-length L; each thread owns 16 / R
@@ -197,12 +204,12 @@ struct ColCfg {
   static constexpr int TPT = N / 16;
   static constexpr int COLS = N >= 2048 ? 16 * 1024 / N : 16;
   static constexpr int THREADS = COLS * TPT;
-  static constexpr size_t SMEM = (size_t)(COLS + 1) * N * 8;
+  static constexpr size_t SMEM = (size_t)COLS * N * 8;
 };
 
 // Row pass with fused element prologue / epilogue.
 template <int N, bool INV>
-__global__ void __launch_bounds__(RowCfg<N>::THREADS)
+__global__ void __launch_bounds__(RowCfg<N>::THREADS, 3)
     k_fft_rows(float* __restrict__ field, float scale, const float2* __restrict__ tw, PixOps pro,
                PixOps epi, FieldInfo fi) {
   using CF = RowCfg<N>;
