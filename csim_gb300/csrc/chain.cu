@@ -76,6 +76,8 @@ struct Elem {
   // fraunhofer
   csg_mft* mft = nullptr;
   int n_out = 0;
+  // per-wavelength tables (mirror phasors, Fresnel transfer function)
+  float2* tab = nullptr;
 };
 
 }  // namespace csg
@@ -88,6 +90,7 @@ struct csg_chain {
   double dx = 0;
   int n_lambda = 0;
   std::vector<double> lambda;
+  double* lam_slots = nullptr;  // device copy of lambda (one per slot)
   int precision = 6;
   std::vector<Elem> elems;
   // batch description (device)
@@ -149,6 +152,15 @@ int csg_chain_create(csg_ctx* ctx, csg_chain** out, int n, double pixel_scale, i
   c->dx = pixel_scale;
   c->n_lambda = n_lambda;
   c->lambda.assign(lambda, lambda + n_lambda);
+  {
+    DeviceGuard g(ctx->device);
+    c->lam_slots = dev_copy(lambda, n_lambda, ctx->stream);
+    if (!c->lam_slots) {
+      delete c;
+      set_error("csg_chain_create: allocation failed");
+      return CSG_E_NOMEM;
+    }
+  }
   c->precision = precision;
   *out = c;
   return CSG_OK;
@@ -164,13 +176,14 @@ int csg_chain_destroy(csg_chain* c) {
     cudaFree(e.b);
     cudaFree(e.hex_id);
     cudaFree(e.count);
+    cudaFree(e.tab);
     csg_mft_destroy(e.mft1);
     csg_mft_destroy(e.mft2);
     csg_mft_destroy(e.mft);
   }
   for (void* p : {(void*)c->slot, (void*)c->lam_f, (void*)c->amp, (void*)c->tip, (void*)c->tilt,
                   (void*)c->cand, (void*)c->ident, (void*)c->field, (void*)c->fpm,
-                  (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->sags})
+                  (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->sags, (void*)c->lam_slots})
     cudaFree(p);
   delete c;
   return CSG_OK;
@@ -201,19 +214,33 @@ int csg_chain_add_mirror(csg_chain* c, const float* sag, double sign) {
   e.sign = sign;
   e.a = dev_copy(sag, (size_t)c->n * c->n, c->ctx->stream);
   CSG_CHECK(e.a, CSG_E_NOMEM, "csg_chain_add_mirror: allocation failed");
+  // per-wavelength phasors, as the reference's mirrorPhase cube (mirror.cpp:66-72)
+  const size_t plane = (size_t)c->n * c->n;
+  e.tab = dev_copy<float2>(nullptr, plane * c->n_lambda, c->ctx->stream);
+  CSG_CHECK(e.tab, CSG_E_NOMEM, "csg_chain_add_mirror: allocation failed");
+  int rc = build_phasor_table(c->ctx->stream, e.a, c->n, c->n, c->lam_slots, c->n_lambda, sign,
+                              e.tab);
+  if (rc) return rc;
   c->elems.push_back(e);
   drop_graph(c);
   return CSG_OK;
 }
 
 // fresnelPropagator (fresnelPropagator.cpp:23-61, pad factor 1): z is the
-// signed distance, ap_rad the efield's arrayRadiusPhysical.
+// signed distance, ap_rad the efield's arrayRadiusPhysical. The transfer
+// function of every wavelength is tabulated once here (the reference rebuilds
+// it on every call, csim_fft.cpp:386).
 int csg_chain_add_fresnel(csg_chain* c, double z, double ap_rad) {
   CSG_CHECK(c && ap_rad > 0, CSG_E_ARG, "csg_chain_add_fresnel: bad argument");
+  DeviceGuard g(c->ctx->device);
   Elem e;
   e.kind = E_FRESNEL;
   e.z = z;
   e.ap_rad = ap_rad;
+  e.tab = dev_copy<float2>(nullptr, (size_t)c->n * c->n * c->n_lambda, c->ctx->stream);
+  CSG_CHECK(e.tab, CSG_E_NOMEM, "csg_chain_add_fresnel: allocation failed");
+  int rc = build_fresnel_table(c->ctx->stream, c->n, c->lam_slots, c->n_lambda, z, ap_rad, e.tab);
+  if (rc) return rc;
   c->elems.push_back(e);
   drop_graph(c);
   return CSG_OK;
@@ -447,19 +474,19 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
       kind = OP_MASK;
       param = e.quirk ? 1.f : 0.f;
     } else if (e.kind == E_MIRROR) {
-      kind = OP_PHASE;
-      param = (float)e.sign;
+      kind = OP_PHASOR;  // reads the element's per-wavelength phasor table
     } else if (e.kind == E_CMASK) {
       kind = OP_CMASK;
     }
     if (kind) {
-      if (epi_open && push_op(prog.back().epi, kind, e.a, e.b, param, e.mrows, e.mcols)) continue;
+      const float* a = kind == OP_PHASOR ? reinterpret_cast<const float*>(e.tab) : e.a;
+      if (epi_open && push_op(prog.back().epi, kind, a, e.b, param, e.mrows, e.mcols)) continue;
       epi_open = false;
-      if (!push_op(pend, kind, e.a, e.b, param, e.mrows, e.mcols)) {
+      if (!push_op(pend, kind, a, e.b, param, e.mrows, e.mcols)) {
         Step s{Step::PIX, pend, PixOps(), nullptr};
         prog.push_back(s);
         pend = PixOps();
-        push_op(pend, kind, e.a, e.b, param, e.mrows, e.mcols);
+        push_op(pend, kind, a, e.b, param, e.mrows, e.mcols);
       }
       continue;
     }
@@ -490,6 +517,7 @@ static int run_walk(csg_chain* c, int calibrating) {
   fi.amp = c->amp;
   fi.tip = c->tip;
   fi.tilt = c->tilt;
+  fi.slot = c->slot;
   int rc = CSG_OK;
   for (const Step& s : plan_walk(c, calibrating)) {
     switch (s.kind) {
@@ -497,7 +525,7 @@ static int run_walk(csg_chain* c, int calibrating) {
         rc = pixops_pass(ctx->stream, c->field, F, n, n, s.pro, fi);
         break;
       case Step::FRESNEL: {
-        FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad};
+        FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad, s.e->tab, c->slot};
         rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi);
         break;
       }

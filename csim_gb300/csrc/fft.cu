@@ -255,6 +255,60 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS, 3)
   }
 }
 
+// Angular-spectrum transfer function (csim_fft.cpp:377-386):
+//   H = exp(2 pi i [z/lambda sqrt(1 - eps)]), eps = (lambda/apRad)^2 f^2 / 4
+//   turns = z/lambda - K f^2 / 2 - K f^2 h,  K = z lambda / (4 apRad^2),
+//   h = eps / (2 (1 + sqrt(1 - eps))^2)
+// with f^2 the fftshifted integer frequency index squared. The large terms
+// are reduced in FP64 (z/lambda) and double-float (K f^2 / 2); eps > 1
+// (evanescent) gives NaN like the reference's real sqrt.
+struct FresnelConsts {
+  float t0, khi, klo, K, c_eps;
+};
+
+__device__ __forceinline__ FresnelConsts fresnel_consts(double lam, double z, double ap_rad) {
+  FresnelConsts c;
+  double t0 = z / lam;
+  t0 -= rint(t0);
+  const double K = z * lam / (4.0 * ap_rad * ap_rad);
+  split_f64_pair(0.5 * K, c.khi, c.klo);
+  c.K = (float)K;
+  c.c_eps = (float)(0.25 * (lam / ap_rad) * (lam / ap_rad));
+  c.t0 = (float)t0;
+  return c;
+}
+
+__device__ __forceinline__ float2 fresnel_h(int N, int r, int c, const FresnelConsts& k) {
+  const int fr = r < N / 2 ? r : r - N;
+  const int fc = c < N / 2 ? c : c - N;
+  const float f2 = (float)(fr * fr + fc * fc);  // exact: < 2^24
+  const float eps = k.c_eps * f2;
+  const float s = sqrtf(1.f - eps);
+  const float h = eps / (2.f * (1.f + s) * (1.f + s));
+  float tt = k.t0 - frac_prod(f2, k.khi, k.klo) - k.K * f2 * h;
+  tt -= rintf(tt);
+  float sn, cs;
+  sincospif(2.f * tt, &sn, &cs);
+  return make_float2(cs, sn);
+}
+
+__global__ void k_fresnel_table(int N, const double* lam, double z, double ap_rad,
+                                float2* __restrict__ out) {
+  const int s = blockIdx.y;
+  const FresnelConsts fc = fresnel_consts(lam[s], z, ap_rad);
+  const int plane = N * N;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x)
+    out[(size_t)s * plane + i] = fresnel_h(N, i / N, i % N, fc);
+}
+
+int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, double z,
+                        double ap_rad, float2* out) {
+  dim3 grid(grid_for((long long)N * N, 256, 1024), n_slot);
+  k_fresnel_table<<<grid, 256, 0, st>>>(N, lam, z, ap_rad, out);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
 // Column pass; MODE 0: forward, 1: inverse, 2: forward * H(lambda_f) * inverse.
 template <int N, int MODE>
 __global__ void __launch_bounds__(ColCfg<N>::THREADS)
@@ -281,35 +335,27 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS)
   const int t = threadIdx.x % CF::COLS, u = threadIdx.x / CF::COLS;
   smem_fft<N, MODE == 1, A>(re, im, t, u, tw);
   if (MODE == 2) {
-    // H = exp(2 pi i [z/lambda sqrt(1 - eps)]), eps = (lambda/apRad)^2 f^2 / 4
-    //   turns = z/lambda - K f^2 / 2 - K f^2 h,  K = z lambda / (4 apRad^2),
-    //   h = eps / (2 (1 + sqrt(1 - eps))^2)
-    // eps > 1 (evanescent) gives NaN like the reference's real sqrt.
-    const double lam = fa.lambda[f];
-    double t0 = fa.z / lam;
-    t0 -= rint(t0);
-    const double K = fa.z * lam / (4.0 * fa.ap_rad * fa.ap_rad);
-    float khi, klo;
-    split_f64_pair(0.5 * K, khi, klo);
-    const float Kf = (float)K;
-    const float c_eps = (float)(0.25 * (lam / fa.ap_rad) * (lam / fa.ap_rad));
-    const float t0f = (float)t0;
-    for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
-      const int r = i / CF::COLS, c = c0 + i % CF::COLS;
-      const int fr = r < N / 2 ? r : r - N;
-      const int fc = c < N / 2 ? c : c - N;
-      const float f2 = (float)(fr * fr + fc * fc);  // exact: < 2^24
-      const float eps = c_eps * f2;
-      const float s = sqrtf(1.f - eps);
-      const float h = eps / (2.f * (1.f + s) * (1.f + s));
-      float tt = t0f - frac_prod(f2, khi, klo) - Kf * f2 * h;
-      tt -= rintf(tt);
-      float sn, cs;
-      sincospif(2.f * tt, &sn, &cs);
-      const int a = A::at(i % CF::COLS, r);
-      const float xr = re[a], xi = im[a];
-      re[a] = xr * cs - xi * sn;
-      im[a] = xr * sn + xi * cs;
+    if (fa.H) {  // per-wavelength table (L2-resident, shared by the batch)
+      const float2* Hs = fa.H + (size_t)fa.slot[f] * N * N + c0;
+#pragma unroll 4
+      for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
+        const int r = i / CF::COLS, cl = i % CF::COLS;
+        const float2 w = Hs[(size_t)r * N + cl];
+        const int a = A::at(cl, r);
+        const float xr = re[a], xi = im[a];
+        re[a] = xr * w.x - xi * w.y;
+        im[a] = xr * w.y + xi * w.x;
+      }
+    } else {
+      const FresnelConsts fc = fresnel_consts(fa.lambda[f], fa.z, fa.ap_rad);
+      for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
+        const int r = i / CF::COLS, cl = i % CF::COLS;
+        const float2 w = fresnel_h(N, r, c0 + cl, fc);
+        const int a = A::at(cl, r);
+        const float xr = re[a], xi = im[a];
+        re[a] = xr * w.x - xi * w.y;
+        im[a] = xr * w.y + xi * w.x;
+      }
     }
     __syncthreads();
     smem_fft<N, true, A>(re, im, t, u, tw);

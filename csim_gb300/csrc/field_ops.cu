@@ -44,6 +44,29 @@ __global__ void k_pixops(float* __restrict__ field, int R, int C, PixOps ops, Fi
   }
 }
 
+// Mirror phasor table [slot][R][C]: exp(-sign 4 pi i sag / lambda_s), the
+// same fp32 arithmetic as OP_PHASE.
+__global__ void k_phasor_table(const float* __restrict__ sag, int plane, const double* lam,
+                               double sign, float2* __restrict__ out) {
+  const int s = blockIdx.y;
+  float kh, kl;
+  split_f64_pair(-sign * 2.0 / lam[s], kh, kl);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x) {
+    const float t = frac_prod(sag[i], kh, kl);
+    float sn, cs;
+    sincospif(2.f * t, &sn, &cs);
+    out[(size_t)s * plane + i] = make_float2(cs, sn);
+  }
+}
+
+int build_phasor_table(cudaStream_t st, const float* sag, int R, int C, const double* lam,
+                       int n_slot, double sign, float2* out) {
+  dim3 grid(grid_for((long long)R * C, 256, 1024), n_slot);
+  k_phasor_table<<<grid, 256, 0, st>>>(sag, R * C, lam, sign, out);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
 int pixops_pass(cudaStream_t st, float* field, int F, int R, int C, const PixOps& ops,
                 const FieldInfo& fi) {
   if (!ops.n) return CSG_OK;

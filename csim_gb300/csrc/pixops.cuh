@@ -15,7 +15,10 @@
 
 namespace csg {
 
-enum PixOpKind { OP_SOURCE = 1, OP_MASK = 2, OP_PHASE = 3, OP_CMASK = 4 };
+// OP_PHASOR multiplies by a precomputed per-wavelength phasor table
+// (float2 [slot][R][C], the reference's mirrorPhase cube, mirror.cpp:66-72),
+// indexed by the field's wavelength slot.
+enum PixOpKind { OP_SOURCE = 1, OP_MASK = 2, OP_PHASE = 3, OP_CMASK = 4, OP_PHASOR = 5 };
 constexpr int MAX_PIXOPS = 6;
 
 struct PixOps {
@@ -33,12 +36,14 @@ struct FieldInfo {
   const double* amp = nullptr;
   const double* tip = nullptr;
   const double* tilt = nullptr;
+  const int* slot = nullptr;  // wavelength slot (OP_PHASOR tables)
 };
 
 // Per-field constants, computed once per CTA.
 struct PixConsts {
   float khi[MAX_PIXOPS], klo[MAX_PIXOPS];  // OP_PHASE turns per metre
   float sxh, sxl, syh, syl, amp;           // OP_SOURCE
+  int slot;                                // OP_PHASOR table
 };
 
 __device__ __forceinline__ float frac_prod(float a, float khi, float klo) {
@@ -55,6 +60,7 @@ __device__ __forceinline__ void split_f64_pair(double v, float& hi, float& lo) {
 
 __device__ __forceinline__ void pix_consts(const PixOps& ops, const FieldInfo& fi, int f, int R,
                                            int C, PixConsts& k) {
+  k.slot = fi.slot ? fi.slot[f] : 0;
 #pragma unroll
   for (int i = 0; i < MAX_PIXOPS; ++i) {
     if (i >= ops.n) break;
@@ -104,6 +110,11 @@ __device__ __forceinline__ void pix_apply(const PixOps& ops, const PixConsts& k,
       const float xr = re;
       re = xr * co - im * s;
       im = xr * s + im * co;
+    } else if (kind == OP_PHASOR) {
+      const float2 w = reinterpret_cast<const float2*>(ops.a[i])[((size_t)k.slot * R + r) * C + c];
+      const float xr = re;
+      re = xr * w.x - im * w.y;
+      im = xr * w.y + im * w.x;
     } else if (kind == OP_CMASK) {
       const int r0 = R / 2 - ops.mr[i] / 2, c0 = C / 2 - ops.mc[i] / 2;
       const int rr = r - r0, cc = c - c0;
@@ -125,10 +136,20 @@ int pixops_pass(cudaStream_t st, float* field, int F, int R, int C, const PixOps
                 const FieldInfo& fi);
 
 struct FresnelArgs {
-  const double* lambda;  // per field
+  const double* lambda;           // per field
   double z;
   double ap_rad;
+  const float2* H = nullptr;      // optional transfer-function table [slot][N][N]
+  const int* slot = nullptr;      // per field, with H
 };
+
+// Per-wavelength tables, built once per chain in FP64-reduced phases:
+// mirror phasors exp(-sign 4 pi i sag / lambda_s) and Fresnel transfer
+// functions H_s (same arithmetic as the in-kernel evaluations).
+int build_phasor_table(cudaStream_t st, const float* sag, int R, int C, const double* lam,
+                       int n_slot, double sign, float2* out);
+int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, double z,
+                        double ap_rad, float2* out);
 
 // 2-D FFT (direction -1 / +1) or, with fa, Fresnel propagation of F square
 // N x N fields with element ops fused before (pro) and after (epi).
