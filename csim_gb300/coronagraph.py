@@ -94,13 +94,14 @@ class Coronagraph:
     image fields as a planar fp32 tensor [F, 2, n_out, n_out]."""
 
     def __init__(self, ctx: Context, tel: Telescope, ef: EField, elements: list,
-                 precision: int = CSG_PREC_BF16X6):
+                 precision: int = CSG_PREC_BF16X6, support_crop: bool = True):
         self.ctx, self.tel, self.ef, self.elements = ctx, tel, ef, elements
         lam = np.ascontiguousarray(ef.wavelengths, dtype=np.float64)
         h = C.c_void_p()
         call("csg_chain_create", ctx.h, C.byref(h), ef.n, ef.pixelScale, lam.size,
              lam.ctypes.data_as(C.c_void_p), precision)
         self.h = h
+        call("csg_chain_set_support_crop", self.h, int(support_crop))
         self.n_hex = None
         self.n_out = None
         self.out_pixel = None
@@ -137,6 +138,12 @@ class Coronagraph:
                  2 * self.ef.beamRadiusPhysical * self.tel.primaryfRatio)
         else:
             raise TypeError(f"unsupported element {type(e).__name__}")
+
+    def fpm_region(self, idx: int = 0):
+        """(r0, c0, rows, cols) of the mask grid the idx-th hex FPM transforms."""
+        v = [C.c_int() for _ in range(4)]
+        call("csg_chain_fpm_region", self.h, idx, *[C.byref(x) for x in v])
+        return tuple(x.value for x in v)
 
     def set_batch(self, lambda_idx, amp, tip, tilt, cand):
         arrs = [np.ascontiguousarray(lambda_idx, np.int32), np.ascontiguousarray(amp, np.float64),

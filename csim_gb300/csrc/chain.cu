@@ -29,6 +29,10 @@ int csg_point_source(csg_ctx*, float*, int, int, int, double, double, const doub
 }
 
 namespace csg {
+int hex_mask_region(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S, int r0,
+                    int c0, int RR, int CC, int n_sub, const double* sags, int n_hex, int n_out,
+                    const int* cand, const double* lambda, double phase_sign, int flip,
+                    double subtract, float* out, float2* phasors);
 int hex_mask_with_phasor_buffer(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S,
                                 int n_sub, const double* sags, int n_hex, int n_out,
                                 const int* cand, const double* lambda, double phase_sign, int flip,
@@ -70,6 +74,7 @@ struct Elem {
   int16_t* hex_id = nullptr;
   uint16_t* count = nullptr;
   int S = 0, n_sub = 0, n_hex = 0;
+  int r0 = 0, c0 = 0, RR = 0, CC = 0;  // transformed box of the S x S mask grid
   double phase_sign = 1.0;
   csg_mft* mft1 = nullptr;
   csg_mft* mft2 = nullptr;
@@ -92,6 +97,7 @@ struct csg_chain {
   std::vector<double> lambda;
   double* lam_slots = nullptr;  // device copy of lambda (one per slot)
   int precision = 6;
+  bool crop_support = true;
   std::vector<Elem> elems;
   // batch description (device)
   int n_fields = 0, cap_fields = 0;
@@ -304,17 +310,76 @@ int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* c
     pref2[2 * l] = zoom_fft_sign * dm * dm * c->dx * c->dx / (f_ratio_sign * lf[l] * lf[l]);
     pref2[2 * l + 1] = 0.0;
   }
+  // Support of fliplr(M) - 1: M = sum_k n_k e^{i phi_k} / nSub^2 with
+  // sum_k n_k = nSub^2, so M - 1 vanishes wherever no sub-pixel falls in a hex,
+  // for every choice of sags. Both transforms run on the bounding box of that
+  // support (rounded out to multiples of 8), which gives exactly the
+  // full-grid result.
+  int rmin = S, rmax = -1, cmin = S, cmax = -1;
+  if (c->crop_support) {
+    const size_t plane = (size_t)S * S;
+    for (int r = 0; r < S; ++r)
+      for (int cc = 0; cc < S; ++cc) {
+        const size_t src = (size_t)r * S + (S - 1 - cc);  // flipped column
+        bool in = false;
+        for (int k = 0; k < 3; ++k) in |= count[k * plane + src] > 0 && hex_id[k * plane + src] >= 0;
+        if (in) {
+          rmin = std::min(rmin, r);
+          rmax = std::max(rmax, r);
+          cmin = std::min(cmin, cc);
+          cmax = std::max(cmax, cc);
+        }
+      }
+  }
+  if (rmax < 0) {  // no cropping (or an empty mask): the full grid
+    rmin = cmin = 0;
+    rmax = cmax = S - 1;
+  }
+  // box sides rounded up to multiples of 128 (the tensor-core tile), centred
+  // on the support and kept inside the grid
+  auto place = [S](int lo, int hi, int& o, int& len) {
+    len = std::min(S, (hi - lo + 1 + 127) / 128 * 128);
+    o = std::max(0, std::min(S - len, (lo + hi + 1) / 2 - len / 2));
+  };
+  place(rmin, rmax, e.r0, e.RR);
+  place(cmin, cmax, e.c0, e.CC);
   std::vector<double> xp = pixel_centres(n, c->dx), xm = pixel_centres(S, dm);
   std::vector<double> xps = pixel_centres(n, c->dx, c->dx / 2.0);
-  int rc = csg_mft_create(c->ctx, &e.mft1, n, n, S, S, xp.data(), xp.data(), xm.data(),
-                          xm.data(), L, lf.data(), pref1.data(), +1.0, c->precision);
+  const double* ym_c = xm.data() + e.r0;  // rows of the box (y)
+  const double* xm_c = xm.data() + e.c0;  // columns of the box (x)
+  int rc = csg_mft_create(c->ctx, &e.mft1, n, n, e.RR, e.CC, xp.data(), xp.data(), ym_c, xm_c, L,
+                          lf.data(), pref1.data(), +1.0, c->precision);
   if (rc) return rc;
-  rc = csg_mft_create(c->ctx, &e.mft2, S, S, n, n, xm.data(), xm.data(), xps.data(), xps.data(), L,
+  rc = csg_mft_create(c->ctx, &e.mft2, e.RR, e.CC, n, n, ym_c, xm_c, xps.data(), xps.data(), L,
                       lf.data(), pref2.data(), -1.0, c->precision);
   if (rc) return rc;
   c->elems.push_back(e);
   drop_graph(c);
   return CSG_OK;
+}
+
+// Whether hex focal-plane masks added after this call run their transforms on
+// the mask's support only (default on; the result is the same either way).
+int csg_chain_set_support_crop(csg_chain* c, int enable) {
+  CSG_CHECK(c, CSG_E_ARG, "csg_chain_set_support_crop: null chain");
+  c->crop_support = enable != 0;
+  return CSG_OK;
+}
+
+// The FPM grid actually transformed by the idx-th hex FPM element.
+int csg_chain_fpm_region(csg_chain* c, int idx, int* r0, int* c0, int* rows, int* cols) {
+  CSG_CHECK(c && r0 && c0 && rows && cols, CSG_E_ARG, "csg_chain_fpm_region: null argument");
+  int k = 0;
+  for (auto& e : c->elems)
+    if (e.kind == E_FPM_HEX && k++ == idx) {
+      *r0 = e.r0;
+      *c0 = e.c0;
+      *rows = e.RR;
+      *cols = e.CC;
+      return CSG_OK;
+    }
+  set_error("csg_chain_fpm_region: no such element");
+  return CSG_E_ARG;
 }
 
 // fraunhoferFocal (fraunhoferFocal.cpp:23-72): zoomFft to n_out x n_out at
@@ -418,7 +483,7 @@ static int prepare(csg_chain* c) {
   size_t fpm_need = 0, ph_need = 0, img_need = 0;
   for (auto& e : c->elems) {
     if (e.kind == E_FPM_HEX) {
-      fpm_need = std::max(fpm_need, F * 2 * e.S * e.S * sizeof(float));
+      fpm_need = std::max(fpm_need, F * 2 * e.RR * e.CC * sizeof(float));
       ph_need = std::max(ph_need, F * (e.n_hex + 1) * sizeof(float2));
       int rc = csg_mft_reserve(e.mft1, c->n_fields);
       if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
@@ -533,10 +598,10 @@ static int run_walk(csg_chain* c, int calibrating) {
         const Elem& e = *s.e;
         CSG_CHECK(c->sags && c->sag_hex == e.n_hex, CSG_E_STATE,
                   "hex FPM: candidate sags not set (csg_chain_sags) or wrong hex count");
-        // (fliplr(M) - 1) for each field's (candidate, wavelength)
-        rc = hex_mask_with_phasor_buffer(ctx, e.hex_id, e.count, e.S, e.n_sub, c->sags, e.n_hex,
-                                         F, c->cand, c->lam_f, e.phase_sign, 1, 1.0, -1,
-                                         c->fpm_mask, c->phasors);
+        // (fliplr(M) - 1) for each field's (candidate, wavelength) on the box
+        rc = hex_mask_region(ctx, e.hex_id, e.count, e.S, e.r0, e.c0, e.RR, e.CC, e.n_sub,
+                             c->sags, e.n_hex, F, c->cand, c->lam_f, e.phase_sign, 1, 1.0,
+                             c->fpm_mask, c->phasors);
         if (!rc) rc = csg_mft_execute(ctx, e.mft1, c->field, c->fpm, F, c->slot, 0, nullptr,
                                       nullptr);
         if (!rc) rc = csg_mft_execute(ctx, e.mft2, c->fpm, c->field, F, c->slot, 1, c->fpm_mask,

@@ -201,6 +201,53 @@ __global__ void k_intensity(const float* __restrict__ field, long long plane, in
 
 // Hex mask with a caller-provided phasor buffer [n_out][n_hex + 1] (used by
 // the chain executor, which owns that buffer).
+// The mask on a sub-rectangle [r0, r0 + RR) x [c0, c0 + CC) of the (flipped)
+// S x S mask grid, written as [n_out][2][RR][CC]: the chain evaluates the
+// Babinet term only where fliplr(M) - 1 can be nonzero.
+__global__ void k_hex_mask_region(const int16_t* __restrict__ hex_id,
+                                  const uint16_t* __restrict__ count, int S, int r0, int c0, int RR,
+                                  int CC, float inv_nsub2, const float2* __restrict__ ph, int n_hex,
+                                  int flip, float subtract, float* __restrict__ out) {
+  const int j = blockIdx.y;
+  const int plane = RR * CC;
+  const size_t splane = (size_t)S * S;
+  const float2* phj = ph + (size_t)j * (n_hex + 1);
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < plane; o += gridDim.x * blockDim.x) {
+    const int r = r0 + o / CC, c = c0 + o % CC;
+    const size_t src = (size_t)r * S + (flip ? (S - 1 - c) : c);
+    float mr = 0.f, mi = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int id = hex_id[k * splane + src];
+      const float w = (float)count[k * splane + src];
+      if (w != 0.f) {
+        const float2 p = phj[id >= 0 ? id : n_hex];
+        mr += w * p.x;
+        mi += w * p.y;
+      }
+    }
+    float* base = out + (size_t)j * 2 * plane + o;
+    base[0] = mr * inv_nsub2 - subtract;
+    base[plane] = mi * inv_nsub2;
+  }
+}
+
+int hex_mask_region(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S, int r0,
+                    int c0, int RR, int CC, int n_sub, const double* sags, int n_hex, int n_out,
+                    const int* cand, const double* lambda, double phase_sign, int flip,
+                    double subtract, float* out, float2* phasors) {
+  cudaStream_t st = ctx->stream;
+  k_hex_phasors<<<grid_for((long long)n_out * (n_hex + 1), 256), 256, 0, st>>>(
+      phasors, sags, n_hex, n_out, cand, lambda, phase_sign);
+  CSG_LAUNCH_CHECK();
+  dim3 grid(grid_for((long long)RR * CC, 256, 256), n_out);
+  k_hex_mask_region<<<grid, 256, 0, st>>>(hex_id, count, S, r0, c0, RR, CC,
+                                          1.f / (float)(n_sub * n_sub), phasors, n_hex, flip,
+                                          (float)subtract, out);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
 int hex_mask_with_phasor_buffer(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S,
                                 int n_sub, const double* sags, int n_hex, int n_out,
                                 const int* cand, const double* lambda, double phase_sign, int flip,

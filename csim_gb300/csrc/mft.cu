@@ -248,7 +248,8 @@ int autotune(csg_mft* m, int F) {
   int best_bn = 0, rc = CSG_OK;
   const bool prof = m->ctx->prof;
   m->ctx->prof = false;
-  for (int i = 0; i < 2 && !rc; ++i) {
+  const int n_cand = m->no >= 256 ? 2 : 1;  // a 256-wide tile needs 256 output columns
+  for (int i = 0; i < n_cand && !rc; ++i) {
     m->bn = cand[i];
     rc = mft_execute_ops(m->ctx, m, in, out, F, slot, 0, nullptr, nullptr, PixOps(), FieldInfo());
     cudaEventRecord(a, st);

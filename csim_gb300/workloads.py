@@ -36,7 +36,8 @@ def hex_tables(ctx: Context, hex_x, hex_y, n_rings, design_size, fpm_scale_facto
     return ids.cpu().numpy(), cnt.cpu().numpy().view(np.uint16), over.value
 
 
-def build_piaacmc(ctx: Context, spec: PiaacmcSpec, sources=None, precision: int = 6):
+def build_piaacmc(ctx: Context, spec: PiaacmcSpec, sources=None, precision: int = 6,
+                  support_crop: bool = True):
     """Returns (coronagraph, inputs dict with every array the oracle needs);
     the hex tables are built on the GPU."""
     a = piaacmc_arrays(spec, sources)
@@ -53,7 +54,7 @@ def build_piaacmc(ctx: Context, spec: PiaacmcSpec, sources=None, precision: int 
         cg.Mask(a["lyot"]),
         cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov),
     ]
-    cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision)
+    cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision, support_crop)
     return cor, a
 
 

@@ -245,6 +245,13 @@ int csg_chain_add_fpm_hex(csg_chain* chain, const int16_t* hex_id, const uint16_
                           int n_sub, int n_hex, double dm, double focal_ratio, double beam_radius,
                           double f_ratio_sign, double zoom_fft_sign, double phase_sign,
                           int disable_for_calibration);
+/* Hex FPMs added after this call transform only the bounding box of the
+ * support of fliplr(M) - 1 (rounded out to multiples of 128): M = 1 wherever
+ * no hex covers a mask pixel, for any sags, so the Babinet term is exactly
+ * the full-grid one. enable = 0 transforms the whole S x S grid. Default 1. */
+int csg_chain_set_support_crop(csg_chain* chain, int enable);
+/* The box [r0, r0 + rows) x [c0, c0 + cols) of the idx-th hex FPM element. */
+int csg_chain_fpm_region(csg_chain* chain, int idx, int* r0, int* c0, int* rows, int* cols);
 /* fraunhoferFocal (fraunhoferFocal.cpp:23-72): zoomFft to n_out x n_out at
  * out_pixel (= loD / samplesPerflD), lambda f = lambda lf_scale with
  * lf_scale = 2 beamRadius primaryfRatio. Must be the last element. */

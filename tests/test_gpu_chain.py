@@ -88,6 +88,32 @@ def test_piaacmc_chain_matches_oracle(ctx, conv_form):
         assert abs(con[c] - ref_con) / ref_con < 0.01, (con[c], ref_con)
 
 
+def test_fpm_support_crop_is_exact(ctx):
+    """Transforming only the support of fliplr(M) - 1 gives the full-grid
+    result (to fp32 rounding), and the box really is smaller than the grid."""
+    from csim_gb300 import workloads as W
+    spec = small_spec(S=256, fpm_sampling=16.0, n_rings=3)
+    rng = np.random.default_rng(6)
+    outs = []
+    for crop in (True, False):
+        cor, inp = W.build_piaacmc(ctx, spec, support_crop=crop)
+        sags = W.random_sags(rng if not outs else np.random.default_rng(6), 2, inp["hex_x"].size,
+                             5e-7)
+        cor.sags(2).copy_(torch.as_tensor(sags))
+        cor.batch_all(2)
+        outs.append(cor.execute().clone())
+        region = cor.fpm_region()
+        ctx.sync()
+        if crop:
+            assert region[2] < spec.S and region[3] < spec.S, region
+        else:
+            assert region == (0, 0, spec.S, spec.S)
+        cor.close()
+    a, b = outs
+    peak = b.abs().max().item()
+    assert (a - b).abs().max().item() / peak < 1e-6
+
+
 def test_chain_graph_replay_is_identical(ctx):
     from csim_gb300 import workloads as W
     spec = small_spec(wavelengths=(650e-9,))
