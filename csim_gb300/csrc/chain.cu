@@ -83,6 +83,13 @@ struct Elem {
   int n_out = 0;
   // per-wavelength tables (mirror phasors, Fresnel transfer function)
   float2* tab = nullptr;
+  // real mask: bounding box [sr0, sr1) x [sc0, sc1) of its nonzero pixels
+  int sr0 = 0, sr1 = 0, sc0 = 0, sc1 = 0;
+  // lazily built transforms: wavelength-f products, prefactors, window
+  std::vector<double> lf, pref;
+  double dm = 0, out_pixel = 0;
+  MftWindow win{0, 0, 0, 0};  // window origin in the n x n field
+  int win_rows = 0, win_cols = 0;
 };
 
 }  // namespace csg
@@ -98,6 +105,7 @@ struct csg_chain {
   double* lam_slots = nullptr;  // device copy of lambda (one per slot)
   int precision = 6;
   bool crop_support = true;
+  bool planned = false;  // lazily built transforms are up to date
   std::vector<Elem> elems;
   // batch description (device)
   int n_fields = 0, cap_fields = 0;
@@ -206,7 +214,19 @@ int csg_chain_add_mask(csg_chain* c, const float* mask, int ref_quirk, int disab
   e.disable_for_calibration = disable_for_calibration;
   e.a = dev_copy(mask, (size_t)c->n * c->n, c->ctx->stream);
   CSG_CHECK(e.a, CSG_E_NOMEM, "csg_chain_add_mask: allocation failed");
+  // support of the mask (where it is nonzero)
+  e.sr0 = e.sc0 = c->n;
+  e.sr1 = e.sc1 = 0;
+  for (int r = 0; r < c->n; ++r)
+    for (int cc = 0; cc < c->n; ++cc)
+      if (mask[(size_t)r * c->n + cc] != 0.f) {
+        e.sr0 = std::min(e.sr0, r);
+        e.sr1 = std::max(e.sr1, r + 1);
+        e.sc0 = std::min(e.sc0, cc);
+        e.sc1 = std::max(e.sc1, cc + 1);
+      }
   c->elems.push_back(e);
+  c->planned = false;
   drop_graph(c);
   return CSG_OK;
 }
@@ -228,6 +248,7 @@ int csg_chain_add_mirror(csg_chain* c, const float* sag, double sign) {
                               e.tab);
   if (rc) return rc;
   c->elems.push_back(e);
+  c->planned = false;
   drop_graph(c);
   return CSG_OK;
 }
@@ -248,6 +269,7 @@ int csg_chain_add_fresnel(csg_chain* c, double z, double ap_rad) {
   int rc = build_fresnel_table(c->ctx->stream, c->n, c->lam_slots, c->n_lambda, z, ap_rad, e.tab);
   if (rc) return rc;
   c->elems.push_back(e);
+  c->planned = false;
   drop_graph(c);
   return CSG_OK;
 }
@@ -267,6 +289,7 @@ int csg_chain_add_complex_mask(csg_chain* c, const float* amp, const float* ph, 
   e.b = dev_copy(ph, (size_t)mrows * mcols, c->ctx->stream);
   CSG_CHECK(e.a && e.b, CSG_E_NOMEM, "csg_chain_add_complex_mask: allocation failed");
   c->elems.push_back(e);
+  c->planned = false;
   drop_graph(c);
   return CSG_OK;
 }
@@ -350,10 +373,13 @@ int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* c
   int rc = csg_mft_create(c->ctx, &e.mft1, n, n, e.RR, e.CC, xp.data(), xp.data(), ym_c, xm_c, L,
                           lf.data(), pref1.data(), +1.0, c->precision);
   if (rc) return rc;
-  rc = csg_mft_create(c->ctx, &e.mft2, e.RR, e.CC, n, n, ym_c, xm_c, xps.data(), xps.data(), L,
-                      lf.data(), pref2.data(), -1.0, c->precision);
-  if (rc) return rc;
+  // the return transform is built once the elements after it are known
+  // (its output may be limited to the support of the following stops)
+  e.lf = lf;
+  e.pref = pref2;
+  e.dm = dm;
   c->elems.push_back(e);
+  c->planned = false;
   drop_graph(c);
   return CSG_OK;
 }
@@ -363,6 +389,8 @@ int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* c
 int csg_chain_set_support_crop(csg_chain* c, int enable) {
   CSG_CHECK(c, CSG_E_ARG, "csg_chain_set_support_crop: null chain");
   c->crop_support = enable != 0;
+  c->planned = false;
+  drop_graph(c);
   return CSG_OK;
 }
 
@@ -400,12 +428,85 @@ int csg_chain_add_fraunhofer(csg_chain* c, int n_out, double out_pixel, double l
     pref[2 * l] = 0.0;
     pref[2 * l + 1] = -c->dx * c->dx / lf[l];
   }
-  std::vector<double> xi = pixel_centres(n, c->dx), xo = pixel_centres(n_out, out_pixel);
-  int rc = csg_mft_create(c->ctx, &e.mft, n, n, n_out, n_out, xi.data(), xi.data(), xo.data(),
-                          xo.data(), L, lf.data(), pref.data(), -1.0, c->precision);
-  if (rc) return rc;
-  c->elems.push_back(e);
+  (void)n;
+  e.lf = lf;
+  e.pref = pref;
+  e.out_pixel = out_pixel;
+  c->elems.push_back(e);  // the transform is built with the rest of the walk
+  c->planned = false;
   drop_graph(c);
+  return CSG_OK;
+}
+
+// Window of the field that the transform after elements (lo, hi) needs:
+// the intersection of the supports of the real masks applied in between
+// (also in calibration), rounded out to multiples of 32; the whole field when
+// there is none or cropping is off.
+static MftWindow stop_window(const csg_chain* c, int lo, int hi) {
+  const int n = c->n;
+  int r0 = 0, r1 = n, c0 = 0, c1 = n;
+  if (c->crop_support) {
+    for (int k = lo + 1; k < hi; ++k) {
+      const Elem& m = c->elems[k];
+      if (m.kind != E_MASK || m.disable_for_calibration) continue;
+      r0 = std::max(r0, m.sr0);
+      r1 = std::min(r1, m.sr1);
+      c0 = std::max(c0, m.sc0);
+      c1 = std::min(c1, m.sc1);
+    }
+    if (r1 <= r0 || c1 <= c0) r0 = c0 = 0, r1 = c1 = 32;  // an all-zero stop
+  }
+  r0 = r0 / 32 * 32;
+  c0 = c0 / 32 * 32;
+  r1 = std::min(n, (r1 + 31) / 32 * 32);
+  c1 = std::min(n, (c1 + 31) / 32 * 32);
+  return MftWindow{r0, c0, r1 - r0, c1 - c0};
+}
+
+static bool is_pointwise(ElemKind k) { return k == E_MASK || k == E_MIRROR || k == E_CMASK; }
+
+// Build the transforms whose shape depends on the elements around them: the
+// hex FPM's return transform and the final-image transform run on the
+// window of the stops between them.
+static int build_plans(csg_chain* c) {
+  if (c->planned) return CSG_OK;
+  const int n = c->n, L = c->n_lambda;
+  const int ne = (int)c->elems.size();
+  std::vector<double> xp = pixel_centres(n, c->dx), xps = pixel_centres(n, c->dx, c->dx / 2.0);
+  for (int i = 0; i < ne; ++i) {
+    Elem& e = c->elems[i];
+    if (e.kind == E_FPM_HEX) {
+      int j = i + 1;
+      while (j < ne && is_pointwise(c->elems[j].kind)) ++j;
+      MftWindow w = (j < ne && c->elems[j].kind == E_FRAUNHOFER) ? stop_window(c, i, j)
+                                                                 : MftWindow{0, 0, n, n};
+      std::vector<double> xm = pixel_centres(e.S, e.dm);
+      csg_mft_destroy(e.mft2);
+      e.mft2 = nullptr;
+      int rc = csg_mft_create(c->ctx, &e.mft2, e.RR, e.CC, w.rows, w.pitch, xm.data() + e.r0,
+                              xm.data() + e.c0, xps.data() + w.r0, xps.data() + w.c0, L,
+                              e.lf.data(), e.pref.data(), -1.0, c->precision);
+      if (rc) return rc;
+      e.win = MftWindow{w.r0, w.c0, n, n};  // output window of the n x n field
+      e.win_rows = w.rows;
+      e.win_cols = w.pitch;
+    } else if (e.kind == E_FRAUNHOFER) {
+      int k = i - 1;
+      while (k >= 0 && is_pointwise(c->elems[k].kind)) --k;
+      const MftWindow w = stop_window(c, k, i);
+      std::vector<double> xo = pixel_centres(e.n_out, e.out_pixel);
+      csg_mft_destroy(e.mft);
+      e.mft = nullptr;
+      int rc = csg_mft_create(c->ctx, &e.mft, w.rows, w.pitch, e.n_out, e.n_out,
+                              xp.data() + w.r0, xp.data() + w.c0, xo.data(), xo.data(), L,
+                              e.lf.data(), e.pref.data(), -1.0, c->precision);
+      if (rc) return rc;
+      e.win = MftWindow{w.r0, w.c0, n, n};  // input window of the n x n field
+      e.win_rows = w.rows;
+      e.win_cols = w.pitch;
+    }
+  }
+  c->planned = true;
   return CSG_OK;
 }
 
@@ -479,6 +580,8 @@ int csg_chain_sags(csg_chain* c, int n_cand, int n_hex, double** dev_sags) {
 }
 
 static int prepare(csg_chain* c) {
+  int prc = build_plans(c);
+  if (prc) return prc;
   const size_t F = (size_t)c->n_fields;
   size_t fpm_need = 0, ph_need = 0, img_need = 0;
   for (auto& e : c->elems) {
@@ -604,13 +707,14 @@ static int run_walk(csg_chain* c, int calibrating) {
                              c->fpm_mask, c->phasors);
         if (!rc) rc = csg_mft_execute(ctx, e.mft1, c->field, c->fpm, F, c->slot, 0, nullptr,
                                       nullptr);
-        if (!rc) rc = csg_mft_execute(ctx, e.mft2, c->fpm, c->field, F, c->slot, 1, c->fpm_mask,
-                                      c->ident);
+        // E + MFT2[...] on the window of the stops that follow (accumulate)
+        if (!rc) rc = mft_execute_ops(ctx, e.mft2, c->fpm, c->field, F, c->slot, 1, c->fpm_mask,
+                                      c->ident, PixOps(), fi, nullptr, &e.win);
         break;
       }
       case Step::FINAL:
         rc = mft_execute_ops(ctx, s.e->mft, c->field, c->image, F, c->slot, 0, nullptr, nullptr,
-                             s.pro, fi);
+                             s.pro, fi, &s.e->win, nullptr);
         break;
     }
     if (rc) return rc;

@@ -108,26 +108,31 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
 // complex multiplier [n_mul][2][R][C] chosen by mul_idx[f]) -> bf16
 // [F][3][2][R][C]. Four pixels per thread (C is a multiple of 8); grid.y is
 // the field.
+// The input is the R x C window at (r0, c0) of fields whose planes are
+// RT x PT (the element ops see the field's own coordinates and size).
 __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int R,
-                              int C, const float* __restrict__ mul,
+                              int C, int r0, int c0, int RT, int PT,
+                              const float* __restrict__ mul,
                               const int* __restrict__ mul_idx, PixOps pre, FieldInfo fi) {
   const int f = blockIdx.y;
   const int plane = R * C;
+  const size_t fplane = (size_t)RT * PT;
   PixConsts k;
-  if (pre.n) pix_consts(pre, fi, f, R, C, k);
-  const float* ire = in + (size_t)f * 2 * plane;
-  const float* iim = ire + plane;
+  if (pre.n) pix_consts(pre, fi, f, RT, PT, k);
+  const float* ire = in + (size_t)f * 2 * fplane;
+  const float* iim = ire + fplane;
   const float* mre = mul ? mul + (size_t)mul_idx[f] * 2 * plane : nullptr;
   const int nv = plane / 4;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
-    const float4 a4 = reinterpret_cast<const float4*>(ire)[v];
-    const float4 b4 = reinterpret_cast<const float4*>(iim)[v];
-    float xr[4] = {a4.x, a4.y, a4.z, a4.w}, xi[4] = {b4.x, b4.y, b4.z, b4.w};
     const int e0 = 4 * v;
+    const int r = e0 / C, c = e0 % C;
+    const size_t g = (size_t)(r0 + r) * PT + c0 + c;  // 16-byte aligned: c0, C, PT % 4 == 0
+    const float4 a4 = *reinterpret_cast<const float4*>(ire + g);
+    const float4 b4 = *reinterpret_cast<const float4*>(iim + g);
+    float xr[4] = {a4.x, a4.y, a4.z, a4.w}, xi[4] = {b4.x, b4.y, b4.z, b4.w};
     if (pre.n) {
-      const int r = e0 / C, c = e0 % C;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) pix_apply(pre, k, r, c + q, R, C, xr[q], xi[q]);
+      for (int q = 0; q < 4; ++q) pix_apply(pre, k, r0 + r, c0 + c + q, RT, PT, xr[q], xi[q]);
     }
     if (mre) {
       const float4 m4 = reinterpret_cast<const float4*>(mre)[v];
@@ -404,10 +409,19 @@ size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
 // (the chain executor fuses the elements before a transform here).
 int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
                          const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
-                         const PixOps& pre, const FieldInfo& fi) {
+                         const PixOps& pre, const FieldInfo& fi, const MftWindow* iw,
+                         const MftWindow* ow) {
   CSG_CHECK(ctx && m && in && out && slot, CSG_E_ARG, "csg_mft_execute: null argument");
   CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_mft_execute: n_fields must be positive");
   CSG_CHECK(!in_mul || mul_idx, CSG_E_ARG, "csg_mft_execute: in_mul needs mul_idx");
+  const MftWindow inw = iw ? *iw : MftWindow{0, 0, m->ny, m->nx};
+  const MftWindow outw = ow ? *ow : MftWindow{0, 0, m->mo, m->no};
+  CSG_CHECK(inw.r0 >= 0 && inw.c0 >= 0 && inw.r0 + m->ny <= inw.rows && inw.c0 + m->nx <= inw.pitch &&
+                ((inw.c0 | inw.pitch) & 3) == 0,
+            CSG_E_SHAPE, "csg_mft_execute: input window outside the field or misaligned");
+  CSG_CHECK(outw.r0 >= 0 && outw.c0 >= 0 && outw.r0 + m->mo <= outw.rows &&
+                outw.c0 + m->no <= outw.pitch,
+            CSG_E_SHAPE, "csg_mft_execute: output window outside the field");
   DeviceGuard g(ctx->device);
   cudaStream_t st = ctx->stream;
   int rc;
@@ -421,7 +435,8 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     ProfScope ps(ctx, "mft_split", 0, F * m->ny * m->nx * (8.0 + 12.0 + (in_mul ? 8.0 : 0.0)));
     CSG_CHECK(n_fields < 65536, CSG_E_SHAPE, "csg_mft_execute: too many fields in one call");
     dim3 grid(grid_for((long long)m->ny * m->nx / 4, 256, 1024), n_fields);
-    k_split_field<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, in_mul, mul_idx, pre, fi);
+    k_split_field<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, inw.r0, inw.c0, inw.rows,
+                                        inw.pitch, in_mul, mul_idx, pre, fi);
     CSG_LAUNCH_CHECK();
   }
 
@@ -473,6 +488,10 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.out = out;
     p.out_rows = m->mo;
     p.out_cols = m->no;
+    p.out_pitch = outw.pitch;
+    p.out_plane_rows = outw.rows;
+    p.out_r0 = outw.r0;
+    p.out_c0 = outw.c0;
     p.accumulate = accumulate;
     p.status = ctx->status;
     const int grid = n_fields * p.m_tiles * p.n_tiles;

@@ -156,9 +156,17 @@ int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, d
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi);
 
-// MFT with element ops applied to the input in the operand split.
+// A window of a field: rows x cols of the transform start at (r0, c0) of
+// planes that are `rows` x `pitch`.
+struct MftWindow {
+  int r0, c0, rows, pitch;
+};
+
+// MFT with element ops applied to the input in the operand split; the input
+// and output may be windows of larger fields (nullptr: the whole plane).
 int mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
                     const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
-                    const PixOps& pre, const FieldInfo& fi);
+                    const PixOps& pre, const FieldInfo& fi, const MftWindow* iw = nullptr,
+                    const MftWindow* ow = nullptr);
 
 }  // namespace csg

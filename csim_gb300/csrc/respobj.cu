@@ -234,6 +234,10 @@ int csg_respobj_execute(csg_respobj* o, const double* x, int pop, double* out) {
   p.out_rows = o->npix;
   p.out_cols = pop;
   p.accumulate = 0;
+  p.out_pitch = pop;
+  p.out_plane_rows = o->npix;
+  p.out_r0 = 0;
+  p.out_c0 = 0;
   p.status = ctx->status;
   {
     ProfScope ps2(ctx, "respobj_gemm", 8.0 * o->n_mat * o->npix * (double)pop * o->ncol);

@@ -43,6 +43,10 @@ struct Params {
   int out_rows;     // EPI_T_SPLIT: No (rows of T^T); EPI_F32: Mo
   int out_cols;     // EPI_T_SPLIT: Ny; EPI_F32: No
   int accumulate;   // EPI_F32 only
+  // EPI_F32 output window: element (v, u) of a field's component plane is
+  // stored at (out_r0 + v) * out_pitch + out_c0 + u of planes that are
+  // out_plane_rows x out_pitch (a sub-rectangle of a larger field).
+  int out_pitch, out_plane_rows, out_r0, out_c0;
   int* status;
 };
 
@@ -378,13 +382,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
       }
     } else {
-      // C[v][u] -> out fp32 [field][d][v][u]
+      // C[v][u] -> out fp32 [field][d][out_r0 + v][out_c0 + u] (pitch out_pitch)
       const int v = row_a0 + row;
       if (v < p.rows_valid) {
         float* out = reinterpret_cast<float*>(p.out) +
-                     ((size_t)(field * 2 + d) * p.out_rows + v) * p.out_cols;
+                     ((size_t)(field * 2 + d) * p.out_plane_rows + p.out_r0 + v) * p.out_pitch +
+                     p.out_c0;
         const int u0 = row_b0 + h * CPW;
-        if (u0 + CPW <= p.cols_valid && (p.out_cols & 3) == 0) {
+        if (u0 + CPW <= p.cols_valid && ((p.out_pitch | p.out_c0) & 3) == 0) {
           float4* o4 = reinterpret_cast<float4*>(out + u0);
 #pragma unroll
           for (int j = 0; j < CPW / 4; ++j) {
