@@ -1,23 +1,24 @@
-// Shared-memory Stockham FFTs for square N x N planar fp32 fields and the
-// fused angular-spectrum Fresnel pipeline.
+// Register-resident Stockham FFTs for square N x N planar fp32 fields and
+// the fused angular-spectrum Fresnel pipeline.
 //
-// A 2-D transform is two HBM passes: a row pass (4096/N rows per CTA, float4
-// row loads) and a column pass (a [N][COLS] tile per CTA, coalesced row
-// segments). Each pass reads and writes the field once. Inside a pass every
-// thread owns 16 elements of one transform in registers; stages are radix 16
-// (one radix 2/4/8 stage first when log2 N is not a multiple of 4), so a
-// 1024-point transform is 3 shared-memory exchanges. The radix-R butterflies
-// are unrolled radix-2 decimation-in-frequency networks with exact W16
-// constants; inter-stage twiddles come from an FP64-generated table. Row
-// transforms are padded in shared memory (one float per 16) so the
-// stride-16 stores of the first stage are conflict-free.
+// A 2-D transform is two HBM passes: a row pass (4096/N rows per CTA) and a
+// column pass (COLS columns per CTA). Each pass reads and writes the field
+// once. Every thread owns 16 elements of one transform, u + s N/16, which it
+// loads straight from global memory (32 independent loads in flight per
+// thread) and stores straight back: the first stage runs on the registers
+// as loaded and the last stage leaves its outputs in the same natural
+// order, so shared memory carries only the exchanges between stages (two
+// for N = 1024: radix 16, 16, 4). The radix-R butterflies are unrolled
+// radix-2 decimation-in-frequency networks with exact W16 constants;
+// inter-stage twiddles come from an FP64-generated table. Shared memory is
+// XOR-swizzled (swz) so every stage access is bank-conflict-free.
 //
 // Element ops (point source, masks, mirrors) ride along in the row passes'
 // prologue and epilogue (pixops.cuh), so they cost no extra HBM pass.
 //
 // Fresnel (csim_fft.cpp:371-392) is row FFT | column FFT x H x column IFFT |
-// row IFFT / N^2: three passes, H generated in-kernel from the integer
-// frequency index.
+// row IFFT / N^2: three passes; H comes from a per-wavelength table or is
+// generated in-kernel from the integer frequency index.
 #include <map>
 #include <mutex>
 
@@ -126,16 +127,15 @@ struct ColAddr {
   __device__ __forceinline__ static int at(int t, int m) { return swz(m * COLS + t); }
 };
 
-// One Stockham stage of radix R at sub-length L; each thread owns 16 / R
-// butterflies j = u + i N / 16.
+// Stockham stages of radix R at sub-length L. Each thread owns 16 / R
+// butterflies j = u + i N / 16 of one transform (index t of the tile).
+// stage_read gathers a stage's inputs (with the inter-stage twiddles) into
+// registers, stage_write scatters its outputs.
 template <int N, int R, int L, bool INV, class A>
-__device__ __forceinline__ void stockham_stage(float* __restrict__ re, float* __restrict__ im,
-                                               int t, int u, const float2* __restrict__ tw) {
-  constexpr int TPT = N / 16;
-  constexpr int BPT = 16 / R;
-  constexpr int STRIDE = N / R;
-  constexpr int TWSTEP = N / (L * R);
-  float xr[16], xi[16];
+__device__ __forceinline__ void stage_read(const float* __restrict__ re,
+                                           const float* __restrict__ im, int t, int u,
+                                           const float2* __restrict__ tw, float* xr, float* xi) {
+  constexpr int TPT = N / 16, BPT = 16 / R, STRIDE = N / R, TWSTEP = N / (L * R);
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
     const int j = u + i * TPT;
@@ -155,41 +155,74 @@ __device__ __forceinline__ void stockham_stage(float* __restrict__ re, float* __
       xi[i * R + q] = b;
     }
   }
-  __syncthreads();
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void stage_butterflies(float* xr, float* xi) {
+#pragma unroll
+  for (int i = 0; i < 16 / R; ++i) dif_stage<R, R / 2, INV>(&xr[i * R], &xi[i * R]);
+}
+
+template <int N, int R, int L, class A>
+__device__ __forceinline__ void stage_write(float* __restrict__ re, float* __restrict__ im, int t,
+                                            int u, const float* xr, const float* xi) {
+  constexpr int TPT = N / 16, BPT = 16 / R, bits = ilog2c(R);
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
-    dif_stage<R, R / 2, INV>(&xr[i * R], &xi[i * R]);
     const int j = u + i * TPT;
     const int k = j % L, g = j / L;
 #pragma unroll
     for (int q = 0; q < R; ++q) {
       const int m = g * L * R + k + q * L;
-      constexpr int bits = ilog2c(R);
       re[A::at(t, m)] = xr[i * R + bitrev(q, bits)];
       im[A::at(t, m)] = xi[i * R + bitrev(q, bits)];
     }
   }
-  __syncthreads();
 }
 
-// Full transform: radix-16 stages first, then one radix 2^(log2 N mod 4)
-// stage if needed. (Radix 16 first keeps every stage's stores either
-// contiguous or at stride 16, which the one-in-16 padding makes
-// conflict-free.)
+// Stages from sub-length L on: shared memory holds the output of the stages
+// before L. Radix 16 while 16 L < N, then one final stage of radix N / L
+// whose outputs stay in registers in natural order.
 template <int N, int L, bool INV, class A>
-__device__ __forceinline__ void stockham_from(float* re, float* im, int t, int u,
-                                              const float2* tw) {
-  if constexpr (L * 16 <= N) {
-    stockham_stage<N, 16, L, INV, A>(re, im, t, u, tw);
-    stockham_from<N, L * 16, INV, A>(re, im, t, u, tw);
-  } else if constexpr (L < N) {
-    stockham_stage<N, N / L, L, INV, A>(re, im, t, u, tw);
+__device__ __forceinline__ void fft_tail(float* xr, float* xi, float* re, float* im, int t, int u,
+                                         const float2* tw) {
+  if constexpr (L * 16 < N) {
+    stage_read<N, 16, L, INV, A>(re, im, t, u, tw, xr, xi);
+    __syncthreads();
+    stage_butterflies<16, INV>(xr, xi);
+    stage_write<N, 16, L, A>(re, im, t, u, xr, xi);
+    __syncthreads();
+    fft_tail<N, L * 16, INV, A>(xr, xi, re, im, t, u, tw);
+  } else {
+    constexpr int R = N / L, BPT = 16 / R, bits = ilog2c(R);
+    float yr[16], yi[16];
+    stage_read<N, R, L, INV, A>(re, im, t, u, tw, yr, yi);
+    stage_butterflies<R, INV>(yr, yi);
+    // the last stage writes element k + q L with k = j = u + i N/16 and
+    // L = BPT N/16: element u + (i + q BPT) N/16
+#pragma unroll
+    for (int i = 0; i < BPT; ++i)
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        xr[i + q * BPT] = yr[i * R + bitrev(q, bits)];
+        xi[i + q * BPT] = yi[i * R + bitrev(q, bits)];
+      }
   }
 }
 
+// Length-N transform held by N/16 threads: on entry and on exit register s
+// of thread u holds element u + s N/16 (natural order). The first stage
+// (radix 16, no twiddles) runs on the registers as loaded, so the caller
+// loads straight from global memory and stores the result straight back;
+// shared memory carries only the exchanges between stages. The caller
+// synchronises before shared memory is reused by another transform.
 template <int N, bool INV, class A>
-__device__ __forceinline__ void smem_fft(float* re, float* im, int t, int u, const float2* tw) {
-  stockham_from<N, 1, INV, A>(re, im, t, u, tw);
+__device__ __forceinline__ void fft_regs(float* xr, float* xi, float* re, float* im, int t, int u,
+                                         const float2* tw) {
+  stage_butterflies<16, INV>(xr, xi);
+  stage_write<N, 16, 1, A>(re, im, t, u, xr, xi);
+  __syncthreads();
+  fft_tail<N, 16, INV, A>(xr, xi, re, im, t, u, tw);
 }
 
 template <int N>
@@ -199,59 +232,70 @@ struct RowCfg {
   static constexpr int THREADS = ROWS * TPT;
   static constexpr size_t SMEM = (size_t)ROWS * RowAddr<N>::NP * 8;
 };
-template <int N>
+// Column tile width: 8 columns (32-byte row segments) at N = 1024, so two
+// CTAs of 512 threads share an SM and one loads while the other computes.
+constexpr int default_cols(int n) { return n <= 512 ? 16 : (n == 1024 ? 8 : 4); }
+template <int N, int COLS>
 struct ColCfg {
   static constexpr int TPT = N / 16;
-  static constexpr int COLS = N >= 2048 ? 16 * 1024 / N : 16;
   static constexpr int THREADS = COLS * TPT;
+  static constexpr int MIN_BLOCKS = THREADS >= 1024 ? 1 : (THREADS >= 512 ? 2 : 3);
   static constexpr size_t SMEM = (size_t)COLS * N * 8;
 };
 
 // Row pass with fused element prologue / epilogue.
 template <int N, bool INV>
 __global__ void __launch_bounds__(RowCfg<N>::THREADS, 3)
-    k_fft_rows(float* __restrict__ field, float scale, const float2* __restrict__ tw, PixOps pro,
-               PixOps epi, FieldInfo fi) {
+    k_fft_rows(float* __restrict__ field, float scale, const float2* __restrict__ tw,
+               const __grid_constant__ PixOps pro, const __grid_constant__ PixOps epi,
+               const __grid_constant__ FieldInfo fi) {
   using CF = RowCfg<N>;
   using A = RowAddr<N>;
   extern __shared__ float sm[];
+  __shared__ PixConsts shk[2];
   float* re = sm;
   float* im = sm + CF::ROWS * A::NP;
   constexpr int CPF = N / CF::ROWS;  // CTAs per field
+  constexpr int TPT = CF::TPT;
   const int f = blockIdx.x / CPF;
-  const int r0 = (blockIdx.x % CPF) * CF::ROWS;
+  const int t = threadIdx.x / TPT, u = threadIdx.x % TPT;
+  const int row = (blockIdx.x % CPF) * CF::ROWS + t;
   const size_t plane = (size_t)N * N;
-  float* fre = field + (size_t)f * 2 * plane + (size_t)r0 * N;
+  float* fre = field + (size_t)f * 2 * plane + (size_t)row * N + u;
   float* fim = fre + plane;
-  PixConsts kp, ke;
-  if (pro.n) pix_consts(pro, fi, f, N, N, kp);
-  if (epi.n) pix_consts(epi, fi, f, N, N, ke);
+  // thread u of row t owns elements u + s N/16: each load and store
+  // instruction of a warp covers 32 consecutive floats of one row
+  float xr[16], xi[16];
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // source overwrites: skip the read
-  // one element per thread per instruction: coalesced global access and
-  // consecutive (conflict-free) shared-memory addresses
-  constexpr int NE = CF::ROWS * N;
-#pragma unroll 4
-  for (int e = threadIdx.x; e < NE; e += CF::THREADS) {
-    const int t = e / N, m = e % N;
-    float xr = 0.f, xi = 0.f;
-    if (!gen) {
-      xr = fre[e];
-      xi = fim[e];
+  if (!gen) {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) {
+      xr[s] = fre[s * TPT];
+      xi[s] = fim[s * TPT];
     }
-    if (pro.n) pix_apply(pro, kp, r0 + t, m, N, N, xr, xi);
-    re[A::at(t, m)] = xr;
-    im[A::at(t, m)] = xi;
+  } else {
+#pragma unroll
+    for (int s = 0; s < 16; ++s) xr[s] = xi[s] = 0.f;
   }
-  __syncthreads();
-  const int t = threadIdx.x / CF::TPT, u = threadIdx.x % CF::TPT;
-  smem_fft<N, INV, A>(re, im, t, u, tw);
-#pragma unroll 4
-  for (int e = threadIdx.x; e < NE; e += CF::THREADS) {
-    const int tt = e / N, m = e % N;
-    float xr = re[A::at(tt, m)] * scale, xi = im[A::at(tt, m)] * scale;
-    if (epi.n) pix_apply(epi, ke, r0 + tt, m, N, N, xr, xi);
-    fre[e] = xr;
-    fim[e] = xi;
+  PixConsts kp, ke;
+  if (pro.n) pix_consts_cta(pro, fi, f, N, N, kp, &shk[0]);
+  if (epi.n) pix_consts_cta(epi, fi, f, N, N, ke, &shk[1]);
+  // element ops in two halves of 8 (bounds the live table values)
+  if (pro.n) {
+    pix_apply_n<8>(pro, kp, row, u, 0, TPT, N, N, xr, xi);
+    pix_apply_n<8>(pro, kp, row, u + 8 * TPT, 0, TPT, N, N, xr + 8, xi + 8);
+  }
+  fft_regs<N, INV, A>(xr, xi, re, im, t, u, tw);
+#pragma unroll
+  for (int s = 0; s < 16; ++s) xr[s] *= scale, xi[s] *= scale;
+  if (epi.n) {
+    pix_apply_n<8>(epi, ke, row, u, 0, TPT, N, N, xr, xi);
+    pix_apply_n<8>(epi, ke, row, u + 8 * TPT, 0, TPT, N, N, xr + 8, xi + 8);
+  }
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    fre[s * TPT] = xr[s];
+    fim[s * TPT] = xi[s];
   }
 }
 
@@ -310,61 +354,71 @@ int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, d
 }
 
 // Column pass; MODE 0: forward, 1: inverse, 2: forward * H(lambda_f) * inverse.
-template <int N, int MODE>
-__global__ void __launch_bounds__(ColCfg<N>::THREADS)
-    k_fft_cols(float* __restrict__ field, const float2* __restrict__ tw, FresnelArgs fa) {
-  using CF = ColCfg<N>;
-  using A = ColAddr<CF::COLS>;
+// Thread (t, u) = (threadIdx % COLS, threadIdx / COLS) owns rows u + s N/16
+// of column c0 + t: a warp's load or store covers 32/COLS rows x COLS
+// consecutive floats. In MODE 2 the forward transform leaves each thread
+// holding exactly the elements the inverse transform's first stage needs,
+// so H is applied in registers and the inverse starts without a
+// shared-memory exchange.
+template <int N, int MODE, int COLS>
+__global__ void __launch_bounds__(ColCfg<N, COLS>::THREADS, ColCfg<N, COLS>::MIN_BLOCKS)
+    k_fft_cols(float* __restrict__ field, const float2* __restrict__ tw,
+               const __grid_constant__ FresnelArgs fa) {
+  using CF = ColCfg<N, COLS>;
+  using A = ColAddr<COLS>;
+  constexpr int TPT = CF::TPT;
   extern __shared__ float sm[];
   float* re = sm;
   float* im = sm + A::PITCH * N;
-  constexpr int CPF = N / CF::COLS;
+  constexpr int CPF = N / COLS;
   const int f = blockIdx.x / CPF;
-  const int c0 = (blockIdx.x % CPF) * CF::COLS;
+  const int c0 = (blockIdx.x % CPF) * COLS;
+  const int t = threadIdx.x % COLS, u = threadIdx.x / COLS;
   const size_t plane = (size_t)N * N;
-  float* fre = field + (size_t)f * 2 * plane + c0;
+  float* fre = field + (size_t)f * 2 * plane + (size_t)u * N + c0 + t;
   float* fim = fre + plane;
-  constexpr int NE = CF::COLS * N;
-#pragma unroll 4
-  for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
-    const int r = i / CF::COLS, c = i % CF::COLS;
-    re[A::at(c, r)] = fre[(size_t)r * N + c];
-    im[A::at(c, r)] = fim[(size_t)r * N + c];
+  float xr[16], xi[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    xr[s] = fre[(size_t)s * TPT * N];
+    xi[s] = fim[(size_t)s * TPT * N];
   }
-  __syncthreads();
-  const int t = threadIdx.x % CF::COLS, u = threadIdx.x / CF::COLS;
-  smem_fft<N, MODE == 1, A>(re, im, t, u, tw);
+  fft_regs<N, MODE == 1, A>(xr, xi, re, im, t, u, tw);
   if (MODE == 2) {
     if (fa.H) {  // per-wavelength table (L2-resident, shared by the batch)
-      const float2* Hs = fa.H + (size_t)fa.slot[f] * N * N + c0;
-#pragma unroll 4
-      for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
-        const int r = i / CF::COLS, cl = i % CF::COLS;
-        const float2 w = Hs[(size_t)r * N + cl];
-        const int a = A::at(cl, r);
-        const float xr = re[a], xi = im[a];
-        re[a] = xr * w.x - xi * w.y;
-        im[a] = xr * w.y + xi * w.x;
+      const float2* Hs = fa.H + (size_t)fa.slot[f] * plane + (size_t)u * N + c0 + t;
+#pragma unroll
+      for (int h = 0; h < 16; h += 8) {  // in halves of 8 (bounds the live table values)
+        float2 w[8];
+#pragma unroll
+        for (int s = 0; s < 8; ++s) w[s] = __ldg(&Hs[(size_t)(h + s) * TPT * N]);
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+          const float a = xr[h + s];
+          xr[h + s] = a * w[s].x - xi[h + s] * w[s].y;
+          xi[h + s] = a * w[s].y + xi[h + s] * w[s].x;
+        }
       }
     } else {
-      const FresnelConsts fc = fresnel_consts(fa.lambda[f], fa.z, fa.ap_rad);
-      for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
-        const int r = i / CF::COLS, cl = i % CF::COLS;
-        const float2 w = fresnel_h(N, r, c0 + cl, fc);
-        const int a = A::at(cl, r);
-        const float xr = re[a], xi = im[a];
-        re[a] = xr * w.x - xi * w.y;
-        im[a] = xr * w.y + xi * w.x;
+      __shared__ FresnelConsts shc;
+      if (threadIdx.x == 0) shc = fresnel_consts(fa.lambda[f], fa.z, fa.ap_rad);
+      __syncthreads();
+      const FresnelConsts fc = shc;
+#pragma unroll
+      for (int s = 0; s < 16; ++s) {
+        const float2 w = fresnel_h(N, u + s * TPT, c0 + t, fc);
+        const float a = xr[s];
+        xr[s] = a * w.x - xi[s] * w.y;
+        xi[s] = a * w.y + xi[s] * w.x;
       }
     }
-    __syncthreads();
-    smem_fft<N, true, A>(re, im, t, u, tw);
+    __syncthreads();  // the forward transform's last reads precede the inverse's writes
+    fft_regs<N, true, A>(xr, xi, re, im, t, u, tw);
   }
-#pragma unroll 4
-  for (int i = threadIdx.x; i < NE; i += CF::THREADS) {
-    const int r = i / CF::COLS, c = i % CF::COLS;
-    fre[(size_t)r * N + c] = re[A::at(c, r)];
-    fim[(size_t)r * N + c] = im[A::at(c, r)];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    fre[(size_t)s * TPT * N] = xr[s];
+    fim[(size_t)s * TPT * N] = xi[s];
   }
 }
 
@@ -377,13 +431,42 @@ static int prep_smem(K kern, size_t bytes) {
   return CSG_OK;
 }
 
+template <int N, int COLS>
+static int launch_cols(cudaStream_t st, float* field, int F, int mode, const float2* tw,
+                       const FresnelArgs* fa) {
+  using CC = ColCfg<N, COLS>;
+  const int grid = F * (N / COLS);
+  int rc;
+  if (mode == 2) {
+    if ((rc = prep_smem(k_fft_cols<N, 2, COLS>, CC::SMEM))) return rc;
+    k_fft_cols<N, 2, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
+  } else if (mode == 1) {
+    if ((rc = prep_smem(k_fft_cols<N, 1, COLS>, CC::SMEM))) return rc;
+    k_fft_cols<N, 1, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+  } else {
+    if ((rc = prep_smem(k_fft_cols<N, 0, COLS>, CC::SMEM))) return rc;
+    k_fft_cols<N, 0, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+  }
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
+// Column tile width override for N = 1024 (4, 8 or 16; tuning only).
+static int cols_override() {
+  static const int v = [] {
+    const char* s = getenv("CSG_FFT_COLS");
+    const int c = s ? atoi(s) : 0;
+    return (c == 4 || c == 8 || c == 16) ? c : 0;
+  }();
+  return v;
+}
+
 template <int N>
 static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const FresnelArgs* fa,
                    const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw) {
   using RC = RowCfg<N>;
-  using CC = ColCfg<N>;
   cudaStream_t st = ctx->stream;
-  const int rgrid = F * (N / RC::ROWS), cgrid = F * (N / CC::COLS);
+  const int rgrid = F * (N / RC::ROWS);
   const float inv_scale = 1.f / ((float)N * (float)N);
   const double pass_bytes = (double)F * N * N * 16.0;
   const PixOps none;
@@ -403,18 +486,12 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
   };
   auto cols = [&](int mode) -> int {
     ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, pass_bytes);
-    if (mode == 2) {
-      if ((rc = prep_smem(k_fft_cols<N, 2>, CC::SMEM))) return rc;
-      k_fft_cols<N, 2><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
-    } else if (mode == 1) {
-      if ((rc = prep_smem(k_fft_cols<N, 1>, CC::SMEM))) return rc;
-      k_fft_cols<N, 1><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
-    } else {
-      if ((rc = prep_smem(k_fft_cols<N, 0>, CC::SMEM))) return rc;
-      k_fft_cols<N, 0><<<cgrid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    if constexpr (N == 1024) {
+      const int c = cols_override();
+      if (c == 4) return launch_cols<N, 4>(st, field, F, mode, tw, fa);
+      if (c == 16) return launch_cols<N, 16>(st, field, F, mode, tw, fa);
     }
-    CSG_LAUNCH_CHECK();
-    return CSG_OK;
+    return launch_cols<N, default_cols(N)>(st, field, F, mode, tw, fa);
   };
   if (fa) {
     if ((rc = rows(false, 1.f, pro, none))) return rc;

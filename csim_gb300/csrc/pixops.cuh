@@ -74,6 +74,109 @@ __device__ __forceinline__ void pix_consts(const PixOps& ops, const FieldInfo& f
   }
 }
 
+// CTA-wide per-field constants: one thread evaluates the FP64 expressions,
+// the rest read them after a barrier (every thread of the CTA must call it,
+// and the CTA must cover a single field).
+__device__ __forceinline__ void pix_consts_cta(const PixOps& ops, const FieldInfo& fi, int f, int R,
+                                               int C, PixConsts& k, PixConsts* shared) {
+  if (threadIdx.x == 0) pix_consts(ops, fi, f, R, C, *shared);
+  __syncthreads();
+  k = *shared;
+}
+
+__device__ __forceinline__ float pick(const float* v, int i) {
+  float x = v[0];
+#pragma unroll
+  for (int j = 1; j < MAX_PIXOPS; ++j)
+    if (i == j) x = v[j];
+  return x;
+}
+
+// Apply the ops to NE pixels (r + e dr, c + e dc), e < NE, of an R x C field
+// held in registers. Ops are applied one at a time over all NE pixels, so
+// each op's NE table reads are issued together.
+template <int NE>
+__device__ __forceinline__ void pix_apply_n(const PixOps& ops, const PixConsts& k, int r, int c,
+                                            int dr, int dc, int R, int C, float* re, float* im) {
+#pragma unroll 1
+  for (int i = 0; i < ops.n; ++i) {
+    const int kind = ops.kind[i];
+    const float* a = ops.a[i];
+    if (kind == OP_SOURCE) {
+      if (k.sxh == 0.f && k.syh == 0.f && k.sxl == 0.f && k.syl == 0.f) {
+#pragma unroll
+        for (int e = 0; e < NE; ++e) re[e] = k.amp, im[e] = 0.f;
+      } else {
+#pragma unroll
+        for (int e = 0; e < NE; ++e) {
+          const float xc = (float)(c + e * dc) - 0.5f * (float)(C - 1);
+          const float yr = (float)(r + e * dr) - 0.5f * (float)(R - 1);
+          float t = frac_prod(xc, k.sxh, k.sxl) + frac_prod(yr, k.syh, k.syl);
+          t -= rintf(t);
+          float s, co;
+          sincospif(2.f * t, &s, &co);
+          re[e] = k.amp * co;
+          im[e] = k.amp * s;
+        }
+      }
+    } else if (kind == OP_MASK) {
+      float m[NE];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) m[e] = __ldg(&a[(size_t)(r + e * dr) * C + c + e * dc]);
+      if (ops.param[i] != 0.f) {
+#pragma unroll
+        for (int e = 0; e < NE; ++e) {
+          const float t = m[e] * (re[e] - im[e]);
+          im[e] = m[e] * (re[e] + im[e]);
+          re[e] = t;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < NE; ++e) re[e] *= m[e], im[e] *= m[e];
+      }
+    } else if (kind == OP_PHASE) {
+      const float khi = pick(k.khi, i), klo = pick(k.klo, i);
+      float sg[NE];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) sg[e] = __ldg(&a[(size_t)(r + e * dr) * C + c + e * dc]);
+#pragma unroll
+      for (int e = 0; e < NE; ++e) {
+        float s, co;
+        sincospif(2.f * frac_prod(sg[e], khi, klo), &s, &co);
+        const float xr = re[e];
+        re[e] = xr * co - im[e] * s;
+        im[e] = xr * s + im[e] * co;
+      }
+    } else if (kind == OP_PHASOR) {
+      const float2* w = reinterpret_cast<const float2*>(a) + (size_t)k.slot * R * C;
+      float2 wv[NE];
+#pragma unroll
+      for (int e = 0; e < NE; ++e) wv[e] = __ldg(&w[(size_t)(r + e * dr) * C + c + e * dc]);
+#pragma unroll
+      for (int e = 0; e < NE; ++e) {
+        const float xr = re[e];
+        re[e] = xr * wv[e].x - im[e] * wv[e].y;
+        im[e] = xr * wv[e].y + im[e] * wv[e].x;
+      }
+    } else if (kind == OP_CMASK) {
+      const int r0 = R / 2 - ops.mr[i] / 2, c0 = C / 2 - ops.mc[i] / 2;
+#pragma unroll
+      for (int e = 0; e < NE; ++e) {
+        const int rr = r + e * dr - r0, cc = c + e * dc - c0;
+        if (rr >= 0 && rr < ops.mr[i] && cc >= 0 && cc < ops.mc[i]) {
+          const size_t o = (size_t)rr * ops.mc[i] + cc;
+          float s, co;
+          sincosf(-ops.b[i][o], &s, &co);
+          const float am = a[o];
+          const float xr = re[e];
+          re[e] = am * (xr * co - im[e] * s);
+          im[e] = am * (xr * s + im[e] * co);
+        }
+      }
+    }
+  }
+}
+
 // Apply the ops to pixel (r, c) of an R x C field.
 __device__ __forceinline__ void pix_apply(const PixOps& ops, const PixConsts& k, int r, int c,
                                           int R, int C, float& re, float& im) {
