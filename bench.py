@@ -63,7 +63,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
 
@@ -131,7 +131,7 @@ def reference_arm(args):
     inp = host_inputs(spec)
     rng = np.random.default_rng(7)
     sags = rng.uniform(-spec.sag_range, spec.sag_range, (8, spec.n_hex))
-    per_step = 2
+    per_step = 1 if args.steps > 20 else 2  # bounded: the whole run stays within minutes
     for _ in range(args.warmup):
         cpu_fields_per_s(spec, inp, sags, 1e9, 1)
     t0 = time.perf_counter()
@@ -157,7 +157,7 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--fields", type=int, default=64)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -223,6 +223,13 @@ def main():
     hbm_peak, tc_peak, peak_kind = peaks()
     clocks = ClockSampler(local)
     clocks.start()
+    # keep the GPU busy while nvidia-smi starts, so its first samples fall
+    # under load rather than on an idle GPU
+    with torch.cuda.stream(stream):
+        t_spin = time.perf_counter()
+        while time.perf_counter() - t_spin < 0.5:
+            step()
+            stream.synchronize()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -343,10 +350,11 @@ def main():
     return 0
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per k_split_gemm launch from the
-# committed ncu capture (see profiles/), keyed by fields per step; None until
-# captured.
-TRAFFIC: dict = {}
+# dram__bytes_read.sum + dram__bytes_write.sum per k_split_gemm launch,
+# averaged over the six GEMM launches of one step, keyed by fields per step:
+# an ncu capture at 32 fields (1222.8 MB per step) scaled by the field count
+# (profiles/k_split_gemm_piaacmc1024_32fields.md).
+TRAFFIC: dict = {64: 407.6e6, 32: 203.8e6}
 
 if __name__ == "__main__":
     sys.exit(main())

@@ -56,15 +56,20 @@ static const float2* twiddles(int device, int n, cudaStream_t st) {
 }
 
 // ------------------------------------------------ in-register butterflies
-// cos and sin of 2 pi m / 16.
-__device__ __forceinline__ float w16c(int m) {
-  constexpr float c[16] = {1.0f, 0.92387953251128674f, 0.70710678118654752f, 0.38268343236508977f,
-                           0.0f, -0.38268343236508977f, -0.70710678118654752f, -0.92387953251128674f,
-                           -1.0f, -0.92387953251128674f, -0.70710678118654752f, -0.38268343236508977f,
-                           0.0f, 0.38268343236508977f, 0.70710678118654752f, 0.92387953251128674f};
+// cos and sin of 2 pi m / 32.
+__device__ __forceinline__ float w32c(int m) {
+  constexpr float c[32] = {
+      1.0f,  0.98078528040323043f,  0.92387953251128674f,  0.83146961230254524f,
+      0.70710678118654757f,  0.55557023301960218f,  0.38268343236508978f,  0.19509032201612828f,
+      0.0f, -0.19509032201612828f, -0.38268343236508978f, -0.55557023301960218f,
+      -0.70710678118654757f, -0.83146961230254524f, -0.92387953251128674f, -0.98078528040323043f,
+      -1.0f, -0.98078528040323043f, -0.92387953251128674f, -0.83146961230254524f,
+      -0.70710678118654757f, -0.55557023301960218f, -0.38268343236508978f, -0.19509032201612828f,
+      0.0f,  0.19509032201612828f,  0.38268343236508978f,  0.55557023301960218f,
+      0.70710678118654757f,  0.83146961230254524f,  0.92387953251128674f,  0.98078528040323043f};
   return c[m];
 }
-__device__ __forceinline__ float w16s(int m) { return w16c((m + 12) & 15); }  // sin = cos(. - pi/2)
+__device__ __forceinline__ float w32s(int m) { return w32c((m + 24) & 31); }  // sin = cos(. - pi/2)
 
 constexpr int bitrev(int q, int bits) {
   int r = 0;
@@ -87,16 +92,16 @@ __device__ __forceinline__ void dif_stage(float* xr, float* xi) {
         xr[base + k] = ar + br;
         xi[base + k] = ai + bi;
         const float dr = ar - br, di = ai - bi;
-        constexpr int step = 16 / (2 * HALF);
+        constexpr int step = 32 / (2 * HALF);  // twiddle W_{2 HALF}^k = W_32^(k step)
         const int m = k * step;
         if (m == 0) {
           xr[base + k + HALF] = dr;
           xi[base + k + HALF] = di;
-        } else if (m == 4) {  // times -i (forward) or +i (inverse)
+        } else if (m == 8) {  // times -i (forward) or +i (inverse)
           xr[base + k + HALF] = INV ? -di : di;
           xi[base + k + HALF] = INV ? dr : -dr;
         } else {
-          const float c = w16c(m), s = INV ? w16s(m) : -w16s(m);
+          const float c = w32c(m), s = INV ? w32s(m) : -w32s(m);
           xr[base + k + HALF] = dr * c - di * s;
           xi[base + k + HALF] = dr * s + di * c;
         }
@@ -106,36 +111,39 @@ __device__ __forceinline__ void dif_stage(float* xr, float* xi) {
   }
 }
 
-// Shared-memory swizzle: word address s is stored at s ^ ((s >> 4) & 31).
-// It permutes words within each aligned 32-word row, and it makes every
-// access of these transforms (32 consecutive elements, the stride-16 stores
-// of a radix-16 stage, the (g, k) scatter of the later stages, and the
-// column tile's 16-column rows) hit 32 distinct banks (checked exhaustively
-// for N = 256..4096).
-__device__ __forceinline__ int swz(int s) { return s ^ ((s >> 4) & 31); }
+// Shared-memory swizzle for E elements per thread: word address s is stored
+// at s ^ ((s >> log2 E) & 31). It permutes words within each aligned
+// 32-word row, and it makes every shared-memory access of these transforms
+// (the stride-E stores of the first stage, the (g, k) gathers and scatters
+// of the later stages, for rows of any N and for column tiles of 4, 8 or 16
+// columns) hit 32 distinct banks; checked exhaustively for N = 64..4096,
+// E = 16 and 32.
+template <int E>
+__device__ __forceinline__ int swz(int s) {
+  return s ^ ((s >> ilog2c(E)) & 31);
+}
 
-// Row layout: transform t at t * N.
-template <int N>
+// Row layout: element m of transform t at t * N + m.
+template <int N, int E>
 struct RowAddr {
-  static constexpr int NP = N;
-  __device__ __forceinline__ static int at(int t, int m) { return t * N + swz(m); }
+  __device__ __forceinline__ static int at(int t, int m) { return swz<E>(t * N + m); }
 };
 // Column layout: element m of column t at m * COLS + t.
-template <int COLS>
+template <int COLS, int E>
 struct ColAddr {
   static constexpr int PITCH = COLS;
-  __device__ __forceinline__ static int at(int t, int m) { return swz(m * COLS + t); }
+  __device__ __forceinline__ static int at(int t, int m) { return swz<E>(m * COLS + t); }
 };
 
-// Stockham stages of radix R at sub-length L. Each thread owns 16 / R
-// butterflies j = u + i N / 16 of one transform (index t of the tile).
+// Stockham stages of radix R at sub-length L. Each thread owns E / R
+// butterflies j = u + i N / E of one transform (index t of the tile).
 // stage_read gathers a stage's inputs (with the inter-stage twiddles) into
 // registers, stage_write scatters its outputs.
-template <int N, int R, int L, bool INV, class A>
+template <int N, int E, int R, int L, bool INV, class A>
 __device__ __forceinline__ void stage_read(const float* __restrict__ re,
                                            const float* __restrict__ im, int t, int u,
                                            const float2* __restrict__ tw, float* xr, float* xi) {
-  constexpr int TPT = N / 16, BPT = 16 / R, STRIDE = N / R, TWSTEP = N / (L * R);
+  constexpr int TPT = N / E, BPT = E / R, STRIDE = N / R, TWSTEP = N / (L * R);
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
     const int j = u + i * TPT;
@@ -157,16 +165,16 @@ __device__ __forceinline__ void stage_read(const float* __restrict__ re,
   }
 }
 
-template <int R, bool INV>
+template <int E, int R, bool INV>
 __device__ __forceinline__ void stage_butterflies(float* xr, float* xi) {
 #pragma unroll
-  for (int i = 0; i < 16 / R; ++i) dif_stage<R, R / 2, INV>(&xr[i * R], &xi[i * R]);
+  for (int i = 0; i < E / R; ++i) dif_stage<R, R / 2, INV>(&xr[i * R], &xi[i * R]);
 }
 
-template <int N, int R, int L, class A>
+template <int N, int E, int R, int L, class A>
 __device__ __forceinline__ void stage_write(float* __restrict__ re, float* __restrict__ im, int t,
                                             int u, const float* xr, const float* xi) {
-  constexpr int TPT = N / 16, BPT = 16 / R, bits = ilog2c(R);
+  constexpr int TPT = N / E, BPT = E / R, bits = ilog2c(R);
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
     const int j = u + i * TPT;
@@ -181,25 +189,25 @@ __device__ __forceinline__ void stage_write(float* __restrict__ re, float* __res
 }
 
 // Stages from sub-length L on: shared memory holds the output of the stages
-// before L. Radix 16 while 16 L < N, then one final stage of radix N / L
+// before L. Radix E while E L < N, then one final stage of radix N / L
 // whose outputs stay in registers in natural order.
-template <int N, int L, bool INV, class A>
+template <int N, int E, int L, bool INV, class A>
 __device__ __forceinline__ void fft_tail(float* xr, float* xi, float* re, float* im, int t, int u,
                                          const float2* tw) {
-  if constexpr (L * 16 < N) {
-    stage_read<N, 16, L, INV, A>(re, im, t, u, tw, xr, xi);
+  if constexpr (L * E < N) {
+    stage_read<N, E, E, L, INV, A>(re, im, t, u, tw, xr, xi);
     __syncthreads();
-    stage_butterflies<16, INV>(xr, xi);
-    stage_write<N, 16, L, A>(re, im, t, u, xr, xi);
+    stage_butterflies<E, E, INV>(xr, xi);
+    stage_write<N, E, E, L, A>(re, im, t, u, xr, xi);
     __syncthreads();
-    fft_tail<N, L * 16, INV, A>(xr, xi, re, im, t, u, tw);
+    fft_tail<N, E, L * E, INV, A>(xr, xi, re, im, t, u, tw);
   } else {
-    constexpr int R = N / L, BPT = 16 / R, bits = ilog2c(R);
-    float yr[16], yi[16];
-    stage_read<N, R, L, INV, A>(re, im, t, u, tw, yr, yi);
-    stage_butterflies<R, INV>(yr, yi);
-    // the last stage writes element k + q L with k = j = u + i N/16 and
-    // L = BPT N/16: element u + (i + q BPT) N/16
+    constexpr int R = N / L, BPT = E / R, bits = ilog2c(R);
+    float yr[E], yi[E];
+    stage_read<N, E, R, L, INV, A>(re, im, t, u, tw, yr, yi);
+    stage_butterflies<E, R, INV>(yr, yi);
+    // the last stage writes element k + q L with k = j = u + i N/E and
+    // L = BPT N/E: element u + (i + q BPT) N/E
 #pragma unroll
     for (int i = 0; i < BPT; ++i)
 #pragma unroll
@@ -210,51 +218,61 @@ __device__ __forceinline__ void fft_tail(float* xr, float* xi, float* re, float*
   }
 }
 
-// Length-N transform held by N/16 threads: on entry and on exit register s
-// of thread u holds element u + s N/16 (natural order). The first stage
-// (radix 16, no twiddles) runs on the registers as loaded, so the caller
+// Length-N transform held by N/E threads: on entry and on exit register s
+// of thread u holds element u + s N/E (natural order). The first stage
+// (radix E, no twiddles) runs on the registers as loaded, so the caller
 // loads straight from global memory and stores the result straight back;
 // shared memory carries only the exchanges between stages. The caller
 // synchronises before shared memory is reused by another transform.
-template <int N, bool INV, class A>
+template <int N, int E, bool INV, class A>
 __device__ __forceinline__ void fft_regs(float* xr, float* xi, float* re, float* im, int t, int u,
                                          const float2* tw) {
-  stage_butterflies<16, INV>(xr, xi);
-  stage_write<N, 16, 1, A>(re, im, t, u, xr, xi);
+  stage_butterflies<E, E, INV>(xr, xi);
+  stage_write<N, E, E, 1, A>(re, im, t, u, xr, xi);
   __syncthreads();
-  fft_tail<N, 16, INV, A>(xr, xi, re, im, t, u, tw);
+  fft_tail<N, E, E, INV, A>(xr, xi, re, im, t, u, tw);
 }
 
-template <int N>
+// Elements per thread: 32 (radix-32 stages, one shared-memory exchange at
+// N = 1024, 128 registers) from N = 512 up, 16 below.
+constexpr int default_e(int n) { return n >= 512 ? 32 : 16; }
+// CTAs per SM the register budget is sized for: 128 registers per thread at
+// E = 32, 64-85 at E = 16.
+constexpr int min_blocks(int e, int threads) {
+  return e == 32 ? (threads >= 512 ? 1 : 512 / threads)
+                 : (threads >= 1024 ? 1 : (threads >= 512 ? 2 : 3));
+}
+
+template <int N, int E>
 struct RowCfg {
-  static constexpr int TPT = N / 16;
-  static constexpr int ROWS = 4096 / N > 0 ? 4096 / N : 1;  // 256 threads per CTA
+  static constexpr int TPT = N / E;
+  static constexpr int ROWS = 256 / TPT > 0 ? 256 / TPT : 1;  // 256 threads per CTA
   static constexpr int THREADS = ROWS * TPT;
-  static constexpr size_t SMEM = (size_t)ROWS * RowAddr<N>::NP * 8;
+  static constexpr int MIN_BLOCKS = min_blocks(E, THREADS);
+  static constexpr size_t SMEM = (size_t)ROWS * N * 8;
 };
-// Column tile width: 8 columns (32-byte row segments) at N = 1024, so two
-// CTAs of 512 threads share an SM and one loads while the other computes.
+// Column tile width: 8 columns (32-byte row segments) at N = 1024.
 constexpr int default_cols(int n) { return n <= 512 ? 16 : (n == 1024 ? 8 : 4); }
-template <int N, int COLS>
+template <int N, int E, int COLS>
 struct ColCfg {
-  static constexpr int TPT = N / 16;
+  static constexpr int TPT = N / E;
   static constexpr int THREADS = COLS * TPT;
-  static constexpr int MIN_BLOCKS = THREADS >= 1024 ? 1 : (THREADS >= 512 ? 2 : 3);
+  static constexpr int MIN_BLOCKS = min_blocks(E, THREADS);
   static constexpr size_t SMEM = (size_t)COLS * N * 8;
 };
 
 // Row pass with fused element prologue / epilogue.
-template <int N, bool INV>
-__global__ void __launch_bounds__(RowCfg<N>::THREADS, 3)
+template <int N, int E, bool INV>
+__global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCKS)
     k_fft_rows(float* __restrict__ field, float scale, const float2* __restrict__ tw,
                const __grid_constant__ PixOps pro, const __grid_constant__ PixOps epi,
                const __grid_constant__ FieldInfo fi) {
-  using CF = RowCfg<N>;
-  using A = RowAddr<N>;
+  using CF = RowCfg<N, E>;
+  using A = RowAddr<N, E>;
   extern __shared__ float sm[];
   __shared__ PixConsts shk[2];
   float* re = sm;
-  float* im = sm + CF::ROWS * A::NP;
+  float* im = sm + CF::ROWS * N;
   constexpr int CPF = N / CF::ROWS;  // CTAs per field
   constexpr int TPT = CF::TPT;
   const int f = blockIdx.x / CPF;
@@ -263,37 +281,39 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS, 3)
   const size_t plane = (size_t)N * N;
   float* fre = field + (size_t)f * 2 * plane + (size_t)row * N + u;
   float* fim = fre + plane;
-  // thread u of row t owns elements u + s N/16: each load and store
-  // instruction of a warp covers 32 consecutive floats of one row
-  float xr[16], xi[16];
+  // thread u of row t owns elements u + s N/E: each load and store
+  // instruction of a warp covers 32 consecutive floats of a row
+  float xr[E], xi[E];
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // source overwrites: skip the read
   if (!gen) {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) {
+    for (int s = 0; s < E; ++s) {
       xr[s] = fre[s * TPT];
       xi[s] = fim[s * TPT];
     }
   } else {
 #pragma unroll
-    for (int s = 0; s < 16; ++s) xr[s] = xi[s] = 0.f;
+    for (int s = 0; s < E; ++s) xr[s] = xi[s] = 0.f;
   }
   PixConsts kp, ke;
   if (pro.n) pix_consts_cta(pro, fi, f, N, N, kp, &shk[0]);
   if (epi.n) pix_consts_cta(epi, fi, f, N, N, ke, &shk[1]);
-  // element ops in two halves of 8 (bounds the live table values)
+  // element ops in groups of 8 (bounds the live table values)
   if (pro.n) {
-    pix_apply_n<8>(pro, kp, row, u, 0, TPT, N, N, xr, xi);
-    pix_apply_n<8>(pro, kp, row, u + 8 * TPT, 0, TPT, N, N, xr + 8, xi + 8);
-  }
-  fft_regs<N, INV, A>(xr, xi, re, im, t, u, tw);
 #pragma unroll
-  for (int s = 0; s < 16; ++s) xr[s] *= scale, xi[s] *= scale;
+    for (int h = 0; h < E; h += 8)
+      pix_apply_n<8>(pro, kp, row, u + h * TPT, 0, TPT, N, N, xr + h, xi + h);
+  }
+  fft_regs<N, E, INV, A>(xr, xi, re, im, t, u, tw);
+#pragma unroll
+  for (int s = 0; s < E; ++s) xr[s] *= scale, xi[s] *= scale;
   if (epi.n) {
-    pix_apply_n<8>(epi, ke, row, u, 0, TPT, N, N, xr, xi);
-    pix_apply_n<8>(epi, ke, row, u + 8 * TPT, 0, TPT, N, N, xr + 8, xi + 8);
+#pragma unroll
+    for (int h = 0; h < E; h += 8)
+      pix_apply_n<8>(epi, ke, row, u + h * TPT, 0, TPT, N, N, xr + h, xi + h);
   }
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < E; ++s) {
     fre[s * TPT] = xr[s];
     fim[s * TPT] = xi[s];
   }
@@ -360,12 +380,12 @@ int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, d
 // holding exactly the elements the inverse transform's first stage needs,
 // so H is applied in registers and the inverse starts without a
 // shared-memory exchange.
-template <int N, int MODE, int COLS>
-__global__ void __launch_bounds__(ColCfg<N, COLS>::THREADS, ColCfg<N, COLS>::MIN_BLOCKS)
+template <int N, int E, int MODE, int COLS>
+__global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS>::MIN_BLOCKS)
     k_fft_cols(float* __restrict__ field, const float2* __restrict__ tw,
                const __grid_constant__ FresnelArgs fa) {
-  using CF = ColCfg<N, COLS>;
-  using A = ColAddr<COLS>;
+  using CF = ColCfg<N, E, COLS>;
+  using A = ColAddr<COLS, E>;
   constexpr int TPT = CF::TPT;
   extern __shared__ float sm[];
   float* re = sm;
@@ -377,18 +397,18 @@ __global__ void __launch_bounds__(ColCfg<N, COLS>::THREADS, ColCfg<N, COLS>::MIN
   const size_t plane = (size_t)N * N;
   float* fre = field + (size_t)f * 2 * plane + (size_t)u * N + c0 + t;
   float* fim = fre + plane;
-  float xr[16], xi[16];
+  float xr[E], xi[E];
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < E; ++s) {
     xr[s] = fre[(size_t)s * TPT * N];
     xi[s] = fim[(size_t)s * TPT * N];
   }
-  fft_regs<N, MODE == 1, A>(xr, xi, re, im, t, u, tw);
+  fft_regs<N, E, MODE == 1, A>(xr, xi, re, im, t, u, tw);
   if (MODE == 2) {
     if (fa.H) {  // per-wavelength table (L2-resident, shared by the batch)
       const float2* Hs = fa.H + (size_t)fa.slot[f] * plane + (size_t)u * N + c0 + t;
 #pragma unroll
-      for (int h = 0; h < 16; h += 8) {  // in halves of 8 (bounds the live table values)
+      for (int h = 0; h < E; h += 8) {  // in groups of 8 (bounds the live table values)
         float2 w[8];
 #pragma unroll
         for (int s = 0; s < 8; ++s) w[s] = __ldg(&Hs[(size_t)(h + s) * TPT * N]);
@@ -405,7 +425,7 @@ __global__ void __launch_bounds__(ColCfg<N, COLS>::THREADS, ColCfg<N, COLS>::MIN
       __syncthreads();
       const FresnelConsts fc = shc;
 #pragma unroll
-      for (int s = 0; s < 16; ++s) {
+      for (int s = 0; s < E; ++s) {
         const float2 w = fresnel_h(N, u + s * TPT, c0 + t, fc);
         const float a = xr[s];
         xr[s] = a * w.x - xi[s] * w.y;
@@ -413,10 +433,10 @@ __global__ void __launch_bounds__(ColCfg<N, COLS>::THREADS, ColCfg<N, COLS>::MIN
       }
     }
     __syncthreads();  // the forward transform's last reads precede the inverse's writes
-    fft_regs<N, true, A>(xr, xi, re, im, t, u, tw);
+    fft_regs<N, E, true, A>(xr, xi, re, im, t, u, tw);
   }
 #pragma unroll
-  for (int s = 0; s < 16; ++s) {
+  for (int s = 0; s < E; ++s) {
     fre[(size_t)s * TPT * N] = xr[s];
     fim[(size_t)s * TPT * N] = xi[s];
   }
@@ -431,67 +451,78 @@ static int prep_smem(K kern, size_t bytes) {
   return CSG_OK;
 }
 
-template <int N, int COLS>
+template <int N, int E, int COLS>
 static int launch_cols(cudaStream_t st, float* field, int F, int mode, const float2* tw,
                        const FresnelArgs* fa) {
-  using CC = ColCfg<N, COLS>;
+  using CC = ColCfg<N, E, COLS>;
   const int grid = F * (N / COLS);
   int rc;
   if (mode == 2) {
-    if ((rc = prep_smem(k_fft_cols<N, 2, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, 2, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
+    if ((rc = prep_smem(k_fft_cols<N, E, 2, COLS>, CC::SMEM))) return rc;
+    k_fft_cols<N, E, 2, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
   } else if (mode == 1) {
-    if ((rc = prep_smem(k_fft_cols<N, 1, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, 1, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    if ((rc = prep_smem(k_fft_cols<N, E, 1, COLS>, CC::SMEM))) return rc;
+    k_fft_cols<N, E, 1, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
   } else {
-    if ((rc = prep_smem(k_fft_cols<N, 0, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, 0, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    if ((rc = prep_smem(k_fft_cols<N, E, 0, COLS>, CC::SMEM))) return rc;
+    k_fft_cols<N, E, 0, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
   }
   CSG_LAUNCH_CHECK();
   return CSG_OK;
 }
 
-// Column tile width override for N = 1024 (4, 8 or 16; tuning only).
-static int cols_override() {
-  static const int v = [] {
-    const char* s = getenv("CSG_FFT_COLS");
-    const int c = s ? atoi(s) : 0;
-    return (c == 4 || c == 8 || c == 16) ? c : 0;
-  }();
-  return v;
+template <int N, int E>
+static int launch_rows(cudaStream_t st, float* field, int F, bool inv, float scale,
+                       const float2* tw, const PixOps& p, const PixOps& e, const FieldInfo& fi) {
+  using RC = RowCfg<N, E>;
+  const int grid = F * (N / RC::ROWS);
+  int rc;
+  if (inv) {
+    if ((rc = prep_smem(k_fft_rows<N, E, true>, RC::SMEM))) return rc;
+    k_fft_rows<N, E, true><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
+  } else {
+    if ((rc = prep_smem(k_fft_rows<N, E, false>, RC::SMEM))) return rc;
+    k_fft_rows<N, E, false><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
+  }
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
+// Tuning overrides for N = 1024: CSG_FFT_COLS (4, 8 or 16 columns per
+// column-pass CTA) and CSG_FFT_E (16 elements per thread instead of 32).
+static int env_choice(const char* name, std::initializer_list<int> allowed) {
+  const char* s = getenv(name);
+  const int c = s ? atoi(s) : 0;
+  for (int a : allowed)
+    if (c == a) return c;
+  return 0;
 }
 
 template <int N>
 static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const FresnelArgs* fa,
                    const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw) {
-  using RC = RowCfg<N>;
   cudaStream_t st = ctx->stream;
-  const int rgrid = F * (N / RC::ROWS);
   const float inv_scale = 1.f / ((float)N * (float)N);
   const double pass_bytes = (double)F * N * N * 16.0;
   const PixOps none;
+  static const int e_over = env_choice("CSG_FFT_E", {16});
+  static const int c_over = env_choice("CSG_FFT_COLS", {4, 16});
   int rc;
   auto rows = [&](bool inv, float scale, const PixOps& p, const PixOps& e) -> int {
     const bool gen = p.n && p.kind[0] == OP_SOURCE;
     ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, pass_bytes * (gen ? 0.5 : 1.0));
-    if (inv) {
-      if ((rc = prep_smem(k_fft_rows<N, true>, RC::SMEM))) return rc;
-      k_fft_rows<N, true><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
-    } else {
-      if ((rc = prep_smem(k_fft_rows<N, false>, RC::SMEM))) return rc;
-      k_fft_rows<N, false><<<rgrid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
-    }
-    CSG_LAUNCH_CHECK();
-    return CSG_OK;
+    if constexpr (N == 1024)
+      if (e_over == 16) return launch_rows<N, 16>(st, field, F, inv, scale, tw, p, e, fi);
+    return launch_rows<N, default_e(N)>(st, field, F, inv, scale, tw, p, e, fi);
   };
   auto cols = [&](int mode) -> int {
     ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, pass_bytes);
     if constexpr (N == 1024) {
-      const int c = cols_override();
-      if (c == 4) return launch_cols<N, 4>(st, field, F, mode, tw, fa);
-      if (c == 16) return launch_cols<N, 16>(st, field, F, mode, tw, fa);
+      if (e_over == 16) return launch_cols<N, 16, 8>(st, field, F, mode, tw, fa);
+      if (c_over == 4) return launch_cols<N, 32, 4>(st, field, F, mode, tw, fa);
+      if (c_over == 16) return launch_cols<N, 32, 16>(st, field, F, mode, tw, fa);
     }
-    return launch_cols<N, default_cols(N)>(st, field, F, mode, tw, fa);
+    return launch_cols<N, default_e(N), default_cols(N)>(st, field, F, mode, tw, fa);
   };
   if (fa) {
     if ((rc = rows(false, 1.f, pro, none))) return rc;
