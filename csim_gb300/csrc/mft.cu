@@ -194,8 +194,8 @@ static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Par
 // [field][re/im][rows][cols]: the response-matrix objective's product.
 int launch_gemm_data_op_f32(int bn, const CUtensorMap& a, const CUtensorMap& b,
                             const tc::Params& p, int grid, cudaStream_t st) {
-  return bn == 256 ? launch_gemm<256, false, tc::EPI_F32>(a, b, p, grid, st)
-                   : launch_gemm<128, false, tc::EPI_F32>(a, b, p, grid, st);
+  return bn == 64 ? launch_gemm<64, false, tc::EPI_F32>(a, b, p, grid, st)
+                  : launch_gemm<128, false, tc::EPI_F32>(a, b, p, grid, st);
 }
 
 }  // namespace csg
@@ -211,13 +211,13 @@ struct csg_mft {
   Scratch tt;                     // [F][3][2][no][ny] bf16
   int bn = 0;                     // tile width chosen by the autotuner (0: default)
   int tuned_fields = 0;           // batch size the choice was measured at
-  float tuned_ms[2] = {0, 0};     // measured time of BN = 128, 256
+  float tuned_ms[2] = {0, 0};     // measured time of BN = 128, 64
 };
 
 namespace {
 std::string g_tune_log;
 
-// Tile autotuner: times the transform with N-tile widths 128 and 256 at the
+// Tile autotuner: times the transform with N-tile widths 128 and 64 at the
 // batch size it will run at (zero input, every field on slot 0) and keeps the
 // faster. Runs outside graph capture (csg_mft_reserve is called before).
 int autotune(csg_mft* m, int F) {
@@ -248,12 +248,12 @@ int autotune(csg_mft* m, int F) {
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  const int cand[2] = {128, 256};
+  const int cand[2] = {128, 64};
   float best = 1e30f;
   int best_bn = 0, rc = CSG_OK;
   const bool prof = m->ctx->prof;
   m->ctx->prof = false;
-  const int n_cand = m->no >= 256 ? 2 : 1;  // a 256-wide tile needs 256 output columns
+  const int n_cand = 2;
   for (int i = 0; i < n_cand && !rc; ++i) {
     m->bn = cand[i];
     rc = mft_execute_ops(m->ctx, m, in, out, F, slot, 0, nullptr, nullptr, PixOps(), FieldInfo());
@@ -281,7 +281,7 @@ int autotune(csg_mft* m, int F) {
   m->tuned_fields = F;
   char line[200];
   snprintf(line, sizeof(line), "%s{\"in\": [%d, %d], \"out\": [%d, %d], \"fields\": %d, "
-           "\"bn\": %d, \"ms_bn128\": %.4f, \"ms_bn256\": %.4f}",
+           "\"bn\": %d, \"ms_bn128\": %.4f, \"ms_bn64\": %.4f}",
            g_tune_log.empty() ? "" : ", ", m->ny, m->nx, m->mo, m->no, F, best_bn,
            m->tuned_ms[0], m->tuned_ms[1]);
   g_tune_log += line;
@@ -440,7 +440,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     CSG_LAUNCH_CHECK();
   }
 
-  const int bn1 = m->bn ? m->bn : (m->no >= 256 ? 256 : 128);
+  const int bn1 = m->bn ? m->bn : 128;
   // ---- stage 1: T^T = split(in . B_x^T)^T
   {
     CUtensorMap ta, tb;
@@ -465,8 +465,8 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     // algorithmic work: 8 flops per complex multiply-add of the contraction
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->ny * m->no * m->nx);
-    rc = bn1 == 256 ? launch_gemm<256, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
-                    : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
+    rc = bn1 == 64 ? launch_gemm<64, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
+                   : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
     if (rc) return rc;
   }
   // ---- stage 2: out = (pref A_y) . T
@@ -496,8 +496,8 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.status = ctx->status;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->mo * m->no * m->ny);
-    rc = bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st)
-                    : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st);
+    rc = bn1 == 64 ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st)
+                   : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st);
     if (rc) return rc;
   }
   return CSG_OK;

@@ -215,7 +215,7 @@ int csg_respobj_execute(csg_respobj* o, const double* x, int pop, double* out) {
   k_phase_operator<<<grid_for((long long)o->n_slot * pop * o->kpad, 256), 256, 0, st>>>(
       x, pop, o->ncol - 1, o->kpad, o->lam, o->n_slot, o->phase_sign, ps);
   CSG_LAUNCH_CHECK();
-  const int bn = pop > 128 ? 256 : 128;
+  const int bn = pop <= 64 ? 64 : 128;
   CUtensorMap ta, tb;
   if ((rc = make_map(&ta, o->msplit, o->kpad, o->npix, (long long)o->n_mat * 6, tc::BM))) return rc;
   if ((rc = make_map(&tb, ps, o->kpad, pop, (long long)o->n_slot * 9, bn))) return rc;

@@ -161,31 +161,58 @@ __device__ __forceinline__ int sel_plane(int d, int c) {
 }
 
 
-// Tensor-core fp32 accumulation truncates at every instruction, so a long
-// accumulation chain in tensor memory shrinks the result by ~2^-24 per
-// instruction. The kernel therefore never accumulates more than one K block
-// (BK = 64, four instructions) in tensor memory: each K block goes to a fresh
-// tensor-memory slot (NSLOT slots rotate through the 512 columns) and eight
-// drain warps add every finished slot into fp32 registers with
-// round-to-nearest adds while the next blocks are multiplied.
+// Accumulation and precision. Tensor-core fp32 accumulation truncates at
+// every instruction, so a long chain of the dominant product in tensor
+// memory would shrink the result by ~2^-24 per instruction. The products of
+// the three-way split are therefore grouped by magnitude (part indices
+// pa + pb): group 0 (hi x hi) goes to a fresh tensor-memory slot every K
+// block (two slots rotate) and eight drain warps add each finished slot into
+// fp32 registers with round-to-nearest adds while the next block is
+// multiplied; group 1 (hi x mid, mid x hi, 2^-8 of the result) and group 2
+// (the 2^-16 terms) accumulate over the whole K range in two persistent
+// slots, where the truncation is relative to their own small magnitude, and
+// are added once at the end.
+//
+// Operand traffic. A pipeline stage holds every split part of the A and B
+// tiles of one K block (3 + 3 tiles for bf16x6), and all the products of
+// that block are issued from it, so each part tile crosses L2 once per K
+// block (instead of once per product).
 constexpr int DRAIN_WARPS = 8;
 constexpr int THREADS = (DRAIN_WARPS + 2) * 32;  // + TMA producer warp + MMA warp
 constexpr int PRODUCER_WARP = DRAIN_WARPS;
 constexpr int MMA_WARP = DRAIN_WARPS + 1;
+constexpr int MAX_PARTS = 3;
 
 template <int BN>
 struct Cfg {
-  static constexpr int NSLOT = 512 / BN;           // tensor-memory slots
-  static constexpr int STAGES = BN == 256 ? 4 : 6; // shared-memory ring depth
+  static_assert(BN == 64 || BN == 128, "N tile must be 64 or 128");
   static constexpr uint32_t A_BYTES = BM * BK * 2;
   static constexpr uint32_t B_BYTES = BN * BK * 2;
-  static constexpr int COLS_PER_WARP = BN / 2;     // two warps share a lane quadrant
-  static constexpr size_t SMEM = (size_t)STAGES * (A_BYTES + B_BYTES) + 1024 + 512;
+  static constexpr uint32_t STAGE_BYTES = MAX_PARTS * (A_BYTES + B_BYTES);
+  static constexpr int STAGES = BN == 128 ? 2 : 3;  // 192 KB / 216 KB of operand ring
+  static constexpr int TMEM_COLS = 4 * BN;          // group 1, group 2, two rotating slots
+  static constexpr int COLS_PER_WARP = BN / 2;      // two warps share a lane quadrant
+  static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 512;
 };
 
 template <int BN>
 constexpr size_t smem_bytes() {
   return Cfg<BN>::SMEM;
+}
+
+// Drain one lane quadrant's CPW columns at taddr into acc (+=).
+template <int CPW>
+__device__ __forceinline__ void drain_add(uint32_t taddr, float* acc) {
+#pragma unroll
+  for (int cb = 0; cb < CPW; cb += 64) {
+    uint32_t r[64];
+    tmem_ld32_nowait(taddr + cb, r);
+    if (cb + 32 < CPW) tmem_ld32_nowait(taddr + cb + 32, r + 32);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 64; ++j)
+      if (cb + j < CPW) acc[cb + j] += __uint_as_float(r[j]);
+  }
 }
 
 // OP_IS_A = false: stage 1 (A = data rows y, B = operator rows u, d from N tile)
@@ -196,15 +223,13 @@ __global__ void __launch_bounds__(THREADS, 1)
                  const Params p) {
   using CF = Cfg<BN>;
   constexpr int STAGES = CF::STAGES;
-  constexpr int NSLOT = CF::NSLOT;
+  constexpr int NSLOT = 2;  // rotating group-0 slots
   constexpr int CPW = CF::COLS_PER_WARP;
   extern __shared__ uint8_t smem_raw[];
 
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
-  uint8_t* sA = sbase;
-  uint8_t* sB = sbase + STAGES * CF::A_BYTES;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + STAGES * CF::B_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sbase + STAGES * CF::STAGE_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* tfull = empty + STAGES;   // slot filled by the MMA warp
   uint64_t* tempty = tfull + NSLOT;   // slot drained by the drain warps
@@ -232,6 +257,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     row_a0 = (mt % p.m_half) * BM;
     row_b0 = nt * BN;
   }
+  int n_parts = 1;
+  for (int i = 0; i < p.n_terms; ++i)
+    n_parts = max(n_parts, 1 + max(p.term_a[i], p.term_b[i]));
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -248,15 +276,16 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(512));
+                 "r"(CF::TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  const uint32_t t_g1 = tmem, t_g2 = tmem + BN, t_rot = tmem + 2 * BN;
 
-  const int k_iters = p.n_terms * 2 * p.k_blocks;
+  const int k_iters = 2 * p.k_blocks;  // (data component c, K block)
 
   if (warp == PRODUCER_WARP) {
     if (lane == 0) {
@@ -270,20 +299,22 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         if (*abort_flag) break;
         const int kb = it % p.k_blocks;
-        const int c = (it / p.k_blocks) & 1;
-        const int term = it / (2 * p.k_blocks);
-        const int pa = p.term_a[term], pb = p.term_b[term];
-        int za, zb;
-        if (!OP_IS_A) {
-          za = (field * 3 + pa) * 2 + c;
-          zb = (slot * 3 + pb) * 3 + sel_plane(d, c);
-        } else {
-          za = (slot * 3 + pa) * 3 + sel_plane(d, c);
-          zb = (field * 3 + pb) * 2 + c;
+        const int c = it / p.k_blocks;
+        uint8_t* sA = sbase + stage * CF::STAGE_BYTES;
+        uint8_t* sB = sA + MAX_PARTS * CF::A_BYTES;
+        mbar_expect_tx(&full[stage], n_parts * (CF::A_BYTES + CF::B_BYTES));
+        for (int pp = 0; pp < n_parts; ++pp) {
+          int za, zb;
+          if (!OP_IS_A) {
+            za = (field * 3 + pp) * 2 + c;
+            zb = (slot * 3 + pp) * 3 + sel_plane(d, c);
+          } else {
+            za = (slot * 3 + pp) * 3 + sel_plane(d, c);
+            zb = (field * 3 + pp) * 2 + c;
+          }
+          tma_load_3d(sA + pp * CF::A_BYTES, &tmA, &full[stage], kb * BK, row_a0, za);
+          tma_load_3d(sB + pp * CF::B_BYTES, &tmB, &full[stage], kb * BK, row_b0, zb);
         }
-        mbar_expect_tx(&full[stage], CF::A_BYTES + CF::B_BYTES);
-        tma_load_3d(sA + stage * CF::A_BYTES, &tmA, &full[stage], kb * BK, row_a0, za);
-        tma_load_3d(sB + stage * CF::B_BYTES, &tmB, &full[stage], kb * BK, row_b0, zb);
         if (++stage == STAGES) {
           stage = 0;
           phase ^= 1;
@@ -296,6 +327,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       constexpr uint32_t idesc = instr_desc(BM, BN);
       int stage = 0;
       uint32_t phase = 0;
+      bool g1_on = false, g2_on = false;  // persistent groups hold data
       for (int it = 0; it < k_iters; ++it) {
         const int ts = it % NSLOT;
         const uint32_t round = (uint32_t)(it / NSLOT);
@@ -312,12 +344,22 @@ __global__ void __launch_bounds__(THREADS, 1)
           break;
         }
         tc_fence_after();
-        const uint32_t a0 = smem_u32(sA + stage * CF::A_BYTES);
-        const uint32_t b0 = smem_u32(sB + stage * CF::B_BYTES);
-        const uint32_t dcol = tmem + (uint32_t)(ts * BN);
+        const uint32_t a0 = smem_u32(sbase + stage * CF::STAGE_BYTES);
+        const uint32_t b0 = a0 + MAX_PARTS * CF::A_BYTES;
+        for (int i = 0; i < p.n_terms; ++i) {
+          const int pa = p.term_a[i], pb = p.term_b[i];
+          const int g = min(pa + pb, 2);
+          const uint32_t dcol = g == 0 ? t_rot + (uint32_t)(ts * BN) : (g == 1 ? t_g1 : t_g2);
+          bool on = g == 0 ? false : (g == 1 ? g1_on : g2_on);
+          const uint32_t aa = a0 + pa * CF::A_BYTES, bb = b0 + pb * CF::B_BYTES;
 #pragma unroll
-        for (int k = 0; k < BK / 16; ++k)
-          umma(dcol, smem_desc(a0 + k * 32), smem_desc(b0 + k * 32), idesc, k > 0 ? 1u : 0u);
+          for (int k = 0; k < BK / 16; ++k) {
+            umma(dcol, smem_desc(aa + k * 32), smem_desc(bb + k * 32), idesc, on ? 1u : 0u);
+            on = true;
+          }
+          if (g == 1) g1_on = true;
+          if (g == 2) g2_on = true;
+        }
         umma_commit(&empty[stage]);
         umma_commit(&tfull[ts]);
         if (++stage == STAGES) {
@@ -331,6 +373,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     // ---------------- drain warps: quadrant q of the 128 rows, half h of the columns
     const int q = warp & 3, h = warp >> 2;
     const int row = q * 32 + lane;
+    const uint32_t lane_off = ((uint32_t)(q * 32) << 16) + (uint32_t)(h * CPW);
     float acc[CPW];
 #pragma unroll
     for (int j = 0; j < CPW; ++j) acc[j] = 0.f;
@@ -342,22 +385,24 @@ __global__ void __launch_bounds__(THREADS, 1)
       ok = __all_sync(0xffffffffu, ok && !*abort_flag);
       if (!ok) break;
       tc_fence_after();
-      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(ts * BN + h * CPW);
-      // two loads in flight per wait
-#pragma unroll
-      for (int cb = 0; cb < CPW; cb += 64) {
-        uint32_t r[64];
-        tmem_ld32_nowait(taddr + cb, r);
-        tmem_ld32_nowait(taddr + cb + 32, r + 32);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 64; ++j) acc[cb + j] += __uint_as_float(r[j]);
-      }
+      drain_add<CPW>(t_rot + (uint32_t)(ts * BN) + lane_off, acc);
       tc_fence_before();
       __syncwarp();
       if (lane == 0)
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[ts]))
                      : "memory");
+    }
+    if (ok) {
+      // the last commit covered every product: add the persistent groups
+      // (smaller first: g2 into g1, then into the accumulator)
+      tc_fence_after();
+      float gsum[CPW];
+#pragma unroll
+      for (int j = 0; j < CPW; ++j) gsum[j] = 0.f;
+      drain_add<CPW>(t_g2 + lane_off, gsum);
+      drain_add<CPW>(t_g1 + lane_off, gsum);
+#pragma unroll
+      for (int j = 0; j < CPW; ++j) acc[j] += gsum[j];
     }
     if (!ok) {
       atomicExch(p.status, 3);
@@ -418,7 +463,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(CF::TMEM_COLS));
   }
 }
 
