@@ -233,7 +233,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint64_t* empty = full + STAGES;
   uint64_t* tfull = empty + STAGES;   // slot filled by the MMA warp
   uint64_t* tempty = tfull + NSLOT;   // slot drained by the drain warps
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + NSLOT);
+  uint64_t* quiesce = tempty + NSLOT;  // abort path: in-flight products done
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(quiesce + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
@@ -270,6 +271,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&tfull[s], 1);
       mbar_init(&tempty[s], DRAIN_WARPS);
     }
+    mbar_init(quiesce, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -337,7 +339,11 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (!ok || *abort_flag) {
           atomicExch(p.status, 2);
           *abort_flag = 1;
-          // release every drain wait so nobody waits for the full budget again
+          // let the products already issued finish before tensor memory is
+          // released (bounded wait), then release every drain wait so nobody
+          // waits for the full budget again
+          umma_commit(quiesce);
+          mbar_wait(quiesce, 0);
           for (int s = 0; s < NSLOT; ++s)
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tfull[s]))
                          : "memory");
