@@ -75,6 +75,7 @@ SIGNATURES = {
     "csg_chain_add_complex_mask": ([P, P, P, I, I, I], None),
     "csg_chain_add_fpm_hex": ([P, P, P, I, I, I, D, D, D, D, D, D, I], None),
     "csg_chain_add_fraunhofer": ([P, I, D, D], None),
+    "csg_chain_add_fft_fpm": ([P, I, P, P, I], None),
     "csg_chain_set_support_crop": ([P, I], None),
     "csg_chain_fpm_region": ([P, I, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)], None),
     "csg_chain_set_batch": ([P, I, P, P, P, P, P], None),

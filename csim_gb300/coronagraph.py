@@ -73,6 +73,17 @@ class FpmPupToLyotHex:
 
 
 @dataclass
+class PaddedFftFpm:
+    """Plain Lyot occulter: embed the N x N field in a zeroed pad x pad grid,
+    FFT, multiply by the focal-plane mask (centred focal coordinates, one
+    [pad][pad] array per wavelength or one for all), inverse FFT, crop
+    (the fpmPupToLyot embedding pattern with an FFT-sampled mask, no Babinet)."""
+    pad: int
+    mask: np.ndarray
+    disableForCalibration: bool = True
+
+
+@dataclass
 class FraunhoferFocal:
     """fraunhoferFocal (fraunhoferFocal.cpp:65-72): ceil(FOV spl)^2 pixels at
     loD(referenceLambda) / spl."""
@@ -131,6 +142,17 @@ class Coronagraph:
                  e.focalRatio, self.ef.beamRadiusPhysical, e.fRatioSign, e.zoomFftSign,
                  e.phaseSign, int(e.disableForCalibration))
             self.n_hex = e.n_hex
+        elif isinstance(e, PaddedFftFpm):
+            L = len(self.ef.wavelengths)
+            m = np.asarray(e.mask)
+            if m.ndim == 2:
+                m = np.broadcast_to(m, (L,) + m.shape)
+            assert m.shape == (L, e.pad, e.pad), "mask must be [n_lambda][pad][pad]"
+            re = _f32(m.real)
+            im = _f32(m.imag) if np.iscomplexobj(m) else None
+            call("csg_chain_add_fft_fpm", self.h, e.pad, re.ctypes.data_as(C.c_void_p),
+                 im.ctypes.data_as(C.c_void_p) if im is not None else None,
+                 int(e.disableForCalibration))
         elif isinstance(e, FraunhoferFocal):
             self.n_out = e.n_out()
             self.out_pixel = self.tel.compute_loD(e.referenceLambda) / e.samplesPerflD

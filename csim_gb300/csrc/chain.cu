@@ -38,7 +38,7 @@ int hex_mask_with_phasor_buffer(csg_ctx* ctx, const int16_t* hex_id, const uint1
                                 const int* cand, const double* lambda, double phase_sign, int flip,
                                 double subtract, int use_only_hex, float* out, float2* phasors);
 
-enum ElemKind { E_MASK, E_MIRROR, E_FRESNEL, E_CMASK, E_FPM_HEX, E_FRAUNHOFER };
+enum ElemKind { E_MASK, E_MIRROR, E_FRESNEL, E_CMASK, E_FPM_HEX, E_FRAUNHOFER, E_FFT_FPM };
 
 template <typename T>
 static T* dev_copy(const T* h, size_t n, cudaStream_t st) {
@@ -81,6 +81,8 @@ struct Elem {
   // fraunhofer
   csg_mft* mft = nullptr;
   int n_out = 0;
+  // padded-FFT focal-plane mask: P x P grid
+  int P = 0;
   // per-wavelength tables (mirror phasors, Fresnel transfer function)
   float2* tab = nullptr;
   // real mask: bounding box [sr0, sr1) x [sc0, sc1) of its nonzero pixels
@@ -122,9 +124,10 @@ struct csg_chain {
   float* fpm_mask = nullptr;    // [F][2][S][S]
   float2* phasors = nullptr;    // [F][n_hex+1]
   float* image = nullptr;       // [F][2][n_out][n_out]
+  float* padbuf = nullptr;      // [F][2][P][P] (padded-FFT focal-plane masks)
   double* sags = nullptr;       // [n_cand][n_hex]
   int n_cand = 0, sag_hex = 0;
-  size_t fpm_cap = 0, img_cap = 0, ph_cap = 0;
+  size_t fpm_cap = 0, img_cap = 0, ph_cap = 0, pad_cap = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_calib = -1;
@@ -197,7 +200,8 @@ int csg_chain_destroy(csg_chain* c) {
   }
   for (void* p : {(void*)c->slot, (void*)c->lam_f, (void*)c->amp, (void*)c->tip, (void*)c->tilt,
                   (void*)c->cand, (void*)c->ident, (void*)c->field, (void*)c->fpm,
-                  (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->sags, (void*)c->lam_slots})
+                  (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->sags,
+                  (void*)c->lam_slots, (void*)c->padbuf})
     cudaFree(p);
   delete c;
   return CSG_OK;
@@ -378,6 +382,44 @@ int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* c
   e.lf = lf;
   e.pref = pref2;
   e.dm = dm;
+  c->elems.push_back(e);
+  c->planned = false;
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// Padded-FFT focal-plane mask (the plain Lyot coronagraph's occulter): the
+// n x n field is embedded at the centre of a zeroed pad x pad grid (as
+// fpmPupToLyot.cpp:112-118 does for pad = 2n), transformed by a pad^2 FFT,
+// multiplied by the focal-plane mask, transformed back (ifft / pad^2) and
+// cropped to its centre. mask_re / mask_im: host [n_lambda][pad][pad] in
+// centred focal coordinates (row pad/2, column pad/2 is zero frequency);
+// mask_im may be null for a real mask. Stored in FFT order, one table per
+// wavelength, and applied between the column transforms (the same three
+// passes as a Fresnel propagation).
+int csg_chain_add_fft_fpm(csg_chain* c, int pad, const float* mask_re, const float* mask_im,
+                          int disable_for_calibration) {
+  CSG_CHECK(c && mask_re, CSG_E_ARG, "csg_chain_add_fft_fpm: null argument");
+  CSG_CHECK(pad >= c->n && pad <= 4096 && (pad & (pad - 1)) == 0, CSG_E_SHAPE,
+            "csg_chain_add_fft_fpm: pad must be a power of two in [n, 4096]");
+  DeviceGuard g(c->ctx->device);
+  Elem e;
+  e.kind = E_FFT_FPM;
+  e.P = pad;
+  e.disable_for_calibration = disable_for_calibration;
+  const size_t plane = (size_t)pad * pad;
+  std::vector<float2> h(plane * c->n_lambda);
+  const int half = pad / 2;
+  for (int l = 0; l < c->n_lambda; ++l)
+    for (int r = 0; r < pad; ++r)
+      for (int cc = 0; cc < pad; ++cc) {
+        const size_t src = l * plane + (size_t)r * pad + cc;
+        const size_t dst = l * plane + (size_t)((r + half) % pad) * pad + (cc + half) % pad;
+        h[dst] = make_float2(mask_re[src], mask_im ? mask_im[src] : 0.f);
+      }
+  e.tab = dev_copy(h.data(), h.size(), c->ctx->stream);
+  CSG_CHECK(e.tab, CSG_E_NOMEM, "csg_chain_add_fft_fpm: allocation failed");
+  CSG_CUDA(cudaStreamSynchronize(c->ctx->stream));  // the host staging buffer goes away
   c->elems.push_back(e);
   c->planned = false;
   drop_graph(c);
@@ -583,7 +625,7 @@ static int prepare(csg_chain* c) {
   int prc = build_plans(c);
   if (prc) return prc;
   const size_t F = (size_t)c->n_fields;
-  size_t fpm_need = 0, ph_need = 0, img_need = 0;
+  size_t fpm_need = 0, ph_need = 0, img_need = 0, pad_need = 0;
   for (auto& e : c->elems) {
     if (e.kind == E_FPM_HEX) {
       fpm_need = std::max(fpm_need, F * 2 * e.RR * e.CC * sizeof(float));
@@ -591,6 +633,8 @@ static int prepare(csg_chain* c) {
       int rc = csg_mft_reserve(e.mft1, c->n_fields);
       if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
       if (rc) return rc;
+    } else if (e.kind == E_FFT_FPM) {
+      pad_need = std::max(pad_need, F * 2 * (size_t)e.P * e.P * sizeof(float));
     } else if (e.kind == E_FRAUNHOFER) {
       img_need = std::max(img_need, F * 2 * e.n_out * e.n_out * sizeof(float));
       int rc = csg_mft_reserve(e.mft, c->n_fields);
@@ -602,6 +646,7 @@ static int prepare(csg_chain* c) {
   if (!rc) rc = ensure_buf(&c->fpm_mask, mask_cap, fpm_need);
   if (!rc) rc = ensure_buf(reinterpret_cast<float**>(&c->phasors), c->ph_cap, ph_need);
   if (!rc) rc = ensure_buf(&c->image, c->img_cap, img_need);
+  if (!rc) rc = ensure_buf(&c->padbuf, c->pad_cap, pad_need);
   return rc;
 }
 
@@ -611,7 +656,7 @@ static int prepare(csg_chain* c) {
 // ops right after it in its last row pass, ops before the final MFT in its
 // operand split; only ops with no such neighbour get one standalone pass.
 struct Step {
-  enum Kind { PIX, FRESNEL, FPM, FINAL } kind;
+  enum Kind { PIX, FRESNEL, FPM, FINAL, FFT_FPM } kind;
   PixOps pro, epi;
   const Elem* e = nullptr;
 };
@@ -667,6 +712,10 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
       pend = PixOps();
       prog.push_back(Step{Step::FPM, PixOps(), PixOps(), &e});
       epi_open = false;
+    } else if (e.kind == E_FFT_FPM) {
+      prog.push_back(Step{Step::FFT_FPM, pend, PixOps(), &e});  // ops ride in the padding pass
+      pend = PixOps();
+      epi_open = false;
     } else if (e.kind == E_FRAUNHOFER) {
       prog.push_back(Step{Step::FINAL, pend, PixOps(), &e});
       pend = PixOps();
@@ -716,6 +765,14 @@ static int run_walk(csg_chain* c, int calibrating) {
         rc = mft_execute_ops(ctx, s.e->mft, c->field, c->image, F, c->slot, 0, nullptr, nullptr,
                              s.pro, fi, &s.e->win, nullptr);
         break;
+      case Step::FFT_FPM: {
+        const Elem& e = *s.e;
+        rc = pad_center_pass(ctx->stream, c->field, c->padbuf, F, n, e.P, s.pro, fi);
+        FresnelArgs fa{c->lam_f, 0.0, 1.0, e.tab, c->slot};  // H = the mask table
+        if (!rc) rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi);
+        if (!rc) rc = crop_center_pass(ctx->stream, c->padbuf, c->field, F, n, e.P);
+        break;
+      }
     }
     if (rc) return rc;
   }

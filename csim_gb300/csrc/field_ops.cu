@@ -67,6 +67,85 @@ int build_phasor_table(cudaStream_t st, const float* sag, int R, int C, const do
   return CSG_OK;
 }
 
+// Zero-padded embedding: out [F][2][P][P] = 0 except the centred n x n block
+// at offset o = (P - n) / 2, which holds ops(in) (the ops see the n x n
+// field's own coordinates). fpmPupToLyot.cpp:112-118 embeds at [N/2, 3N/2)
+// the same way for P = 2N. Four pixels per thread (n, P multiples of 4).
+__global__ void k_pad_center(const float* __restrict__ in, float* __restrict__ out, int n,
+                             int lp, PixOps ops, FieldInfo fi) {
+  const int f = blockIdx.y;
+  const int P = 1 << lp, o = (P - n) / 2;
+  const size_t pplane = (size_t)P * P, nplane = (size_t)n * n;
+  PixConsts k;
+  if (ops.n) pix_consts(ops, fi, f, n, n, k);
+  const bool gen = ops.n && ops.kind[0] == OP_SOURCE;
+  const float* ire = in + (size_t)f * 2 * nplane;
+  const float* iim = ire + nplane;
+  float* ore = out + (size_t)f * 2 * pplane;
+  float* oim = ore + pplane;
+  const long long nv = (long long)pplane / 4;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)((4 * v) >> lp), c = (int)((4 * v) & (P - 1));
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    const int rr = r - o, cc = c - o;
+    if (rr >= 0 && rr < n && cc >= 0 && cc < n) {
+      if (!gen) {
+        a = *reinterpret_cast<const float4*>(ire + (size_t)rr * n + cc);
+        b = *reinterpret_cast<const float4*>(iim + (size_t)rr * n + cc);
+      }
+      if (ops.n) {
+        float xr[4] = {a.x, a.y, a.z, a.w}, xi[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pix_apply(ops, k, rr, cc + q, n, n, xr[q], xi[q]);
+        a = make_float4(xr[0], xr[1], xr[2], xr[3]);
+        b = make_float4(xi[0], xi[1], xi[2], xi[3]);
+      }
+    }
+    reinterpret_cast<float4*>(ore)[v] = a;
+    reinterpret_cast<float4*>(oim)[v] = b;
+  }
+}
+
+// The centred n x n block of P x P fields (fpmPupToLyot.cpp:154-157).
+__global__ void k_crop_center(const float* __restrict__ in, float* __restrict__ out, int n,
+                              int P) {
+  const int f = blockIdx.y;
+  const int o = (P - n) / 2;
+  const size_t pplane = (size_t)P * P, nplane = (size_t)n * n;
+  const long long nv = (long long)nplane / 4 * 2;  // both planes
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int d = (int)(v / (nplane / 4));
+    const long long e0 = 4 * (v % (long long)(nplane / 4));
+    const int r = (int)(e0 / n), c = (int)(e0 % n);
+    const float4 x = *reinterpret_cast<const float4*>(in + ((size_t)f * 2 + d) * pplane +
+                                                      (size_t)(r + o) * P + c + o);
+    *reinterpret_cast<float4*>(out + ((size_t)f * 2 + d) * nplane + e0) = x;
+  }
+}
+
+int pad_center_pass(cudaStream_t st, const float* in, float* out, int F, int n, int P,
+                    const PixOps& ops, const FieldInfo& fi) {
+  CSG_CHECK(F > 0 && F < 65536 && n % 4 == 0 && P >= n && (P & (P - 1)) == 0 && (P - n) % 8 == 0,
+            CSG_E_SHAPE, "pad: bad shape");
+  int lp = 0;
+  while ((1 << lp) < P) ++lp;
+  dim3 grid(grid_for((long long)P * P / 4, 256, 2048), F);
+  k_pad_center<<<grid, 256, 0, st>>>(in, out, n, lp, ops, fi);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
+int crop_center_pass(cudaStream_t st, const float* in, float* out, int F, int n, int P) {
+  CSG_CHECK(F > 0 && F < 65536 && n % 4 == 0 && P >= n && (P - n) % 8 == 0, CSG_E_SHAPE,
+            "crop: bad shape");
+  dim3 grid(grid_for((long long)n * n / 2, 256, 1024), F);
+  k_crop_center<<<grid, 256, 0, st>>>(in, out, n, P);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
 int pixops_pass(cudaStream_t st, float* field, int F, int R, int C, const PixOps& ops,
                 const FieldInfo& fi) {
   if (!ops.n) return CSG_OK;

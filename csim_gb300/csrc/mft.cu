@@ -390,11 +390,11 @@ int csg_mft_reserve(csg_mft* m, int n_fields) {
 
 // Tile width the autotuner chose for the last reserved batch size and the
 // times it measured (ms per transform for widths 128 and 256).
-int csg_mft_tuning(csg_mft* m, int* bn, float* ms128, float* ms256) {
+int csg_mft_tuning(csg_mft* m, int* bn, float* ms128, float* ms64) {
   CSG_CHECK(m && bn, CSG_E_ARG, "csg_mft_tuning: null argument");
   *bn = m->bn;
   if (ms128) *ms128 = m->tuned_ms[0];
-  if (ms256) *ms256 = m->tuned_ms[1];
+  if (ms64) *ms64 = m->tuned_ms[1];
   return CSG_OK;
 }
 

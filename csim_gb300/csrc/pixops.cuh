@@ -238,6 +238,12 @@ __device__ __forceinline__ void pix_apply(const PixOps& ops, const PixConsts& k,
 int pixops_pass(cudaStream_t st, float* field, int F, int R, int C, const PixOps& ops,
                 const FieldInfo& fi);
 
+// out [F][2][P][P] <- n x n fields ops(in) embedded at the centre of zeros;
+// crop: out [F][2][n][n] <- the centred n x n block of P x P fields.
+int pad_center_pass(cudaStream_t st, const float* in, float* out, int F, int n, int P,
+                    const PixOps& ops, const FieldInfo& fi);
+int crop_center_pass(cudaStream_t st, const float* in, float* out, int F, int n, int P);
+
 struct FresnelArgs {
   const double* lambda;           // per field
   double z;

@@ -151,3 +151,88 @@ def piaacmc_arrays(spec: PiaacmcSpec, sources=None) -> dict:
                 lod_image=tel.compute_loD(lam_ref))
 
 
+
+
+# ------------------------------------------------------------ plain Lyot
+def noll_nm(j: int):
+    """Noll index j >= 1 -> radial order n and azimuthal m (m > 0: cos,
+    m < 0: sin, even j carries cos)."""
+    n = 0
+    while (n + 1) * (n + 2) // 2 < j:
+        n += 1
+    k = j - n * (n + 1) // 2 - 1
+    m = 2 * ((k + 1) // 2) if n % 2 == 0 else 2 * (k // 2) + 1
+    return n, (m if (j % 2 == 0 or m == 0) else -m)
+
+
+def zernike(j: int, rho: np.ndarray, theta: np.ndarray) -> np.ndarray:
+    """Orthonormal (over the unit disk) Zernike polynomial of Noll index j."""
+    n, m = noll_nm(j)
+    am = abs(m)
+    rad = np.zeros_like(rho)
+    for s in range((n - am) // 2 + 1):
+        c = ((-1) ** s * math.factorial(n - s)
+             / (math.factorial(s) * math.factorial((n + am) // 2 - s)
+                * math.factorial((n - am) // 2 - s)))
+        rad = rad + c * rho ** (n - 2 * s)
+    if m == 0:
+        return math.sqrt(n + 1) * rad
+    ang = np.cos(am * theta) if m > 0 else np.sin(am * theta)
+    return math.sqrt(2 * (n + 1)) * rad * ang
+
+
+@dataclass
+class PlainLyotSpec:
+    """Plain Lyot coronagraph: 512^2 pupil, circular aperture of radius 200 px
+    with a 0.3 central obstruction, Zernike 4-15 aberration (N(0,1)
+    coefficients, seeded) scaled to 10 nm RMS wavefront, zero-padded 2048^2
+    FFT to the focal plane, opaque occulting disk of radius 3 lambda/D,
+    inverse FFT, Lyot stop at 0.9 of the pupil radius, final 128^2 MFT at
+    0.25 lambda/D (+-16 lambda/D)."""
+    n: int = 512
+    pad: int = 2048
+    radius_px: float = 200.0
+    obstruction: float = 0.3
+    beam_radius: float = 0.01
+    wavelengths: tuple = (550e-9,)
+    f_ratio: float = 15.0
+    diameter: float = 2.4
+    zernike_modes: tuple = tuple(range(4, 16))
+    wfe_rms: float = 10e-9
+    occulter_lod: float = 3.0
+    lyot: float = 0.9
+    n_out_fov: float = 32.0
+    spl: float = 4.0
+    seed: int = 5
+
+
+def plain_lyot_arrays(spec: PlainLyotSpec, sources=None) -> dict:
+    """Seeded host-side inputs of the plain Lyot chain: pupil, aberration
+    (as a mirror sag: half the wavefront), FFT-sampled occulter per
+    wavelength, Lyot stop, telescope and efield."""
+    rng = np.random.default_rng(spec.seed)
+    dx = spec.beam_radius / spec.radius_px
+    lam = np.asarray(spec.wavelengths, dtype=np.float64)
+    tel = Telescope(spec.diameter, spec.f_ratio)
+    ef = EField(spec.n, spec.beam_radius, dx, lam, sources or [PointSource()])
+    pupil = circle_mask(spec.n, spec.radius_px, spec.obstruction)
+    c = (spec.n - 1) / 2.0
+    yy, xx = np.mgrid[:spec.n, :spec.n]
+    rho = np.hypot(xx - c, yy - c) / spec.radius_px
+    theta = np.arctan2(yy - c, xx - c)
+    coef = rng.standard_normal(len(spec.zernike_modes))
+    w = sum(a * zernike(j, rho, theta) for a, j in zip(coef, spec.zernike_modes))
+    inside = pupil > 0
+    w = w - w[inside].mean()
+    w *= spec.wfe_rms / np.sqrt(np.mean(w[inside] ** 2))
+    w[~inside] = 0.0
+    # FFT focal sampling: 2 R / pad lambda/D per pixel at every wavelength;
+    # the occulter has a fixed size in lambda_ref / D
+    lam_ref = float(lam.mean())
+    P = spec.pad
+    fy, fx = np.mgrid[:P, :P]
+    fr = np.hypot(fx - P // 2, fy - P // 2) * (2 * spec.radius_px / P)  # lambda/D
+    occ = np.stack([(fr > spec.occulter_lod * lam_ref / l).astype(np.float32) for l in lam])
+    return dict(pupil=pupil, sag=(0.5 * w).astype(np.float32), occulter=occ,
+                lyot=circle_mask(spec.n, spec.lyot * spec.radius_px), dx=dx, lam=lam, tel=tel,
+                ef=ef, lam_ref=lam_ref, lod_image=tel.compute_loD(lam_ref))

@@ -16,8 +16,8 @@ import numpy as np
 import torch
 
 from . import coronagraph as cg
-from .synth import (PiaacmcSpec, circle_mask, hex_layout_standard,  # noqa: F401
-                    piaa_sag, piaacmc_arrays)
+from .synth import (PiaacmcSpec, PlainLyotSpec, circle_mask,  # noqa: F401
+                    hex_layout_standard, piaa_sag, piaacmc_arrays, plain_lyot_arrays)
 from ._lib import call
 from .runtime import Context, dvec, ptr
 
@@ -55,6 +55,21 @@ def build_piaacmc(ctx: Context, spec: PiaacmcSpec, sources=None, precision: int 
         cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov),
     ]
     cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision, support_crop)
+    return cor, a
+
+
+def build_plain_lyot(ctx: Context, spec: PlainLyotSpec, sources=None, precision: int = 6):
+    """Plain Lyot coronagraph chain: pupil -> aberration -> padded-FFT
+    occulter -> Lyot stop -> final MFT. Returns (coronagraph, inputs)."""
+    a = plain_lyot_arrays(spec, sources)
+    elems = [
+        cg.Mask(a["pupil"]),
+        cg.Mirror(a["sag"], 1.0),
+        cg.PaddedFftFpm(spec.pad, a["occulter"]),
+        cg.Mask(a["lyot"]),
+        cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov),
+    ]
+    cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision)
     return cor, a
 
 

@@ -252,6 +252,13 @@ int csg_chain_add_fpm_hex(csg_chain* chain, const int16_t* hex_id, const uint16_
 int csg_chain_set_support_crop(csg_chain* chain, int enable);
 /* The box [r0, r0 + rows) x [c0, c0 + cols) of the idx-th hex FPM element. */
 int csg_chain_fpm_region(csg_chain* chain, int idx, int* r0, int* c0, int* rows, int* cols);
+/* Padded-FFT focal-plane mask, the plain Lyot coronagraph's occulter (the
+ * fpmPupToLyot pattern of fpmPupToLyot.cpp:112-161 with an FFT-sampled mask,
+ * without Babinet): E <- crop_n(ifft_pad(mask_lambda . fft_pad(embed_pad(E)))).
+ * mask_re / mask_im (may be null): host fp32 [n_lambda][pad][pad] in centred
+ * focal coordinates (index pad/2 is zero frequency); pad a power of two >= N. */
+int csg_chain_add_fft_fpm(csg_chain* chain, int pad, const float* mask_re, const float* mask_im,
+                          int disable_for_calibration);
 /* fraunhoferFocal (fraunhoferFocal.cpp:23-72): zoomFft to n_out x n_out at
  * out_pixel (= loD / samplesPerflD), lambda f = lambda lf_scale with
  * lf_scale = 2 beamRadius primaryfRatio. Must be the last element. */
@@ -273,12 +280,12 @@ int csg_chain_execute(csg_chain* chain, int calibrating, int use_graph);
 int csg_chain_image(csg_chain* chain, float** dev_image, int* n_out);
 int csg_chain_field(csg_chain* chain, float** dev_field);
 /* Pre-size an MFT plan's scratch for n_fields (so graph capture allocates
- * nothing) and autotune its tensor-core tile width (128 or 256 output
+ * nothing) and autotune its tensor-core tile width (128 or 64 output
  * columns per tile) by timing both at that batch size. Set the environment
- * variable CSG_MFT_AUTOTUNE=0 to keep the default width. */
+ * variable CSG_MFT_AUTOTUNE=0 to keep the default width (128). */
 int csg_mft_reserve(csg_mft* plan, int n_fields);
 /* The chosen tile width and the measured ms per transform of each width. */
-int csg_mft_tuning(csg_mft* plan, int* bn, float* ms128, float* ms256);
+int csg_mft_tuning(csg_mft* plan, int* bn, float* ms128, float* ms64);
 /* Every autotuning decision of the process as a JSON list. */
 int csg_mft_tuning_log(char* buf, size_t len);
 

@@ -58,3 +58,24 @@ def piaacmc_field(inp: dict, spec, lam: float, amp: float, tip: float, tilt: flo
     gout = of.ArrayGeom.set_xy(n_out, n_out, inp["lod_image"] / spec.spl)
     return oe.fraunhofer_focal(e, geom, gout, [lam], ef.beamRadiusPhysical, tel.primaryfRatio,
                                use_czt=czt)[0]
+
+
+def plain_lyot_field(inp: dict, spec, lam_idx: int, amp: float, tip: float, tilt: float,
+                     calibrating: bool = False, czt: bool = False):
+    """One field of the plain Lyot coronagraph: point source -> pupil mask ->
+    aberration (mirror) -> padded-FFT occulter -> Lyot mask ->
+    fraunhoferFocal. Returns the final image field [n_out][n_out]."""
+    ef, tel = inp["ef"], inp["tel"]
+    lam = float(inp["lam"][lam_idx])
+    n, dx = ef.n, inp["dx"]
+    geom = of.ArrayGeom.set_xy(n, n, dx)
+    e = oe.point_source_field(geom, 1, amp * amp, tip, tilt)
+    e = oe.mask_apply(e, inp["pupil"])
+    e = oe.mirror_apply(e, inp["sag"].astype(np.float64), [lam], 1.0)
+    if not calibrating:
+        e = oe.padded_fft_fpm(e, spec.pad, inp["occulter"][lam_idx:lam_idx + 1].astype(np.float64))
+    e = oe.mask_apply(e, inp["lyot"])
+    n_out = int(np.ceil(spec.n_out_fov * spec.spl))
+    gout = of.ArrayGeom.set_xy(n_out, n_out, inp["lod_image"] / spec.spl)
+    return oe.fraunhofer_focal(e, geom, gout, [lam], ef.beamRadiusPhysical, tel.primaryfRatio,
+                               use_czt=czt)[0]

@@ -270,6 +270,23 @@ def pup_to_lyot_mft(cube, lambdas, egeom: ArrayGeom, mask_geom: ArrayGeom, mask_
     return out
 
 
+def padded_fft_fpm(cube, pad: int, masks):
+    """Plain Lyot occulter with an FFT-sampled mask: per slice embed E at the
+    centre of a zeroed pad x pad array (the embedding of
+    fpmPupToLyot.cpp:112-118), FFT, multiply by the mask given in centred
+    focal coordinates (masks[sl], index pad // 2 = zero frequency), inverse
+    FFT (/ pad^2) and crop the centre (:154-157)."""
+    n = cube.shape[-1]
+    o = (pad - n) // 2
+    out = np.empty_like(cube)
+    for sl in range(cube.shape[0]):
+        p = np.zeros((pad, pad), dtype=np.complex128)
+        p[o:o + n, o:o + n] = cube[sl]
+        r = ifft2(fft2(p) * np.fft.ifftshift(masks[sl]))
+        out[sl] = r[o:o + n, o:o + n]
+    return out
+
+
 # ------------------------------------------------------- region contrast --
 def region_pixels(geom: ArrayGeom, loD: float, radius1, radius2, angle1=-180.0, angle2=180.0,
                   xlim1=-1e300, xlim2=1e300) -> np.ndarray:

@@ -87,3 +87,25 @@ def test_mask_quirk_and_mirror():
     s = np.full((4, 4), 1e-7)
     out = oe.mirror_apply(e, s, [6.5e-7], 1.0)
     assert np.allclose(out, np.exp(-4j * math.pi * 1e-7 / 6.5e-7))
+
+
+def test_padded_fft_fpm_is_centred_convolution():
+    """The plain-Lyot occulter restatement: a mask of ones is the identity,
+    and a general mask equals the circular convolution of the padded field
+    with the inverse FFT of the (ifftshifted) mask, cropped."""
+    rng = np.random.default_rng(3)
+    n, pad = 16, 64
+    e = rng.standard_normal((1, n, n)) + 1j * rng.standard_normal((1, n, n))
+    assert np.allclose(oe.padded_fft_fpm(e, pad, np.ones((1, pad, pad))), e, atol=1e-13)
+    m = rng.uniform(0, 1, (1, pad, pad))
+    got = oe.padded_fft_fpm(e, pad, m)
+    k = np.fft.ifft2(np.fft.ifftshift(m[0]))
+    p = np.zeros((pad, pad), complex)
+    o = (pad - n) // 2
+    p[o:o + n, o:o + n] = e[0]
+    conv = np.zeros((pad, pad), complex)
+    for dy in range(pad):
+        for dx in range(pad):
+            if k[dy, dx] != 0:
+                conv += k[dy, dx] * np.roll(np.roll(p, dy, 0), dx, 1)
+    assert np.allclose(got[0], conv[o:o + n, o:o + n], atol=1e-12)
