@@ -76,6 +76,11 @@ SIGNATURES = {
     "csg_chain_add_fpm_hex": ([P, P, P, I, I, I, D, D, D, D, D, D, I], None),
     "csg_chain_add_fraunhofer": ([P, I, D, D], None),
     "csg_chain_add_fft_fpm": ([P, I, P, P, I], None),
+    "csg_chain_add_fraunhofer_ragged": ([P, P, D, D], None),
+    "csg_mft_create_ragged": ([P, C.POINTER(P), I, I, I, P, P, P, P, P, I, P, P, D, I], None),
+    "csg_dm_create": ([P, C.POINTER(P), I, I, D], None),
+    "csg_dm_destroy": ([P], None),
+    "csg_dm_surface": ([P, P, P], None),
     "csg_chain_set_support_crop": ([P, I], None),
     "csg_chain_fpm_region": ([P, I, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)], None),
     "csg_chain_set_batch": ([P, I, P, P, P, P, P], None),

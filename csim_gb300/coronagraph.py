@@ -84,6 +84,25 @@ class PaddedFftFpm:
 
 
 @dataclass
+class DeformableMirror:
+    """deformableMirror (deformableMirror.cpp): actuator strokes [nA][nA]
+    (metres), Gaussian influence width sigma (actuator pitches); the surface
+    is computed on the GPU (csg_dm_surface) and applied like a mirror."""
+    actuators: np.ndarray
+    sigma: float = 1.0
+    mirrorSign: float = 1.0
+
+
+@dataclass
+class FraunhoferFocalRagged:
+    """fraunhoferFocal with a per-wavelength image size at one pixel scale
+    (loD(referenceLambda) / samplesPerflD): a ragged batch in one launch."""
+    referenceLambda: float
+    samplesPerflD: float
+    n_out: list
+
+
+@dataclass
 class FraunhoferFocal:
     """fraunhoferFocal (fraunhoferFocal.cpp:65-72): ceil(FOV spl)^2 pixels at
     loD(referenceLambda) / spl."""
@@ -153,6 +172,19 @@ class Coronagraph:
             call("csg_chain_add_fft_fpm", self.h, e.pad, re.ctypes.data_as(C.c_void_p),
                  im.ctypes.data_as(C.c_void_p) if im is not None else None,
                  int(e.disableForCalibration))
+        elif isinstance(e, DeformableMirror):
+            surf = dm_surface(self.ctx, np.asarray(e.actuators, np.float64), self.ef.n, e.sigma)
+            self.dm_surface = surf
+            s = _f32(surf)
+            call("csg_chain_add_mirror", self.h, s.ctypes.data_as(C.c_void_p), e.mirrorSign)
+        elif isinstance(e, FraunhoferFocalRagged):
+            sizes = np.ascontiguousarray(e.n_out, np.int32)
+            assert sizes.size == len(self.ef.wavelengths)
+            self.n_out = int(sizes.max())
+            self.n_out_l = sizes
+            self.out_pixel = self.tel.compute_loD(e.referenceLambda) / e.samplesPerflD
+            call("csg_chain_add_fraunhofer_ragged", self.h, sizes.ctypes.data_as(C.c_void_p),
+                 self.out_pixel, 2 * self.ef.beamRadiusPhysical * self.tel.primaryfRatio)
         elif isinstance(e, FraunhoferFocal):
             self.n_out = e.n_out()
             self.out_pixel = self.tel.compute_loD(e.referenceLambda) / e.samplesPerflD
@@ -215,6 +247,20 @@ class Coronagraph:
             self.close()
         except Exception:
             pass
+
+
+def dm_surface(ctx: Context, act: np.ndarray, n: int, sigma: float) -> np.ndarray:
+    """deformableMirror surface [n][n] (metres) from strokes [nA][nA] on the GPU."""
+    h = C.c_void_p()
+    call("csg_dm_create", ctx.h, C.byref(h), n, act.shape[0], sigma)
+    try:
+        a = torch.as_tensor(np.ascontiguousarray(act, np.float64), device="cuda")
+        out = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        call("csg_dm_surface", h, ptr(a), ptr(out))
+        ctx.sync()
+        return out.cpu().numpy()
+    finally:
+        call("csg_dm_destroy", h)
 
 
 def _tensor_from_ptr(addr: int, shape, dtype) -> torch.Tensor:

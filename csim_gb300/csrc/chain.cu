@@ -16,6 +16,9 @@
 extern "C" {
 int csg_mft_create(csg_ctx*, csg_mft**, int, int, int, int, const double*, const double*,
                    const double*, const double*, int, const double*, const double*, double, int);
+int csg_mft_create_ragged(csg_ctx*, csg_mft**, int, int, int, const int*, const double*,
+                          const double*, const double*, const double*, int, const double*,
+                          const double*, double, int);
 int csg_mft_destroy(csg_mft*);
 int csg_mft_execute(csg_ctx*, csg_mft*, const float*, float*, int, const int*, int, const float*,
                     const int*);
@@ -81,6 +84,7 @@ struct Elem {
   // fraunhofer
   csg_mft* mft = nullptr;
   int n_out = 0;
+  std::vector<int> n_out_l;  // ragged: per-wavelength image size (n_out = the largest)
   // padded-FFT focal-plane mask: P x P grid
   int P = 0;
   // per-wavelength tables (mirror phasors, Fresnel transfer function)
@@ -480,6 +484,20 @@ int csg_chain_add_fraunhofer(csg_chain* c, int n_out, double out_pixel, double l
   return CSG_OK;
 }
 
+int csg_chain_add_fraunhofer_ragged(csg_chain* c, const int* n_out, double out_pixel,
+                                    double lf_scale) {
+  CSG_CHECK(c && n_out, CSG_E_ARG, "csg_chain_add_fraunhofer_ragged: null argument");
+  int n_max = 0;
+  for (int l = 0; l < c->n_lambda; ++l) {
+    CSG_CHECK(n_out[l] > 0, CSG_E_SHAPE, "csg_chain_add_fraunhofer_ragged: bad size");
+    n_max = std::max(n_max, n_out[l]);
+  }
+  int rc = csg_chain_add_fraunhofer(c, n_max, out_pixel, lf_scale);
+  if (rc) return rc;
+  c->elems.back().n_out_l.assign(n_out, n_out + c->n_lambda);
+  return CSG_OK;
+}
+
 // Window of the field that the transform after elements (lo, hi) needs:
 // the intersection of the supports of the real masks applied in between
 // (also in calibration), rounded out to multiples of 32; the whole field when
@@ -539,9 +557,21 @@ static int build_plans(csg_chain* c) {
       std::vector<double> xo = pixel_centres(e.n_out, e.out_pixel);
       csg_mft_destroy(e.mft);
       e.mft = nullptr;
-      int rc = csg_mft_create(c->ctx, &e.mft, w.rows, w.pitch, e.n_out, e.n_out,
-                              xp.data() + w.r0, xp.data() + w.c0, xo.data(), xo.data(), L,
-                              e.lf.data(), e.pref.data(), -1.0, c->precision);
+      int rc;
+      if (e.n_out_l.empty()) {
+        rc = csg_mft_create(c->ctx, &e.mft, w.rows, w.pitch, e.n_out, e.n_out, xp.data() + w.r0,
+                            xp.data() + w.c0, xo.data(), xo.data(), L, e.lf.data(),
+                            e.pref.data(), -1.0, c->precision);
+      } else {  // each wavelength's own grid, centred, at the same pixel scale
+        std::vector<double> xr((size_t)L * e.n_out, 0.0);
+        for (int l = 0; l < L; ++l) {
+          std::vector<double> v = pixel_centres(e.n_out_l[l], e.out_pixel);
+          std::copy(v.begin(), v.end(), xr.begin() + (size_t)l * e.n_out);
+        }
+        rc = csg_mft_create_ragged(c->ctx, &e.mft, w.rows, w.pitch, e.n_out, e.n_out_l.data(),
+                                   xp.data() + w.r0, xp.data() + w.c0, xr.data(), xr.data(), L,
+                                   e.lf.data(), e.pref.data(), -1.0, c->precision);
+      }
       if (rc) return rc;
       e.win = MftWindow{w.r0, w.c0, n, n};  // input window of the n x n field
       e.win_rows = w.rows;

@@ -65,10 +65,12 @@ int make_map(CUtensorMap* m, const void* base, int k, int rows, long long planes
 // ------------------------------------------------------------ kernels
 // Operator generator: op[slot][part][sel][r][k] for r < rows, k < K.
 // value = pref_s * exp(sgn 2 pi i frac(cout_r cin_k / lf_s)); sel 0/1/2 = re/im/-im.
+// Ragged plans: slot s reads its output coordinates at cout + s * cstride
+// and its rows r >= valid[s] are zero.
 __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* __restrict__ cout,
                                  const double* __restrict__ cin, int rows, int K, int n_slots,
                                  const double* __restrict__ lf, const double* __restrict__ pref,
-                                 double sgn) {
+                                 double sgn, int cstride, const int* __restrict__ valid) {
   const long long n = (long long)n_slots * rows * K;
   const long long plane = (long long)rows * K;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -77,7 +79,7 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
     const long long t = i / K;
     const int r = (int)(t % rows);
     const int s = (int)(t / rows);
-    double turns = cout[r] * cin[k] / lf[s];
+    double turns = cout[(long long)s * cstride + r] * cin[k] / lf[s];
     turns -= rint(turns);  // exact in FP64 for |turns| < 2^52
     double sn, cs;
     sincospi(2.0 * sgn * turns, &sn, &cs);
@@ -86,6 +88,7 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
       pr = pref[2 * s];
       pi = pref[2 * s + 1];
     }
+    if (valid && r >= valid[s]) pr = pi = 0.0;
     const double re = pr * cs - pi * sn;
     const double im = pr * sn + pi * cs;
     __nv_bfloat16 a0, a1, a2, b0, b1, b2;
@@ -300,10 +303,13 @@ extern "C" int csg_mft_tuning_log(char* buf, size_t len) {
 
 extern "C" {
 
-int csg_mft_create(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_out_y,
-                   int n_out_x, const double* yin, const double* xin, const double* yout,
-                   const double* xout, int n_slots, const double* lf, const double* pref,
-                   double sgn, int precision) {
+// Shared body of csg_mft_create and csg_mft_create_ragged: with n_out
+// non-null, slot s has its own n_out[s] output coordinates at yout/xout +
+// s * n_out_y (n_out_y = n_out_x = the largest size).
+static int create_plan(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_out_y,
+                       int n_out_x, const double* yin, const double* xin, const double* yout,
+                       const double* xout, int n_slots, const double* lf, const double* pref,
+                       double sgn, int precision, const int* n_out) {
   CSG_CHECK(ctx && plan && yin && xin && yout && xout && lf, CSG_E_ARG,
             "csg_mft_create: null argument");
   CSG_CHECK(n_in_y > 0 && n_in_x > 0 && n_out_y > 0 && n_out_x > 0 && n_slots > 0, CSG_E_SHAPE,
@@ -326,7 +332,9 @@ int csg_mft_create(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_o
   const size_t op1_elems = (size_t)n_slots * 9 * n_out_x * n_in_x;
   const size_t op2_elems = (size_t)n_slots * 9 * n_out_y * n_in_y;
   double* dvec = nullptr;
-  const size_t nvec = (size_t)n_in_y + n_in_x + n_out_y + n_out_x + 3 * n_slots;
+  const int rs = n_out ? n_slots : 1;  // output coordinate sets
+  const size_t nvec = (size_t)n_in_y + n_in_x + (size_t)rs * (n_out_y + n_out_x) + 3 * n_slots +
+                      (n_out ? (n_slots + 1) / 2 : 0);
   if (cudaMalloc(&m->op1, op1_elems * 2) != cudaSuccess ||
       cudaMalloc(&m->op2, op2_elems * 2) != cudaSuccess ||
       cudaMalloc(&dvec, nvec * sizeof(double)) != cudaSuccess) {
@@ -342,29 +350,57 @@ int csg_mft_create(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_o
   size_t o = 0;
   const size_t o_yin = o; for (int i = 0; i < n_in_y; ++i) h[o++] = yin[i];
   const size_t o_xin = o; for (int i = 0; i < n_in_x; ++i) h[o++] = xin[i];
-  const size_t o_yout = o; for (int i = 0; i < n_out_y; ++i) h[o++] = yout[i];
-  const size_t o_xout = o; for (int i = 0; i < n_out_x; ++i) h[o++] = xout[i];
+  const size_t o_yout = o; for (size_t i = 0; i < (size_t)rs * n_out_y; ++i) h[o++] = yout[i];
+  const size_t o_xout = o; for (size_t i = 0; i < (size_t)rs * n_out_x; ++i) h[o++] = xout[i];
   const size_t o_lf = o; for (int i = 0; i < n_slots; ++i) h[o++] = lf[i];
   const size_t o_pref = o;
   for (int i = 0; i < n_slots; ++i) {
     h[o++] = pref ? pref[2 * i] : 1.0;
     h[o++] = pref ? pref[2 * i + 1] : 0.0;
   }
+  const size_t o_valid = o;  // int32 per slot, packed into the FP64 vector
+  if (n_out) memcpy(&h[o_valid], n_out, sizeof(int) * n_slots);
+  const int* valid = n_out ? reinterpret_cast<const int*>(dvec + o_valid) : nullptr;
   cudaStream_t st = ctx->stream;
   CSG_CUDA(cudaMemcpyAsync(dvec, h.data(), nvec * sizeof(double), cudaMemcpyHostToDevice, st));
   // stage-1 operator: rows u (xout), K = x (xin), no prefactor
   k_build_operator<<<grid_for((long long)n_slots * n_out_x * n_in_x, 256), 256, 0, st>>>(
-      m->op1, dvec + o_xout, dvec + o_xin, n_out_x, n_in_x, n_slots, dvec + o_lf, nullptr, sgn);
+      m->op1, dvec + o_xout, dvec + o_xin, n_out_x, n_in_x, n_slots, dvec + o_lf, nullptr, sgn,
+      n_out ? n_out_x : 0, valid);
   CSG_LAUNCH_CHECK();
   // stage-2 operator: rows v (yout), K = y (yin), carries the prefactor
   k_build_operator<<<grid_for((long long)n_slots * n_out_y * n_in_y, 256), 256, 0, st>>>(
       m->op2, dvec + o_yout, dvec + o_yin, n_out_y, n_in_y, n_slots, dvec + o_lf,
-      dvec + o_pref, sgn);
+      dvec + o_pref, sgn, n_out ? n_out_y : 0, valid);
   CSG_LAUNCH_CHECK();
   CSG_CUDA(cudaStreamSynchronize(st));
   cudaFree(dvec);
   *plan = m;
   return CSG_OK;
+}
+
+int csg_mft_create(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_out_y,
+                   int n_out_x, const double* yin, const double* xin, const double* yout,
+                   const double* xout, int n_slots, const double* lf, const double* pref,
+                   double sgn, int precision) {
+  return create_plan(ctx, plan, n_in_y, n_in_x, n_out_y, n_out_x, yin, xin, yout, xout, n_slots,
+                     lf, pref, sgn, precision, nullptr);
+}
+
+// Ragged batch (one plan, one launch, fields of every size): slot s maps to
+// an n_out[s] x n_out[s] grid at yout/xout[s][0 .. n_out[s]); outputs are
+// n_out_max^2 planes whose leading n_out[s] rows and columns hold the slot's
+// transform and the rest is zero.
+int csg_mft_create_ragged(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_out_max,
+                          const int* n_out, const double* yin, const double* xin,
+                          const double* yout, const double* xout, int n_slots, const double* lf,
+                          const double* pref, double sgn, int precision) {
+  CSG_CHECK(n_out && n_slots > 0, CSG_E_ARG, "csg_mft_create_ragged: null n_out");
+  for (int s = 0; s < n_slots; ++s)
+    CSG_CHECK(n_out[s] > 0 && n_out[s] <= n_out_max, CSG_E_SHAPE,
+              "csg_mft_create_ragged: n_out[s] must be in [1, n_out_max]");
+  return create_plan(ctx, plan, n_in_y, n_in_x, n_out_max, n_out_max, yin, xin, yout, xout,
+                     n_slots, lf, pref, sgn, precision, n_out);
 }
 
 int csg_mft_destroy(csg_mft* m) {

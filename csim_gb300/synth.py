@@ -236,3 +236,90 @@ def plain_lyot_arrays(spec: PlainLyotSpec, sources=None) -> dict:
     return dict(pupil=pupil, sag=(0.5 * w).astype(np.float32), occulter=occ,
                 lyot=circle_mask(spec.n, spec.lyot * spec.radius_px), dx=dx, lam=lam, tel=tel,
                 ef=ef, lam_ref=lam_ref, lod_image=tel.compute_loD(lam_ref))
+
+
+# ------------------------------------------------------------- broadband
+def segmented_hex_aperture(n: int, n_rings: int, radius_px: float, gap: float) -> np.ndarray:
+    """Hex-segmented aperture: the 3 n (n+1) + 1 flat-topped hexagonal
+    segments of the standard rings (neighbours along 90 and +-30 degrees),
+    scaled so the outermost segment corners touch radius_px, each segment
+    shrunk by gap of the segment pitch (1% gaps: gap = 0.01)."""
+    # outermost corner distance in pitch units: ring n along 30 deg plus the
+    # circumradius 1/sqrt(3)
+    pitch = radius_px / (n_rings + 1.0 / math.sqrt(3.0))
+    c = (n - 1) / 2.0
+    yy, xx = np.mgrid[:n, :n]
+    x = (xx - c) / pitch
+    y = (yy - c) / pitch
+    # axial coordinates of the lattice (e_q = (sqrt(3)/2, 1/2), e_r = (0, 1))
+    q = x * 2.0 / math.sqrt(3.0)
+    r = y - q / 2.0
+    # cube rounding to the nearest lattice point
+    cx, cz = q, r
+    cy = -cx - cz
+    rx, ry, rz = np.rint(cx), np.rint(cy), np.rint(cz)
+    dxr, dyr, dzr = np.abs(rx - cx), np.abs(ry - cy), np.abs(rz - cz)
+    fix_x = (dxr > dyr) & (dxr > dzr)
+    fix_y = ~fix_x & (dyr > dzr)
+    rx = np.where(fix_x, -ry - rz, rx)
+    ry = np.where(fix_y, -rx - rz, ry)
+    rz = np.where(~fix_x & ~fix_y, -rx - ry, rz)
+    ring = np.maximum(np.maximum(np.abs(rx), np.abs(ry)), np.abs(rz))
+    # position inside the segment, in pitch units
+    px = x - rx * math.sqrt(3.0) / 2.0
+    py = y - (rz + rx / 2.0)
+    apo = 0.5 - gap / 2.0  # apothem of the shrunk segment
+    inside = (np.abs(py) <= apo) & (math.sqrt(3.0) * np.abs(px) + np.abs(py) <= 2.0 * apo)
+    return ((ring <= n_rings) & inside).astype(np.float64)
+
+
+@dataclass
+class BroadbandSpec:
+    """Broadband batched propagation: 2048^2 pupil with a 6-ring segmented hex
+    aperture (127 segments, 1% gaps), a 48 x 48 actuator deformable mirror
+    (Gaussian influence, sigma = 1 actuator pitch, strokes N(0, 5 nm)),
+    11 wavelengths uniform over a 10% band at 650 nm, 3 sources (on axis and
+    +-0.01 lambda/D), and per-wavelength focal grids of 460^2 .. 540^2 at one
+    pixel scale (the grid grows with lambda), all 33 fields in one launch."""
+    n: int = 2048
+    radius_px: float = 900.0
+    n_rings: int = 6
+    gap: float = 0.01
+    beam_radius: float = 0.025
+    center: float = 650e-9
+    bandwidth: float = 0.10
+    n_lambda: int = 11
+    f_ratio: float = 15.0
+    diameter: float = 2.4
+    n_act: int = 48
+    dm_sigma: float = 1.0
+    dm_rms: float = 5e-9
+    source_offsets_lod: tuple = (0.0, 0.01, -0.01)
+    n_out_min: int = 460
+    n_out_max: int = 540
+    spl: float = 4.0
+    seed: int = 11
+
+    def n_out(self) -> list:
+        return [int(round(v)) for v in np.linspace(self.n_out_min, self.n_out_max, self.n_lambda)]
+
+
+def broadband_arrays(spec: BroadbandSpec) -> dict:
+    """Seeded host-side inputs of the broadband chain (the DM surface itself is
+    built from the strokes by the DM element)."""
+    rng = np.random.default_rng(spec.seed)
+    dx = spec.beam_radius / spec.radius_px
+    # wavelengthBandwidth (efield.cpp:351-417): n points uniform over c (1 +- f/2)
+    lam = np.linspace(spec.center * (1 - spec.bandwidth / 2), spec.center * (1 + spec.bandwidth / 2),
+                      spec.n_lambda)
+    tel = Telescope(spec.diameter, spec.f_ratio)
+    # a tilt of t lambda/D: phase 2 pi (2 x tip / Lx) has gradient 2 pi / D_beam
+    lx = spec.n * dx
+    srcs = [PointSource(1.0, o * lx / (2.0 * 2.0 * spec.beam_radius), 0.0)
+            for o in spec.source_offsets_lod]
+    ef = EField(spec.n, spec.beam_radius, dx, lam, srcs)
+    act = rng.normal(0.0, spec.dm_rms, (spec.n_act, spec.n_act))
+    lam_ref = float(spec.center)
+    return dict(pupil=segmented_hex_aperture(spec.n, spec.n_rings, spec.radius_px, spec.gap),
+                act=act, dx=dx, lam=lam, tel=tel, ef=ef, lam_ref=lam_ref,
+                lod_image=tel.compute_loD(lam_ref), n_out=spec.n_out())

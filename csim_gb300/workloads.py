@@ -16,8 +16,9 @@ import numpy as np
 import torch
 
 from . import coronagraph as cg
-from .synth import (PiaacmcSpec, PlainLyotSpec, circle_mask,  # noqa: F401
-                    hex_layout_standard, piaa_sag, piaacmc_arrays, plain_lyot_arrays)
+from .synth import (BroadbandSpec, PiaacmcSpec, PlainLyotSpec, broadband_arrays,  # noqa: F401
+                    circle_mask, hex_layout_standard, piaa_sag, piaacmc_arrays,
+                    plain_lyot_arrays, segmented_hex_aperture)
 from ._lib import call
 from .runtime import Context, dvec, ptr
 
@@ -70,6 +71,20 @@ def build_plain_lyot(ctx: Context, spec: PlainLyotSpec, sources=None, precision:
         cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov),
     ]
     cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision)
+    return cor, a
+
+
+def build_broadband(ctx: Context, spec: BroadbandSpec, precision: int = 6):
+    """Broadband chain: segmented aperture -> DM -> per-wavelength ragged
+    final MFT; the batch is every (wavelength, source) pair (33 fields)."""
+    a = broadband_arrays(spec)
+    elems = [
+        cg.Mask(a["pupil"]),
+        cg.DeformableMirror(a["act"], spec.dm_sigma, 1.0),
+        cg.FraunhoferFocalRagged(a["lam_ref"], spec.spl, a["n_out"]),
+    ]
+    cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision)
+    a["dm_surface"] = cor.dm_surface
     return cor, a
 
 

@@ -54,6 +54,7 @@ typedef struct csg_mft csg_mft;
 typedef struct csg_chain csg_chain;
 typedef struct csg_respobj csg_respobj;
 typedef struct csg_de csg_de;
+typedef struct csg_dm csg_dm;
 
 /* ------------------------------------------------------------ context */
 /* One context per host thread: owns a CUDA stream on `device`. No global
@@ -152,6 +153,16 @@ int csg_mft_create(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_o
                    int n_out_x, const double* yin, const double* xin, const double* yout,
                    const double* xout, int n_slots, const double* lf, const double* pref,
                    double sgn, int precision);
+/* Ragged plan: per-wavelength focal grids of different sizes in one launch
+ * (zoomFft output grows with lambda at fixed pixel scale). Slot s maps to an
+ * n_out[s] x n_out[s] grid whose coordinates are yout/xout[s][0..n_out[s])
+ * (arrays [n_slots][n_out_max]); the plan's outputs are n_out_max^2 planes
+ * holding slot s's transform in the leading n_out[s] rows and columns and
+ * zeros elsewhere. */
+int csg_mft_create_ragged(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int n_out_max,
+                          const int* n_out, const double* yin, const double* xin,
+                          const double* yout, const double* xout, int n_slots, const double* lf,
+                          const double* pref, double sgn, int precision);
 int csg_mft_destroy(csg_mft* plan);
 /* Transform n_fields planar fields (in: [F][2][n_in_y][n_in_x]) into
  * out ([F][2][n_out_y][n_out_x]); slot[f] picks the operator slot of field f
@@ -263,6 +274,11 @@ int csg_chain_add_fft_fpm(csg_chain* chain, int pad, const float* mask_re, const
  * out_pixel (= loD / samplesPerflD), lambda f = lambda lf_scale with
  * lf_scale = 2 beamRadius primaryfRatio. Must be the last element. */
 int csg_chain_add_fraunhofer(csg_chain* chain, int n_out, double out_pixel, double lf_scale);
+/* fraunhoferFocal with a per-wavelength output size n_out[n_lambda] at the
+ * same out_pixel (a ragged batch, one launch): images are n_max^2 planes
+ * holding wavelength l's n_out[l]^2 image in their leading rows and columns. */
+int csg_chain_add_fraunhofer_ragged(csg_chain* chain, const int* n_out, double out_pixel,
+                                    double lf_scale);
 /* The batch: per field the wavelength index, point-source amplitude
  * (sqrt(flux)), tip and tilt (times magnification), and candidate index. */
 int csg_chain_set_batch(csg_chain* chain, int n_fields, const int* lambda_idx, const double* amp,
@@ -288,6 +304,21 @@ int csg_mft_reserve(csg_mft* plan, int n_fields);
 int csg_mft_tuning(csg_mft* plan, int* bn, float* ms128, float* ms64);
 /* Every autotuning decision of the process as a JSON list. */
 int csg_mft_tuning_log(char* buf, size_t len);
+
+/* ------------------------------------------------------ deformable mirror */
+/* deformableMirror::compute_influence_function / compute_deformable_mirror_surface
+ * (deformableMirror.cpp:205-270): Gaussian influence of width sigma actuator
+ * pitches, n_act x n_act actuators as delta points on the upsampled grid,
+ * half-cell shift, fft_truncate to N x N, times the influence spectrum,
+ * inverse FFT, real part. The whole chain is separable, so the surface is
+ * computed exactly as Re(M A M^T) with an N x n_act FP64 basis M built once
+ * per geometry. */
+int csg_dm_create(csg_ctx* ctx, csg_dm** dm, int n, int n_act, double sigma);
+int csg_dm_destroy(csg_dm* dm);
+/* Device FP64 strokes [n_act][n_act] (metres) -> device fp32 surface [N][N]
+ * (metres), on the context's stream. Apply it with a mirror element
+ * (deformableMirror::execute = mirror::execute with this surface). */
+int csg_dm_surface(csg_dm* dm, const double* act, float* surface);
 
 /* ---------------------------------------------------- intensity / contrast */
 /* regionContrast::compute_intensity (regionContrast.cpp:124-143) and the

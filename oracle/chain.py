@@ -79,3 +79,23 @@ def plain_lyot_field(inp: dict, spec, lam_idx: int, amp: float, tip: float, tilt
     gout = of.ArrayGeom.set_xy(n_out, n_out, inp["lod_image"] / spec.spl)
     return oe.fraunhofer_focal(e, geom, gout, [lam], ef.beamRadiusPhysical, tel.primaryfRatio,
                                use_czt=czt)[0]
+
+
+def broadband_field(inp: dict, spec, lam_idx: int, amp: float, tip: float, tilt: float,
+                    surface=None):
+    """One (wavelength, source) field of the broadband chain: point source ->
+    segmented aperture (mask) -> deformable mirror -> fraunhoferFocal onto the
+    wavelength's own n_out[l]^2 grid. surface: the DM surface (FP64 oracle
+    surface from the strokes when None)."""
+    ef, tel = inp["ef"], inp["tel"]
+    lam = float(inp["lam"][lam_idx])
+    n, dx = ef.n, inp["dx"]
+    geom = of.ArrayGeom.set_xy(n, n, dx)
+    if surface is None:
+        surface = oe.dm_surface(inp["act"], oe.dm_influence(geom, spec.dm_sigma, spec.n_act))
+    e = oe.point_source_field(geom, 1, amp * amp, tip, tilt)
+    e = oe.mask_apply(e, inp["pupil"])
+    e = oe.mirror_apply(e, surface, [lam], 1.0)
+    n_out = inp["n_out"][lam_idx]
+    gout = of.ArrayGeom.set_xy(n_out, n_out, inp["lod_image"] / spec.spl)
+    return oe.fraunhofer_focal(e, geom, gout, [lam], ef.beamRadiusPhysical, tel.primaryfRatio)[0]

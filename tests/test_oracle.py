@@ -109,3 +109,38 @@ def test_padded_fft_fpm_is_centred_convolution():
             if k[dy, dx] != 0:
                 conv += k[dy, dx] * np.roll(np.roll(p, dy, 0), dx, 1)
     assert np.allclose(got[0], conv[o:o + n, o:o + n], atol=1e-12)
+
+
+def _dm_separable(act, n, sigma):
+    """Separable restatement of the DM surface used by the GPU (Re(M A M^T))."""
+    nA = act.shape[0]
+    ur = -(-(n + 1) // nA)
+    U = ur * nA
+    s = sigma * n / nA
+    y = -(n - 1) / 2.0 + np.arange(n)
+    ghat = np.fft.fft(np.exp(-4 * math.log(2) * y * y / (s * s)))
+    h = n * (1 - 1 / nA) / 2
+
+    def Y(k):
+        f = np.where(k < U // 2, k, k - U) / n
+        return np.exp(2j * math.pi * (f[:, None] * h - np.outer(k, np.arange(nA)) / nA))
+    kp = np.arange(n)
+    src = np.where(kp < n // 2, kp, U - n + kp)
+    X = Y(src)
+    X[n // 2] = 0.5 * (Y(np.array([n // 2]))[0] + Y(np.array([U - n // 2]))[0])
+    X = X * ghat[:, None]
+    M = np.fft.ifft(X, axis=0)
+    return np.real(M @ act @ M.T)
+
+
+@pytest.mark.parametrize("n,nA,sigma", [(64, 8, 1.0), (128, 12, 1.3), (256, 48, 1.0)])
+def test_dm_surface_separable_form(n, nA, sigma):
+    """deformableMirror.cpp:216-270 (upsample, FFT, shift, fft_truncate,
+    x FFT(influence), IFFT, real) equals Re(M A M^T) with the N x nA basis
+    the GPU builds."""
+    rng = np.random.default_rng(n)
+    act = rng.normal(0, 5e-9, (nA, nA))
+    geom = of.ArrayGeom.set_xy(n, n, 1e-4)
+    ref = oe.dm_surface(act, oe.dm_influence(geom, sigma, nA))
+    got = _dm_separable(act, n, sigma)
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
