@@ -76,6 +76,7 @@ SIGNATURES = {
     "csg_chain_add_fpm_hex": ([P, P, P, I, I, I, D, D, D, D, D, D, I], None),
     "csg_chain_add_fraunhofer": ([P, I, D, D], None),
     "csg_chain_add_fft_fpm": ([P, I, P, P, I], None),
+    "csg_chain_response": ([P, I, P, I, P, P], None),
     "csg_chain_add_fraunhofer_ragged": ([P, P, D, D], None),
     "csg_mft_create_ragged": ([P, C.POINTER(P), I, I, I, P, P, P, P, P, I, P, P, D, I], None),
     "csg_dm_create": ([P, C.POINTER(P), I, I, D], None),

@@ -230,6 +230,16 @@ class Coronagraph:
         self._sag_ptr = p.value
         return _tensor_from_ptr(p.value, (n_cand, self.n_hex), torch.float64)
 
+    def response(self, pix_idx, fpm_index: int = 0):
+        """makeHexCFpmResponse: (M [n_base][n_pix][n_hex + 1] complex128,
+        calibration max) for the current batch's (wavelength, source) fields."""
+        pix = np.ascontiguousarray(pix_idx, np.int32)
+        m = np.zeros((self.n_fields, pix.size, self.n_hex + 1), np.complex128)
+        cmax = C.c_double()
+        call("csg_chain_response", self.h, fpm_index, pix.ctypes.data_as(C.c_void_p), pix.size,
+             m.ctypes.data_as(C.c_void_p), C.byref(cmax))
+        return m, cmax.value
+
     def execute(self, calibrating: bool = False, use_graph: bool = False) -> torch.Tensor:
         call("csg_chain_execute", self.h, int(calibrating), int(use_graph))
         p = C.c_void_p()

@@ -27,6 +27,7 @@ int csg_mask_real(csg_ctx*, float*, int, int, int, const float*, int);
 int csg_phase_screen(csg_ctx*, float*, int, int, int, const float*, const double*, double);
 int csg_complex_mask(csg_ctx*, float*, int, int, int, const float*, const float*, int, int);
 int csg_fresnel(csg_ctx*, float*, int, int, const double*, double, double);
+int csg_intensity(csg_ctx*, const float*, int, int, int, double*, double*);
 int csg_point_source(csg_ctx*, float*, int, int, int, double, double, const double*,
                      const double*, const double*);
 }
@@ -756,17 +757,12 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
   return prog;
 }
 
-static int run_walk(csg_chain* c, int calibrating) {
+// One step of the walk over the chain's first F fields.
+static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
   csg_ctx* ctx = c->ctx;
-  const int F = c->n_fields, n = c->n;
-  FieldInfo fi;
-  fi.lam = c->lam_f;
-  fi.amp = c->amp;
-  fi.tip = c->tip;
-  fi.tilt = c->tilt;
-  fi.slot = c->slot;
+  const int n = c->n;
   int rc = CSG_OK;
-  for (const Step& s : plan_walk(c, calibrating)) {
+  {
     switch (s.kind) {
       case Step::PIX:
         rc = pixops_pass(ctx->stream, c->field, F, n, n, s.pro, fi);
@@ -804,6 +800,19 @@ static int run_walk(csg_chain* c, int calibrating) {
         break;
       }
     }
+  }
+  return rc;
+}
+
+static int run_walk(csg_chain* c, int calibrating) {
+  FieldInfo fi;
+  fi.lam = c->lam_f;
+  fi.amp = c->amp;
+  fi.tip = c->tip;
+  fi.tilt = c->tilt;
+  fi.slot = c->slot;
+  for (const Step& s : plan_walk(c, calibrating)) {
+    int rc = run_step(c, s, fi, c->n_fields);
     if (rc) return rc;
   }
   return CSG_OK;
@@ -843,6 +852,224 @@ int csg_chain_execute(csg_chain* c, int calibrating, int use_graph) {
   }
   CSG_CUDA(cudaGraphLaunch(c->exec, c->ctx->stream));
   return CSG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------ response matrix
+namespace csg {
+
+// Mask of one response column on the transformed box (makeHexCFpmResponse
+// with complexHexMaskFPM's useOnlyThisHex, complexHexMaskFPM.cpp:72-87, all
+// sags zero): column h < n_hex keeps the sub-pixel counts of hex h only;
+// column n_hex keeps the counts outside every hex and is the Babinet column
+// (fliplr(M) - 1, fpmPupToLyot.cpp:444-450). Output [K][2][RR][CC] (real).
+__global__ void k_hex_column_mask(const int16_t* __restrict__ hex_id,
+                                  const uint16_t* __restrict__ count, int S, int r0, int c0,
+                                  int RR, int CC, float inv_nsub2, int n_hex,
+                                  const int* __restrict__ col, float* __restrict__ out) {
+  const int j = blockIdx.y;
+  const int h = col[j];
+  const int plane = RR * CC;
+  const size_t splane = (size_t)S * S;
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < plane; o += gridDim.x * blockDim.x) {
+    const int r = r0 + o / CC, cc = c0 + o % CC;
+    const size_t src = (size_t)r * S + (S - 1 - cc);  // fliplr
+    float m = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int id = hex_id[k * splane + src];
+      if (id == h || (h == n_hex && id < 0)) m += (float)count[k * splane + src];
+    }
+    float* base = out + (size_t)j * 2 * plane + o;
+    base[0] = m * inv_nsub2 - (h == n_hex ? 1.f : 0.f);
+    base[plane] = 0.f;
+  }
+}
+
+// Chunk fields j: the Babinet column starts from the field E (the "+ E" of
+// fpmPupToLyot.cpp:155-158), every other column from zero.
+__global__ void k_response_init(const float* __restrict__ e0, float* __restrict__ out, int n,
+                                const int* __restrict__ col, const int* __restrict__ base,
+                                int n_hex) {
+  const int j = blockIdx.y;
+  const size_t fp = (size_t)2 * n * n;
+  const bool bab = col[j] == n_hex;
+  const float* src = e0 + (size_t)base[j] * fp;
+  float* dst = out + (size_t)j * fp;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < fp;
+       i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = bab ? src[i] : 0.f;
+}
+
+// M[base][pix][col] (complex FP64, interleaved) <- region pixels of the image.
+__global__ void k_response_gather(const float* __restrict__ img, int no, const int* __restrict__ pix,
+                                  int n_pix, const int* __restrict__ col,
+                                  const int* __restrict__ base, int ncol,
+                                  double* __restrict__ M) {
+  const int j = blockIdx.y;
+  const size_t plane = (size_t)no * no;
+  const float* re = img + (size_t)j * 2 * plane;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_pix; p += gridDim.x * blockDim.x) {
+    const size_t o = ((size_t)base[j] * n_pix + p) * ncol + col[j];
+    M[2 * o] = re[pix[p]];
+    M[2 * o + 1] = re[plane + pix[p]];
+  }
+}
+
+}  // namespace csg
+
+extern "C" {
+
+// makeHexCFpmResponse::compute_response (makeHexCFpmResponse.cpp:91-190) for
+// the chain's current batch (each field one (wavelength, source) pair; the
+// candidate index is ignored): column h of M for base field b is the final
+// image at the region pixels with only hex h in the fpm_index-th hex FPM
+// (Babinet off), and column n_hex the Babinet response of the area outside
+// the hexes. The walk up to the FPM and its forward transform run once per
+// base field; the columns are batched through the return transform and the
+// rest of the walk in chunks. m_host: complex<double> interleaved, row-major
+// [n_base][n_pix][n_hex + 1] (csg_respobj_create's layout); calib_max: the
+// maximum of the calibration intensity summed over the batch
+// (makeHexCFpmResponse.cpp:96-113).
+int csg_chain_response(csg_chain* c, int fpm_index, const int* pix_idx, int n_pix,
+                       double* m_host, double* calib_max) {
+  CSG_CHECK(c && pix_idx && m_host && calib_max && n_pix > 0, CSG_E_ARG,
+            "csg_chain_response: bad argument");
+  CSG_CHECK(c->n_fields > 0, CSG_E_STATE, "csg_chain_response: no batch (csg_chain_set_batch)");
+  DeviceGuard g(c->ctx->device);
+  csg_ctx* ctx = c->ctx;
+  cudaStream_t st = ctx->stream;
+  int rc = prepare(c);
+  if (rc) return rc;
+  const int B = c->n_fields, n = c->n;
+  std::vector<Step> prog = plan_walk(c, 0);
+  int fi_step = -1, k = 0;
+  for (size_t i = 0; i < prog.size(); ++i)
+    if (prog[i].kind == Step::FPM && k++ == fpm_index) fi_step = (int)i;
+  CSG_CHECK(fi_step >= 0, CSG_E_ARG, "csg_chain_response: no such hex FPM element");
+  for (size_t i = fi_step + 1; i < prog.size(); ++i)
+    CSG_CHECK(prog[i].kind == Step::PIX || prog[i].kind == Step::FINAL, CSG_E_STATE,
+              "csg_chain_response: only element ops and the final image may follow the FPM");
+  CSG_CHECK(prog.back().kind == Step::FINAL, CSG_E_STATE,
+            "csg_chain_response: the walk must end in a fraunhoferFocal");
+  const Elem& e = *prog[fi_step].e;
+  const Elem& fin = *prog.back().e;
+  const int no = fin.n_out, ncol = e.n_hex + 1;
+  for (int p = 0; p < n_pix; ++p)
+    CSG_CHECK(pix_idx[p] >= 0 && pix_idx[p] < no * no, CSG_E_ARG,
+              "csg_chain_response: region pixel outside the image");
+
+  // calibration normalisation: max over pixels of sum_fields |E|^2
+  rc = run_walk(c, 1);
+  if (rc) return rc;
+  {
+    double* isum = nullptr;
+    double* imax = nullptr;
+    CSG_CUDA(cudaMalloc(&isum, sizeof(double) * no * no));
+    CSG_CUDA(cudaMalloc(&imax, sizeof(double)));
+    rc = csg_intensity(ctx, c->image, no, no, B, isum, imax);
+    if (!rc) CSG_CUDA(cudaMemcpyAsync(calib_max, imax, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CSG_CUDA(cudaStreamSynchronize(st));
+    cudaFree(isum);
+    cudaFree(imax);
+    if (rc) return rc;
+  }
+
+  // the walk up to the FPM and its forward transform, once per base field
+  FieldInfo fi{c->lam_f, c->amp, c->tip, c->tilt, c->slot};
+  for (int i = 0; i < fi_step && !rc; ++i) rc = run_step(c, prog[i], fi, B);
+  if (rc) return rc;
+  rc = csg_mft_execute(ctx, e.mft1, c->field, c->fpm, B, c->slot, 0, nullptr, nullptr);
+  if (rc) return rc;
+
+  // chunks of columns x base fields
+  const long long total = (long long)ncol * B;
+  const int K = (int)std::min<long long>(total, 128);
+  const size_t fbytes = sizeof(float) * 2 * n * n;
+  float *e0 = nullptr, *work = nullptr, *mask = nullptr, *img = nullptr;
+  double* Md = nullptr;
+  int *d_idx = nullptr, *d_pix = nullptr;
+  auto cleanup = [&]() {
+    for (void* p : {(void*)e0, (void*)work, (void*)mask, (void*)img, (void*)Md, (void*)d_idx,
+                    (void*)d_pix})
+      cudaFree(p);
+  };
+  const size_t box = (size_t)e.RR * e.CC;
+  if (cudaMalloc(&e0, fbytes * B) != cudaSuccess || cudaMalloc(&work, fbytes * K) != cudaSuccess ||
+      cudaMalloc(&mask, sizeof(float) * 2 * box * K) != cudaSuccess ||
+      cudaMalloc(&img, sizeof(float) * 2 * no * no * K) != cudaSuccess ||
+      cudaMalloc(&Md, sizeof(double) * 2 * (size_t)B * n_pix * ncol) != cudaSuccess ||
+      cudaMalloc(&d_idx, sizeof(int) * 6 * K) != cudaSuccess ||
+      cudaMalloc(&d_pix, sizeof(int) * n_pix) != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    set_error("csg_chain_response: allocation failed");
+    return CSG_E_NOMEM;
+  }
+  CSG_CUDA(cudaMemcpyAsync(e0, c->field, fbytes * B, cudaMemcpyDeviceToDevice, st));
+  CSG_CUDA(cudaMemcpyAsync(d_pix, pix_idx, sizeof(int) * n_pix, cudaMemcpyHostToDevice, st));
+  int* d_col = d_idx;
+  int* d_base = d_idx + K;
+  int* d_slot = d_idx + 2 * K;
+  int* d_ident = d_idx + 3 * K;
+  double* d_lam = reinterpret_cast<double*>(d_idx + 4 * K);  // 2K ints = K doubles
+  std::vector<int> h_slot(B);
+  std::vector<double> h_lam(B);
+  CSG_CUDA(cudaMemcpyAsync(h_slot.data(), c->slot, sizeof(int) * B, cudaMemcpyDeviceToHost, st));
+  CSG_CUDA(cudaMemcpyAsync(h_lam.data(), c->lam_f, sizeof(double) * B, cudaMemcpyDeviceToHost, st));
+  CSG_CUDA(cudaStreamSynchronize(st));
+  rc = csg_mft_reserve(e.mft2, K);
+  if (!rc) rc = csg_mft_reserve(fin.mft, K);
+  std::vector<int> hb(4 * K + 2 * K);
+  for (long long j0 = 0; j0 < total && !rc; j0 += K) {
+    const int nk = (int)std::min<long long>(K, total - j0);
+    for (int j = 0; j < nk; ++j) {
+      const long long jj = j0 + j;
+      const int b = (int)(jj % B), h = (int)(jj / B);
+      hb[j] = h;
+      hb[K + j] = b;
+      hb[2 * K + j] = h_slot[b];
+      hb[3 * K + j] = j;
+      memcpy(&hb[4 * K + 2 * j], &h_lam[b], sizeof(double));
+    }
+    CSG_CUDA(cudaMemcpyAsync(d_idx, hb.data(), sizeof(int) * 6 * K, cudaMemcpyHostToDevice, st));
+    dim3 gm(grid_for((long long)box, 256, 256), nk);
+    k_hex_column_mask<<<gm, 256, 0, st>>>(e.hex_id, e.count, e.S, e.r0, e.c0, e.RR, e.CC,
+                                          1.f / (float)(e.n_sub * e.n_sub), e.n_hex, d_col, mask);
+    CSG_LAUNCH_CHECK();
+    dim3 gi(grid_for((long long)2 * n * n, 256, 512), nk);
+    k_response_init<<<gi, 256, 0, st>>>(e0, work, n, d_col, d_base, e.n_hex);
+    CSG_LAUNCH_CHECK();
+    FieldInfo fk{d_lam, nullptr, nullptr, nullptr, d_slot};
+    rc = mft_execute_ops(ctx, e.mft2, c->fpm, work, nk, d_slot, 1, mask, d_ident, PixOps(), fk,
+                         nullptr, &e.win, d_base);
+    for (size_t i = fi_step + 1; i < prog.size() && !rc; ++i) {
+      const Step& s = prog[i];
+      if (s.kind == Step::PIX)
+        rc = pixops_pass(st, work, nk, n, n, s.pro, fk);
+      else
+        rc = mft_execute_ops(ctx, s.e->mft, work, img, nk, d_slot, 0, nullptr, nullptr, s.pro,
+                             fk, &s.e->win, nullptr);
+    }
+    if (rc) break;
+    dim3 gg(grid_for(n_pix, 256, 64), nk);
+    k_response_gather<<<gg, 256, 0, st>>>(img, no, d_pix, n_pix, d_col, d_base, ncol, Md);
+    CSG_LAUNCH_CHECK();
+    CSG_CUDA(cudaStreamSynchronize(st));  // the host index staging is reused
+  }
+  if (!rc) {
+    cudaError_t ce = cudaMemcpyAsync(m_host, Md, sizeof(double) * 2 * (size_t)B * n_pix * ncol,
+                                     cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) {
+      set_error(std::string("csg_chain_response: ") + cudaGetErrorString(ce));
+      rc = CSG_E_CUDA;
+    }
+  }
+  cudaStreamSynchronize(st);
+  cleanup();
+  return rc;
 }
 
 // Final-plane field of the batch: [F][2][n_out][n_out] fp32 on the device.

@@ -110,19 +110,20 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
 // Data split: planar fp32 [F][2][R][C] -> (element ops `pre`) -> (times a
 // complex multiplier [n_mul][2][R][C] chosen by mul_idx[f]) -> bf16
 // [F][3][2][R][C]. Four pixels per thread (C is a multiple of 8); grid.y is
-// the field.
+// the field; field f reads input field in_idx[f] (f when in_idx is null).
 // The input is the R x C window at (r0, c0) of fields whose planes are
 // RT x PT (the element ops see the field's own coordinates and size).
 __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int R,
                               int C, int r0, int c0, int RT, int PT,
                               const float* __restrict__ mul,
-                              const int* __restrict__ mul_idx, PixOps pre, FieldInfo fi) {
+                              const int* __restrict__ mul_idx, PixOps pre, FieldInfo fi,
+                              const int* __restrict__ in_idx) {
   const int f = blockIdx.y;
   const int plane = R * C;
   const size_t fplane = (size_t)RT * PT;
   PixConsts k;
   if (pre.n) pix_consts(pre, fi, f, RT, PT, k);
-  const float* ire = in + (size_t)f * 2 * fplane;
+  const float* ire = in + (size_t)(in_idx ? in_idx[f] : f) * 2 * fplane;
   const float* iim = ire + fplane;
   const float* mre = mul ? mul + (size_t)mul_idx[f] * 2 * plane : nullptr;
   const int nv = plane / 4;
@@ -446,7 +447,7 @@ size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
 int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
                          const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
                          const PixOps& pre, const FieldInfo& fi, const MftWindow* iw,
-                         const MftWindow* ow) {
+                         const MftWindow* ow, const int* in_idx) {
   CSG_CHECK(ctx && m && in && out && slot, CSG_E_ARG, "csg_mft_execute: null argument");
   CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_mft_execute: n_fields must be positive");
   CSG_CHECK(!in_mul || mul_idx, CSG_E_ARG, "csg_mft_execute: in_mul needs mul_idx");
@@ -472,7 +473,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     CSG_CHECK(n_fields < 65536, CSG_E_SHAPE, "csg_mft_execute: too many fields in one call");
     dim3 grid(grid_for((long long)m->ny * m->nx / 4, 256, 1024), n_fields);
     k_split_field<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, inw.r0, inw.c0, inw.rows,
-                                        inw.pitch, in_mul, mul_idx, pre, fi);
+                                        inw.pitch, in_mul, mul_idx, pre, fi, in_idx);
     CSG_LAUNCH_CHECK();
   }
 

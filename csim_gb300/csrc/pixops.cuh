@@ -272,10 +272,11 @@ struct MftWindow {
 };
 
 // MFT with element ops applied to the input in the operand split; the input
-// and output may be windows of larger fields (nullptr: the whole plane).
+// and output may be windows of larger fields (nullptr: the whole plane), and
+// output field f may read input field in_idx[f] (device, nullptr: f).
 int mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
                     const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
                     const PixOps& pre, const FieldInfo& fi, const MftWindow* iw = nullptr,
-                    const MftWindow* ow = nullptr);
+                    const MftWindow* ow = nullptr, const int* in_idx = nullptr);
 
 }  // namespace csg

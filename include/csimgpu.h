@@ -291,6 +291,18 @@ int csg_chain_sags(csg_chain* chain, int n_cand, int n_hex, double** dev_sags);
  * calibration propagation of regionContrast.cpp:124-143); use_graph != 0
  * captures a CUDA graph on first use and replays it on later calls. */
 int csg_chain_execute(csg_chain* chain, int calibrating, int use_graph);
+/* makeHexCFpmResponse::compute_response (makeHexCFpmResponse.cpp:91-190)
+ * for the current batch (one base field per (wavelength, source); candidate
+ * ignored): column h < n_hex of M is the final image at the n_pix region
+ * pixels (row-major flat indices into the n_out^2 image) with only hex h in
+ * the fpm_index-th hex FPM and no Babinet term; column n_hex is the Babinet
+ * response of the area outside every hex. The walk up to the FPM runs once
+ * per base field; the columns run batched. m_host: complex<double>
+ * interleaved [n_base][n_pix][n_hex + 1] (csg_respobj_create's layout);
+ * calib_max: max over pixels of the calibration intensity summed over the
+ * batch. Synchronous. */
+int csg_chain_response(csg_chain* chain, int fpm_index, const int* pix_idx, int n_pix,
+                       double* m_host, double* calib_max);
 /* Device pointers to the final image fields [F][2][n_out][n_out] and to the
  * working pupil-plane fields [F][2][N][N]. */
 int csg_chain_image(csg_chain* chain, float** dev_image, int* n_out);
