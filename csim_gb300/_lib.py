@@ -76,6 +76,14 @@ SIGNATURES = {
     "csg_chain_add_fpm_hex": ([P, P, P, I, I, I, D, D, D, D, D, D, I], None),
     "csg_chain_add_fraunhofer": ([P, I, D, D], None),
     "csg_chain_add_fft_fpm": ([P, I, P, P, I], None),
+    "csg_mlp_create": ([P, C.POINTER(P), I, I, P, I, C.c_ulonglong], None),
+    "csg_mlp_destroy": ([P], None),
+    "csg_de_generate_draw": ([P, I, D, D, I], None),
+    "csg_mlp_features": ([P, P, I, P, D, D, D, I, I], None),
+    "csg_mlp_set_input": ([P, P, I], None),
+    "csg_mlp_forward": ([P, I, P], None),
+    "csg_mlp_train_step": ([P, I, P, C.c_float, P], None),
+    "csg_mlp_param": ([P, I, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P)], None),
     "csg_chain_response": ([P, I, P, I, P, P], None),
     "csg_chain_add_fraunhofer_ragged": ([P, P, D, D], None),
     "csg_mft_create_ragged": ([P, C.POINTER(P), I, I, I, P, P, P, P, P, I, P, P, D, I], None),

@@ -57,6 +57,7 @@ struct DeDev {
   int* perm;         // [3][P] r1, r2, r3
   int* coin;         // [1]
   unsigned long long* gen;
+  uint64_t draw = 0;  // extra trial sets of one generation (0: the standard draw)
 };
 
 // Shuffles (Fisher-Yates) and the either-or coin for one generation:
@@ -64,7 +65,7 @@ struct DeDev {
 // pop[si1], slice i+1 = slice i's order rotated by si2(i) + 1.
 __global__ void k_de_perm(DeDev d, int n_slices) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const uint64_t g = *d.gen;
+  const uint64_t g = *d.gen ^ (d.draw << 48);
   const int P = d.P;
   int* si1 = d.perm;  // slice 0 order, built in place
   for (int i = 0; i < P; ++i) si1[i] = i;
@@ -94,7 +95,7 @@ __global__ void k_de_perm(DeDev d, int n_slices) {
 // (:395-434) for every (candidate, variable).
 __global__ void k_de_trial(DeDev d, int strategy, double fw, double cr) {
   const int P = d.P, nv = d.nvar;
-  const uint64_t g = *d.gen;
+  const uint64_t g = *d.gen ^ (d.draw << 48);
   const long long n = (long long)P * nv;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -343,18 +344,24 @@ int csg_de_init(csg_de* de, const double* origin_host, double spread, int type) 
   return CSG_OK;
 }
 
-int csg_de_generate(csg_de* de, int strategy, double f_weight, double cr) {
+int csg_de_generate_draw(csg_de* de, int strategy, double f_weight, double cr, int draw) {
   CSG_CHECK(de, CSG_E_ARG, "csg_de_generate: null state");
   CSG_CHECK(strategy >= 0 && strategy <= 2, CSG_E_ARG,
             "csg_de_generate: strategy 0 (rand/1), 1 (local-to-best/1) or 2 (either-or)");
+  CSG_CHECK(draw >= 0 && draw < 65536, CSG_E_ARG, "csg_de_generate: draw out of range");
   DeviceGuard g(de->ctx->device);
   cudaStream_t st = de->ctx->stream;
-  k_de_perm<<<1, 32, 0, st>>>(de->d, strategy == 1 ? 2 : 3);
+  DeDev d = de->d;
+  d.draw = (uint64_t)draw;
+  k_de_perm<<<1, 32, 0, st>>>(d, strategy == 1 ? 2 : 3);
   CSG_LAUNCH_CHECK();
-  k_de_trial<<<grid_for((long long)de->d.P * de->d.nvar, 256), 256, 0, st>>>(de->d, strategy,
-                                                                             f_weight, cr);
+  k_de_trial<<<grid_for((long long)d.P * d.nvar, 256), 256, 0, st>>>(d, strategy, f_weight, cr);
   CSG_LAUNCH_CHECK();
   return CSG_OK;
+}
+
+int csg_de_generate(csg_de* de, int strategy, double f_weight, double cr) {
+  return csg_de_generate_draw(de, strategy, f_weight, cr, 0);
 }
 
 int csg_de_select(csg_de* de, int initial) {

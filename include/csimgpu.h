@@ -55,6 +55,7 @@ typedef struct csg_chain csg_chain;
 typedef struct csg_respobj csg_respobj;
 typedef struct csg_de csg_de;
 typedef struct csg_dm csg_dm;
+typedef struct csg_mlp csg_mlp;
 
 /* ------------------------------------------------------------ context */
 /* One context per host thread: owns a CUDA stream on `device`. No global
@@ -332,6 +333,32 @@ int csg_dm_destroy(csg_dm* dm);
  * (deformableMirror::execute = mirror::execute with this surface). */
 int csg_dm_surface(csg_dm* dm, const double* act, float* surface);
 
+/* ------------------------------------------------------- surrogate MLP */
+/* No reference counterpart: a fully connected network n_in -> hidden[] -> 1
+ * (exact-erf GELU) that maps a hex-FPM sag vector and wavelength to log10
+ * dark-hole contrast, used to pre-screen DE trial vectors. bf16 weights and
+ * activations, fp32 accumulation (tcgen05 GEMMs), fp32 master weights, Adam.
+ * Batches are multiples of 8 up to max_batch; hidden widths multiples of 8. */
+int csg_mlp_create(csg_ctx* ctx, csg_mlp** mlp, int n_in, int n_hidden, const int* hidden,
+                   int max_batch, unsigned long long seed);
+int csg_mlp_destroy(csg_mlp* mlp);
+/* Input batch from device FP64 sags [B][n_var] and wavelengths [B]: mode 0
+ * x = sag / sag_scale; mode 1 the hex phasors cos, sin(4 pi sag_scale sag /
+ * lambda) (2 n_var features; sag_scale = phaseSign); then (lambda - lam0) /
+ * lam_scale. */
+int csg_mlp_features(csg_mlp* mlp, const double* sags, int n_var, const double* lam,
+                     double sag_scale, double lam0, double lam_scale, int batch, int mode);
+/* Input batch from raw device fp32 features [B][n_in]. */
+int csg_mlp_set_input(csg_mlp* mlp, const float* x, int batch);
+/* Prediction of the current input batch into y (device fp32 [B], may be null). */
+int csg_mlp_forward(csg_mlp* mlp, int batch, float* y);
+/* Forward, MSE loss against t (device fp32 [B]; *loss device scalar, may be
+ * null), backward and one Adam step (lr = 0: gradients only). */
+int csg_mlp_train_step(csg_mlp* mlp, int batch, const float* t, float lr, float* loss);
+/* Device pointers of layer l: fp32 weights [out][in], bias [out] and their
+ * gradients from the last training step (any pointer may be null). */
+int csg_mlp_param(csg_mlp* mlp, int layer, float** w, float** b, float** gw, float** gb);
+
 /* ---------------------------------------------------- intensity / contrast */
 /* regionContrast::compute_intensity (regionContrast.cpp:124-143) and the
  * contrast mean (:195) / optObjective mean-or-max (optObjective.cpp:56-67):
@@ -387,6 +414,10 @@ int csg_de_buffers(csg_de* de, double** pop, double** f, double** trial, double*
 int csg_de_set_trial_buffer(csg_de* de, double* trial);
 /* strategy 0 = DE/rand/1, 1 = DE/local-to-best/1, 2 = either-or. */
 int csg_de_generate(csg_de* de, int strategy, double f_weight, double cr);
+/* Another independent trial set of the same generation (draw > 0; draw 0 is
+ * csg_de_generate), for screening several trials per member with a
+ * surrogate before the full evaluation. */
+int csg_de_generate_draw(csg_de* de, int strategy, double f_weight, double cr, int draw);
 /* initial != 0 after evaluating a fresh population (no selection). */
 int csg_de_select(csg_de* de, int initial);
 /* bestVal = huge, as on a re-initialisation (:249-258). */
