@@ -8,6 +8,12 @@ on-axis source), each propagated through the full element walk
 candidate. Metric: field propagations per second.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--workload piaacmc|plain_lyot|broadband]
+
+The other workloads measure the plain Lyot coronagraph (512^2 pupil,
+2048^2 padded-FFT occulter, 128^2 image; a batch of off-axis sources) and
+the broadband batch (2048^2 segmented pupil + DM, 11 wavelengths x 3
+sources onto ragged 460^2..540^2 images in one launch).
 
 Under torchrun each rank runs its own batch (candidates are independent:
 weak scaling, no data-path collective); timing is the max over ranks.
@@ -154,6 +160,131 @@ def reference_arm(args):
 
 
 # ------------------------------------------------------------------ GPU
+class Workload:
+    """One benchmark configuration: the chain, its batch, the per-step
+    device work (graph replay + contrast reduction) and the host input a
+    user uploads every step for the end-to-end number."""
+
+
+def setup_piaacmc(args, ctx, W, cg, rank):
+    import torch
+    wl = Workload()
+    spec = W.PiaacmcSpec()
+    B = args.fields
+    cor, inp = W.build_piaacmc(ctx, spec, precision=args.precision, support_crop=not args.no_crop)
+    rng = np.random.default_rng(100 + rank)
+    sags_h = W.random_sags(rng, B, spec.n_hex, spec.sag_range)
+    sags_d = cor.sags(B)
+    sags_d.copy_(torch.as_tensor(sags_h))
+    cor.batch_all(1)
+    cal = cor.execute(calibrating=True)
+    reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 2.0, 8.0)
+    wl.cmax = reg.calibration_max(cal)
+    cor.batch_all(B)
+    wl.per_group = 1
+    wl.cor, wl.inp, wl.reg, wl.B, wl.spec = cor, inp, reg, B, spec
+    # every step the candidates' sags come from the host
+    wl.host_in, wl.dev_in = torch.as_tensor(sags_h), sags_d
+    wl.cpu = lambda budget, nmax: cpu_fields_per_s(spec, inp, sags_h, budget, nmax)
+    wl.cpu_sample = ("FP64, reference algorithm: chirp-Z mask hat + 2048^2 FFT convolution")
+    wl.bound = "tensor"
+    wl.config = {"workload": WORKLOAD, "fields_per_step": B, "n": spec.n, "fpm_grid": spec.S,
+                 "n_hex": spec.n_hex, "image": cor.n_out,
+                 "precision": f"bf16x{args.precision}", "fpm_support_crop": not args.no_crop,
+                 "fpm_transformed_box": list(cor.fpm_region()),
+                 "l2": "working set > L2 (fields + MFT operands ~1.5 GB per step)"}
+    return wl
+
+
+def setup_plain_lyot(args, ctx, W, cg, rank):
+    """Plain Lyot coronagraph (512^2 pupil, 2048^2 padded-FFT occulter, 0.9
+    Lyot stop, 128^2 final MFT): a batch of point sources at random offsets
+    within 4 lambda/D, uploaded every step."""
+    import torch
+    wl = Workload()
+    spec = W.PlainLyotSpec()
+    B = args.fields
+    cor, inp = W.build_plain_lyot(ctx, spec, precision=args.precision)
+    cor.batch_all(1)
+    cal = cor.execute(calibrating=True)
+    reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 3.0, 12.0)
+    wl.cmax = reg.calibration_max(cal)
+    rng = np.random.default_rng(200 + rank)
+    lx = spec.n * inp["dx"]
+    per_lod = lx / (2.0 * 2.0 * spec.beam_radius)  # tip of one lambda/D
+    tips = rng.uniform(-4, 4, (2, B)) * per_lod
+    cor.set_batch(np.zeros(B, np.int32), np.ones(B), tips[0], tips[1], np.zeros(B, np.int32))
+    _, tip_d, tilt_d = cor.source_buffers()
+    wl.per_group = 1
+    wl.cor, wl.inp, wl.reg, wl.B, wl.spec = cor, inp, reg, B, spec
+    wl.host_in = torch.as_tensor(np.concatenate([tips[0], tips[1]]))
+    wl.dev_in = torch.empty(2 * B, dtype=torch.float64, device="cuda")
+    wl.dev_split = (tip_d, tilt_d)
+
+    def cpu(budget, nmax):
+        from oracle import chain as oc
+        t0 = time.perf_counter()
+        n = 0
+        while n < nmax and time.perf_counter() - t0 < budget:
+            oc.plain_lyot_field(inp, spec, 0, 1.0, tips[0][n % B], tips[1][n % B])
+            n += 1
+        dt = time.perf_counter() - t0
+        return n / dt, n, dt
+    wl.cpu = cpu
+    wl.cpu_sample = "FP64 numpy/scipy: 2048^2 FFT occulter + direct MFT"
+    wl.bound = "hbm"
+    wl.config = {"workload": "plain-lyot-512: 512^2 pupil (r = 200 px, 0.3 obstruction), "
+                             "Zernike 4-15 at 10 nm RMS, 2048^2 FFT, 3 lambda/D occulter, "
+                             "Lyot 0.9, 128^2 MFT at 0.25 lambda/D",
+                 "fields_per_step": B, "n": spec.n, "pad": spec.pad, "image": cor.n_out,
+                 "l2": "working set > L2 (padded fields 2 GB at 64 fields)"}
+    return wl
+
+
+def setup_broadband(args, ctx, W, cg, rank):
+    """Broadband batch: 2048^2 segmented pupil with a 48^2 DM, 11 wavelengths
+    x 3 sources = 33 fields in one launch onto ragged 460^2..540^2 grids; the
+    sources' offsets are uploaded every step."""
+    import torch
+    wl = Workload()
+    spec = W.BroadbandSpec()
+    cor, inp = W.build_broadband(ctx, spec, precision=args.precision)
+    B = cor.batch_all(1)
+    _, tip_d, tilt_d = cor.source_buffers()
+    tips = np.stack([tip_d.cpu().numpy(), tilt_d.cpu().numpy()])
+    wl.per_group = B
+    wl.cor, wl.inp, wl.reg, wl.B, wl.spec = cor, inp, None, B, spec
+    wl.cmax = 1.0
+    wl.host_in = torch.as_tensor(np.concatenate([tips[0], tips[1]]))
+    wl.dev_in = torch.empty(2 * B, dtype=torch.float64, device="cuda")
+    wl.dev_split = (tip_d, tilt_d)
+    li, amp, tip, tilt, _ = cor._batch
+
+    def cpu(budget, nmax):
+        from oracle import chain as oc
+        t0 = time.perf_counter()
+        n = 0
+        surf = inp["dm_surface"].astype(np.float64)
+        while n < nmax and time.perf_counter() - t0 < budget:
+            f = n % B
+            oc.broadband_field(inp, spec, int(li[f]), amp[f], tip[f], tilt[f], surface=surf)
+            n += 1
+        dt = time.perf_counter() - t0
+        return n / dt, n, dt
+    wl.cpu = cpu
+    wl.cpu_sample = "FP64 numpy: direct 2048^2 -> n_lambda^2 MFT per field"
+    wl.bound = "tensor"
+    wl.config = {"workload": "broadband-2048: 6-ring segmented aperture, 48^2 DM, 11 lambda "
+                             "(10% at 650 nm) x 3 sources, ragged 460^2..540^2 MFTs in one launch",
+                 "fields_per_step": B, "n": spec.n, "image_sizes": inp["n_out"],
+                 "precision": f"bf16x{args.precision}",
+                 "l2": "working set > L2 (33 x 32 MB fields + MFT operands)"}
+    return wl
+
+
+SETUP = {"piaacmc": setup_piaacmc, "plain_lyot": setup_plain_lyot, "broadband": setup_broadband}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -161,6 +292,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--fields", type=int, default=64)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="piaacmc", choices=sorted(SETUP),
+                    help="piaacmc (headline), plain_lyot, broadband")
     ap.add_argument("--precision", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-crop", action="store_true",
@@ -181,32 +314,22 @@ def main():
     from csim_gb300 import _lib
     from csim_gb300 import coronagraph as cg
     from csim_gb300 import workloads as W
-    from csim_gb300.runtime import Context, ptr
+    from csim_gb300.runtime import Context
 
     ctx = Context(local)
     stream = torch.cuda.Stream(local)
     ctx.bind_stream(stream)
-    spec = W.PiaacmcSpec()
-    B = args.fields
     with torch.cuda.stream(stream):
-        cor, inp = W.build_piaacmc(ctx, spec, precision=args.precision,
-                                   support_crop=not args.no_crop)
-        fpm_region = cor.fpm_region()
-        rng = np.random.default_rng(100 + rank)
-        sags_h = W.random_sags(rng, B, spec.n_hex, spec.sag_range)
-        sags_d = cor.sags(B)
-        sags_d.copy_(torch.as_tensor(sags_h))
-        # calibration (FPM removed) for the contrast normaliser
-        cor.batch_all(1)
-        cal = cor.execute(calibrating=True)
-        reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 2.0, 8.0)
-        cmax = reg.calibration_max(cal)
-        cor.batch_all(B)
-        contrast = torch.empty(B, dtype=torch.float64, device="cuda")
+        wl = SETUP[args.workload](args, ctx, W, cg, rank)
+        cor, B = wl.cor, wl.B
+        n_groups = B // wl.per_group
+        contrast = torch.zeros(n_groups, dtype=torch.float64, device="cuda")
 
         def step():
             img = cor.execute(calibrating=False, use_graph=True)
-            ctx.region_reduce(img, 1, reg.pix, mode=0, scale=1.0 / cmax, out=contrast)
+            if wl.reg is not None:
+                ctx.region_reduce(img, wl.per_group, wl.reg.pix, mode=0, scale=1.0 / wl.cmax,
+                                  out=contrast)
             return img
 
         for _ in range(args.warmup):
@@ -215,8 +338,10 @@ def main():
         # kernels per step, counted on an eager (non-graph) step after the
         # warm-up; graph replays launch exactly these kernels
         n0 = _lib.api["csg_launch_count"]()
-        ctx.region_reduce(cor.execute(use_graph=False), 1, reg.pix, mode=0, scale=1.0 / cmax,
-                          out=contrast)
+        img = cor.execute(use_graph=False)
+        if wl.reg is not None:
+            ctx.region_reduce(img, wl.per_group, wl.reg.pix, mode=0, scale=1.0 / wl.cmax,
+                              out=contrast)
         launches_per_step = _lib.api["csg_launch_count"]() - n0
         ctx.sync()
 
@@ -252,24 +377,29 @@ def main():
     ctx.sync()
     value = B * args.steps * ws / (ms / 1e3)
 
-    # ---- e2e through the C ABI with host buffers (pinned), every step:
-    # H2D of the candidates' sags, the walk, the contrast, D2H of the final
-    # image fields and the contrasts.
+    # ---- e2e through the C ABI with host buffers (pinned), every step: H2D
+    # of the step's input (the candidates' sags, or the sources' offsets), the
+    # walk, the contrast, D2H of the final image fields and the contrasts.
     img0 = cor.execute(use_graph=True)
-    host_sags = torch.as_tensor(sags_h).pin_memory()
+    host_in = wl.host_in.pin_memory()
     host_img = torch.empty(img0.shape, dtype=torch.float32).pin_memory()
-    host_con = torch.empty(B, dtype=torch.float64).pin_memory()
-    h2d = host_sags.numel() * 8
-    d2h = host_img.numel() * 4 + B * 8
+    host_con = torch.empty(n_groups, dtype=torch.float64).pin_memory()
+    h2d = host_in.numel() * host_in.element_size()
+    d2h = host_img.numel() * 4 + (n_groups * 8 if wl.reg is not None else 0)
     with torch.cuda.stream(stream):
         def e2e_step():
-            _lib.call("csg_memcpy_h2d", ctx.h, C.c_void_p(sags_d.data_ptr()),
-                      C.c_void_p(host_sags.data_ptr()), h2d)
+            _lib.call("csg_memcpy_h2d", ctx.h, C.c_void_p(wl.dev_in.data_ptr()),
+                      C.c_void_p(host_in.data_ptr()), h2d)
+            if hasattr(wl, "dev_split"):  # tip / tilt halves into the chain's batch
+                half = wl.dev_in.numel() // 2
+                wl.dev_split[0].copy_(wl.dev_in[:half])
+                wl.dev_split[1].copy_(wl.dev_in[half:])
             img = step()
             _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_img.data_ptr()),
                       C.c_void_p(img.data_ptr()), host_img.numel() * 4)
-            _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_con.data_ptr()),
-                      C.c_void_p(contrast.data_ptr()), B * 8)
+            if wl.reg is not None:
+                _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_con.data_ptr()),
+                          C.c_void_p(contrast.data_ptr()), n_groups * 8)
         for _ in range(3):
             e2e_step()
         ctx.sync()
@@ -298,51 +428,58 @@ def main():
     tbuf = C.create_string_buffer(1 << 16)
     _lib.call("csg_mft_tuning_log", tbuf, len(tbuf))
     tuning = json.loads(tbuf.value.decode())
-    g = prof.get("mft_gemm", {"count": 1, "ms": float("nan"), "flops": 0.0})
-    gemm_tflops = g["flops"] / (g["ms"] / 1e3) / 1e12
     # per-launch kernels only (the fresnel / fft aggregates repeat their passes)
     total_ms = sum(v["ms"] for k, v in prof.items() if k not in ("fresnel_3pass", "fft2d_2pass"))
-    split_terms = args.precision
-    roofline = {"bound": "tensor", "kernel": "k_split_gemm (tcgen05 split-bf16 MFT)",
-                "achieved": gemm_tflops, "peak": tc_peak, "unit": "TFLOP/s",
-                "frac": gemm_tflops / tc_peak, "peak_kind": f"{peak_kind} bf16 sustained",
-                "traffic": TRAFFIC.get(B),
-                "algorithmic_flops_per_launch": g["flops"] / g["count"],
-                "avg_launch_ms": g["ms"] / g["count"],
-                "executed_bf16_tflops": gemm_tflops * split_terms,
-                "share_of_step": g["ms"] / total_ms if total_ms else None,
-                "kernels": {k: {"count": v["count"], "ms": round(v["ms"], 4),
-                                **({"gbs": round(v["bytes"] / v["ms"] / 1e6, 1)} if v["bytes"] else {})}
-                            for k, v in prof.items()},
-                "mft_tile_autotune": tuning}
-    if "fresnel_3pass" in prof:
+    kernels = {k: {"count": v["count"], "ms": round(v["ms"], 4),
+                   **({"gbs": round(v["bytes"] / v["ms"] / 1e6, 1)} if v["bytes"] else {})}
+               for k, v in prof.items()}
+    g = prof.get("mft_gemm", {"count": 1, "ms": float("nan"), "flops": 0.0, "bytes": 0.0})
+    if wl.bound == "tensor":
+        gemm_tflops = g["flops"] / (g["ms"] / 1e3) / 1e12
+        roofline = {"bound": "tensor", "kernel": "k_split_gemm (tcgen05 split-bf16 MFT)",
+                    "achieved": gemm_tflops, "peak": tc_peak, "unit": "TFLOP/s",
+                    "frac": gemm_tflops / tc_peak, "peak_kind": f"{peak_kind} bf16 sustained",
+                    "traffic": TRAFFIC.get(B) if args.workload == "piaacmc" else None,
+                    "algorithmic_flops_per_launch": g["flops"] / g["count"],
+                    "avg_launch_ms": g["ms"] / g["count"],
+                    "executed_bf16_tflops": gemm_tflops * args.precision,
+                    "share_of_step": g["ms"] / total_ms if total_ms else None}
+    else:  # the padded-FFT occulter passes dominate
+        fz = prof.get("fresnel_3pass", {"count": 1, "ms": float("nan"), "bytes": 0.0})
+        gbs = fz["bytes"] / (fz["ms"] / 1e3) / 1e9
+        passes = sum(prof[k]["ms"] for k in prof if k.startswith("fft_"))
+        roofline = {"bound": "hbm", "kernel": "k_fft_rows / k_fft_cols (padded-FFT occulter)",
+                    "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                    "peak_kind": f"{peak_kind} copy bandwidth", "traffic": None,
+                    "algorithmic_bytes_per_launch": fz["bytes"] / fz["count"],
+                    "avg_launch_ms": fz["ms"] / fz["count"],
+                    "share_of_step": passes / total_ms if total_ms else None}
+    roofline["kernels"] = kernels
+    roofline["mft_tile_autotune"] = tuning
+    if "fresnel_3pass" in prof and wl.bound == "tensor":
         fz = prof["fresnel_3pass"]
         roofline["fresnel_gbs"] = fz["bytes"] / (fz["ms"] / 1e3) / 1e9
         roofline["fresnel_frac_hbm"] = roofline["fresnel_gbs"] / hbm_peak
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        v, n, dt = cpu_fields_per_s(spec, inp, sags_h, 15.0, 32)
+        v, n, dt = wl.cpu(15.0, 32)
         cpu = {"value": v, "unit": "fields/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{n} fields of the same workload in {dt:.1f} s (FP64, reference "
-                         "algorithm: chirp-Z mask hat + 2048^2 FFT convolution)"}
+               "sample": f"{n} fields of the same workload in {dt:.1f} s ({wl.cpu_sample})"}
 
+    wl.config["parallelism"] = f"fields sharded over {ws} rank(s)"
     line = {"metric": "field propagations/s", "value": value, "unit": "fields/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 fields, bf16x%d-split tensor-core MFT, f64 phases" % args.precision,
             "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "fields_per_step": B, "n": spec.n, "fpm_grid": spec.S,
-                       "n_hex": spec.n_hex, "image": cor.n_out, "precision": f"bf16x{args.precision}",
-                       "fpm_support_crop": not args.no_crop,
-                       "fpm_transformed_box": list(fpm_region),
-                       "l2": "working set > L2 (fields + MFT operands ~1.5 GB per step)",
-                       "parallelism": f"candidates sharded over {ws} rank(s)"},
+            "config": wl.config,
             "e2e": {"value": e2e_value, "unit": "fields/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches_per_step * args.steps,
-            "roofline": roofline, "clocks": clk, "cpu_baseline": cpu,
-            "contrast_sample": float(contrast[0].item())}
+            "roofline": roofline, "clocks": clk, "cpu_baseline": cpu}
+    if wl.reg is not None:
+        line["contrast_sample"] = float(contrast[0].item())
     if rank == 0:
         print(json.dumps(line))
     if dist:

@@ -85,6 +85,7 @@ SIGNATURES = {
     "csg_mlp_train_step": ([P, I, P, C.c_float, P], None),
     "csg_mlp_param": ([P, I, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P)], None),
     "csg_chain_response": ([P, I, P, I, P, P], None),
+    "csg_chain_batch_buffers": ([P, C.POINTER(P), C.POINTER(P), C.POINTER(P)], None),
     "csg_chain_add_fraunhofer_ragged": ([P, P, D, D], None),
     "csg_mft_create_ragged": ([P, C.POINTER(P), I, I, I, P, P, P, P, P, I, P, P, D, I], None),
     "csg_dm_create": ([P, C.POINTER(P), I, I, D], None),

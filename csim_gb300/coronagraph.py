@@ -223,6 +223,13 @@ class Coronagraph:
         self.set_batch(li, amp, tip, tilt, cand)
         return len(li)
 
+    def source_buffers(self):
+        """Device FP64 views [n_fields] of the batch's amplitude, tip and tilt
+        (written in place between executions)."""
+        a, t, u = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        call("csg_chain_batch_buffers", self.h, C.byref(a), C.byref(t), C.byref(u))
+        return tuple(_tensor_from_ptr(p.value, (self.n_fields,), torch.float64) for p in (a, t, u))
+
     def sags(self, n_cand: int) -> torch.Tensor:
         """The device sag buffer [n_cand, n_hex] (a torch view, written in place)."""
         p = C.c_void_p()

@@ -633,6 +633,18 @@ int csg_chain_set_batch(csg_chain* c, int n_fields, const int* lambda_idx, const
   return CSG_OK;
 }
 
+// Device FP64 arrays [n_fields] of the batch's source amplitude, tip and tilt:
+// writing them in place between executions changes the sources without a new
+// batch (or a new graph).
+int csg_chain_batch_buffers(csg_chain* c, double** amp, double** tip, double** tilt) {
+  CSG_CHECK(c, CSG_E_ARG, "csg_chain_batch_buffers: null chain");
+  CSG_CHECK(c->n_fields > 0, CSG_E_STATE, "csg_chain_batch_buffers: no batch");
+  if (amp) *amp = c->amp;
+  if (tip) *tip = c->tip;
+  if (tilt) *tilt = c->tilt;
+  return CSG_OK;
+}
+
 // Device buffer of candidate sags [n_cand][n_hex] (FP64 metres), allocated on
 // first use; the caller (or the DE kernels) writes it in place.
 int csg_chain_sags(csg_chain* c, int n_cand, int n_hex, double** dev_sags) {

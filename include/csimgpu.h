@@ -288,6 +288,10 @@ int csg_chain_set_batch(csg_chain* chain, int n_fields, const int* lambda_idx, c
  * by the caller or the DE kernels (complexHexMaskFPM set_optimization_data,
  * complexHexMaskFPM.cpp:176-191). */
 int csg_chain_sags(csg_chain* chain, int n_cand, int n_hex, double** dev_sags);
+/* Device FP64 arrays [n_fields] of the batch's source amplitude, tip and tilt
+ * (any pointer may be null); written in place between executions they change
+ * the sources without a new batch or graph. */
+int csg_chain_batch_buffers(csg_chain* chain, double** amp, double** tip, double** tilt);
 /* Run the walk (calibrating != 0 skips disable_for_calibration elements, the
  * calibration propagation of regionContrast.cpp:124-143); use_graph != 0
  * captures a CUDA graph on first use and replays it on later calls. */
