@@ -805,10 +805,24 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         break;
       case Step::FFT_FPM: {
         const Elem& e = *s.e;
-        rc = pad_center_pass(ctx->stream, c->field, c->padbuf, F, n, e.P, s.pro, fi);
         FresnelArgs fa{c->lam_f, 0.0, 1.0, e.tab, c->slot};  // H = the mask table
-        if (!rc) rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi);
-        if (!rc) rc = crop_center_pass(ctx->stream, c->padbuf, c->field, F, n, e.P);
+        const int lo = (e.P - n) / 2;
+        if (fft_band_supported(e.P, lo, n)) {
+          // only the n rows that hold the field are transformed; the padding
+          // is generated in registers and the crop is the last pass's store
+          rc = pixops_pass(ctx->stream, c->field, F, n, n, s.pro, fi);
+          FftBand band;
+          band.lo = lo;
+          band.n = n;
+          band.src = c->field;
+          band.dst = c->field;
+          if (!rc)
+            rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi, &band);
+        } else {
+          rc = pad_center_pass(ctx->stream, c->field, c->padbuf, F, n, e.P, s.pro, fi);
+          if (!rc) rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi);
+          if (!rc) rc = crop_center_pass(ctx->stream, c->padbuf, c->field, F, n, e.P);
+        }
         break;
       }
     }

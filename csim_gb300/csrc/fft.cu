@@ -1,15 +1,15 @@
 // Register-resident Stockham FFTs for square N x N planar fp32 fields and
 // the fused angular-spectrum Fresnel pipeline.
 //
-// A 2-D transform is two HBM passes: a row pass (4096/N rows per CTA) and a
-// column pass (COLS columns per CTA). Each pass reads and writes the field
-// once. Every thread owns 16 elements of one transform, u + s N/16, which it
-// loads straight from global memory (32 independent loads in flight per
-// thread) and stores straight back: the first stage runs on the registers
-// as loaded and the last stage leaves its outputs in the same natural
-// order, so shared memory carries only the exchanges between stages (two
-// for N = 1024: radix 16, 16, 4). The radix-R butterflies are unrolled
-// radix-2 decimation-in-frequency networks with exact W16 constants;
+// A 2-D transform is two HBM passes: a row pass (256 threads: 256 E / N
+// rows per CTA) and a column pass (COLS columns per CTA). Each pass reads
+// and writes the field once. Every thread owns E elements of one transform
+// (E = 32 from N = 512 up, 16 below), u + s N/E, which it loads straight
+// from global memory and stores straight back: the first stage runs on the
+// registers as loaded and the last stage leaves its outputs in the same
+// natural order, so shared memory carries only the exchanges between stages
+// (one for N = 1024: radix 32 x 32). The radix-R butterflies are unrolled
+// radix-2 decimation-in-frequency networks with exact W32 constants;
 // inter-stage twiddles come from an FP64-generated table. Shared memory is
 // XOR-swizzled (swz) so every stage access is bank-conflict-free.
 //
@@ -266,26 +266,38 @@ template <int N, int E, bool INV>
 __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCKS)
     k_fft_rows(float* __restrict__ field, float scale, const float2* __restrict__ tw,
                const __grid_constant__ PixOps pro, const __grid_constant__ PixOps epi,
-               const __grid_constant__ FieldInfo fi) {
+               const __grid_constant__ FieldInfo fi, const FftBand band) {
   using CF = RowCfg<N, E>;
   using A = RowAddr<N, E>;
   extern __shared__ float sm[];
   __shared__ PixConsts shk[2];
   float* re = sm;
   float* im = sm + CF::ROWS * N;
-  constexpr int CPF = N / CF::ROWS;  // CTAs per field
   constexpr int TPT = CF::TPT;
-  const int f = blockIdx.x / CPF;
+  const int cpf = band.n ? band.n / CF::ROWS : N / CF::ROWS;  // CTAs per field
+  const int f = blockIdx.x / cpf;
   const int t = threadIdx.x / TPT, u = threadIdx.x % TPT;
-  const int row = (blockIdx.x % CPF) * CF::ROWS + t;
+  const int row = band.lo + (blockIdx.x % cpf) * CF::ROWS + t;
   const size_t plane = (size_t)N * N;
   float* fre = field + (size_t)f * 2 * plane + (size_t)row * N + u;
   float* fim = fre + plane;
   // thread u of row t owns elements u + s N/E: each load and store
   // instruction of a warp covers 32 consecutive floats of a row
   float xr[E], xi[E];
+  // band: element s is in the n-wide centre iff s0 <= s < s1
+  const int s0 = band.lo / TPT, s1 = (band.lo + band.n) / TPT;
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // source overwrites: skip the read
-  if (!gen) {
+  if (band.n && !INV) {  // rows of the n x n source, zero outside its columns
+    const size_t np = (size_t)band.n * band.n;
+    const float* sre = band.src + (size_t)f * 2 * np + (size_t)(row - band.lo) * band.n + u -
+                       band.lo;
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+      const bool in = s >= s0 && s < s1;
+      xr[s] = in ? sre[s * TPT] : 0.f;
+      xi[s] = in ? sre[np + s * TPT] : 0.f;
+    }
+  } else if (!gen) {
 #pragma unroll
     for (int s = 0; s < E; ++s) {
       xr[s] = fre[s * TPT];
@@ -311,6 +323,17 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
 #pragma unroll
     for (int h = 0; h < E; h += 8)
       pix_apply_n<8>(epi, ke, row, u + h * TPT, 0, TPT, N, N, xr + h, xi + h);
+  }
+  if (band.n && INV) {  // the centre n columns straight to the n x n field
+    const size_t np = (size_t)band.n * band.n;
+    float* dre = band.dst + (size_t)f * 2 * np + (size_t)(row - band.lo) * band.n + u - band.lo;
+#pragma unroll
+    for (int s = 0; s < E; ++s)
+      if (s >= s0 && s < s1) {
+        dre[s * TPT] = xr[s];
+        dre[np + s * TPT] = xi[s];
+      }
+    return;
   }
 #pragma unroll
   for (int s = 0; s < E; ++s) {
@@ -383,7 +406,7 @@ int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, d
 template <int N, int E, int MODE, int COLS>
 __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS>::MIN_BLOCKS)
     k_fft_cols(float* __restrict__ field, const float2* __restrict__ tw,
-               const __grid_constant__ FresnelArgs fa) {
+               const __grid_constant__ FresnelArgs fa, int band_lo, int band_n) {
   using CF = ColCfg<N, E, COLS>;
   using A = ColAddr<COLS, E>;
   constexpr int TPT = CF::TPT;
@@ -398,10 +421,14 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS
   float* fre = field + (size_t)f * 2 * plane + (size_t)u * N + c0 + t;
   float* fim = fre + plane;
   float xr[E], xi[E];
+  // band: rows u + s N/E outside [band_lo, band_lo + band_n) are zero on
+  // input and not stored (band_n = 0: every row)
+  const int s0 = band_n ? band_lo / TPT : 0, s1 = band_n ? (band_lo + band_n) / TPT : E;
 #pragma unroll
   for (int s = 0; s < E; ++s) {
-    xr[s] = fre[(size_t)s * TPT * N];
-    xi[s] = fim[(size_t)s * TPT * N];
+    const bool in = s >= s0 && s < s1;
+    xr[s] = in ? fre[(size_t)s * TPT * N] : 0.f;
+    xi[s] = in ? fim[(size_t)s * TPT * N] : 0.f;
   }
   fft_regs<N, E, MODE == 1, A>(xr, xi, re, im, t, u, tw);
   if (MODE == 2) {
@@ -436,10 +463,11 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS
     fft_regs<N, E, true, A>(xr, xi, re, im, t, u, tw);
   }
 #pragma unroll
-  for (int s = 0; s < E; ++s) {
-    fre[(size_t)s * TPT * N] = xr[s];
-    fim[(size_t)s * TPT * N] = xi[s];
-  }
+  for (int s = 0; s < E; ++s)
+    if (s >= s0 && s < s1) {
+      fre[(size_t)s * TPT * N] = xr[s];
+      fim[(size_t)s * TPT * N] = xi[s];
+    }
 }
 
 template <typename K>
@@ -453,19 +481,22 @@ static int prep_smem(K kern, size_t bytes) {
 
 template <int N, int E, int COLS>
 static int launch_cols(cudaStream_t st, float* field, int F, int mode, const float2* tw,
-                       const FresnelArgs* fa) {
+                       const FresnelArgs* fa, const FftBand& band) {
   using CC = ColCfg<N, E, COLS>;
   const int grid = F * (N / COLS);
   int rc;
   if (mode == 2) {
     if ((rc = prep_smem(k_fft_cols<N, E, 2, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, E, 2, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa);
+    k_fft_cols<N, E, 2, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa, band.lo,
+                                                                   band.n);
   } else if (mode == 1) {
     if ((rc = prep_smem(k_fft_cols<N, E, 1, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, E, 1, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    k_fft_cols<N, E, 1, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{}, 0,
+                                                                   0);
   } else {
     if ((rc = prep_smem(k_fft_cols<N, E, 0, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, E, 0, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{});
+    k_fft_cols<N, E, 0, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{}, 0,
+                                                                   0);
   }
   CSG_LAUNCH_CHECK();
   return CSG_OK;
@@ -473,16 +504,17 @@ static int launch_cols(cudaStream_t st, float* field, int F, int mode, const flo
 
 template <int N, int E>
 static int launch_rows(cudaStream_t st, float* field, int F, bool inv, float scale,
-                       const float2* tw, const PixOps& p, const PixOps& e, const FieldInfo& fi) {
+                       const float2* tw, const PixOps& p, const PixOps& e, const FieldInfo& fi,
+                       const FftBand& band) {
   using RC = RowCfg<N, E>;
-  const int grid = F * (N / RC::ROWS);
+  const int grid = F * ((band.n ? band.n : N) / RC::ROWS);
   int rc;
   if (inv) {
     if ((rc = prep_smem(k_fft_rows<N, E, true>, RC::SMEM))) return rc;
-    k_fft_rows<N, E, true><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
+    k_fft_rows<N, E, true><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi, band);
   } else {
     if ((rc = prep_smem(k_fft_rows<N, E, false>, RC::SMEM))) return rc;
-    k_fft_rows<N, E, false><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi);
+    k_fft_rows<N, E, false><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi, band);
   }
   CSG_LAUNCH_CHECK();
   return CSG_OK;
@@ -500,29 +532,32 @@ static int env_choice(const char* name, std::initializer_list<int> allowed) {
 
 template <int N>
 static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const FresnelArgs* fa,
-                   const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw) {
+                   const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw,
+                   const FftBand& band) {
   cudaStream_t st = ctx->stream;
   const float inv_scale = 1.f / ((float)N * (float)N);
-  const double pass_bytes = (double)F * N * N * 16.0;
+  // a band-limited pass moves n rows of N (the first and last touch n x n)
+  const double pass_bytes = (double)F * N * (band.n ? band.n : N) * 16.0;
+  const double edge_bytes = band.n ? (double)F * band.n * (N + band.n) * 8.0 : pass_bytes;
   const PixOps none;
-  static const int e_over = env_choice("CSG_FFT_E", {16});
-  static const int c_over = env_choice("CSG_FFT_COLS", {4, 16});
+  const bool e16 = (N == 1024) && !band.n && env_choice("CSG_FFT_E", {16}) == 16;
+  const int c_over = env_choice("CSG_FFT_COLS", {4, 16});
   int rc;
   auto rows = [&](bool inv, float scale, const PixOps& p, const PixOps& e) -> int {
     const bool gen = p.n && p.kind[0] == OP_SOURCE;
-    ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, pass_bytes * (gen ? 0.5 : 1.0));
+    ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, edge_bytes * (gen ? 0.5 : 1.0));
     if constexpr (N == 1024)
-      if (e_over == 16) return launch_rows<N, 16>(st, field, F, inv, scale, tw, p, e, fi);
-    return launch_rows<N, default_e(N)>(st, field, F, inv, scale, tw, p, e, fi);
+      if (e16) return launch_rows<N, 16>(st, field, F, inv, scale, tw, p, e, fi, band);
+    return launch_rows<N, default_e(N)>(st, field, F, inv, scale, tw, p, e, fi, band);
   };
   auto cols = [&](int mode) -> int {
     ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, pass_bytes);
     if constexpr (N == 1024) {
-      if (e_over == 16) return launch_cols<N, 16, 8>(st, field, F, mode, tw, fa);
-      if (c_over == 4) return launch_cols<N, 32, 4>(st, field, F, mode, tw, fa);
-      if (c_over == 16) return launch_cols<N, 32, 16>(st, field, F, mode, tw, fa);
+      if (e16) return launch_cols<N, 16, 8>(st, field, F, mode, tw, fa, band);
+      if (c_over == 4) return launch_cols<N, 32, 4>(st, field, F, mode, tw, fa, band);
+      if (c_over == 16) return launch_cols<N, 32, 16>(st, field, F, mode, tw, fa, band);
     }
-    return launch_cols<N, default_e(N), default_cols(N)>(st, field, F, mode, tw, fa);
+    return launch_cols<N, default_e(N), default_cols(N)>(st, field, F, mode, tw, fa, band);
   };
   if (fa) {
     if ((rc = rows(false, 1.f, pro, none))) return rc;
@@ -540,28 +575,42 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
   return CSG_OK;
 }
 
+bool fft_band_supported(int N, int lo, int n) {
+  const int E = default_e(N), TPT = N / E, rows = 256 / TPT > 0 ? 256 / TPT : 1;
+  return n > 0 && lo >= 0 && lo + n <= N && lo % TPT == 0 && n % TPT == 0 && n % rows == 0;
+}
+
 // 2-D FFT or Fresnel propagation of F square N x N fields with fused element
 // ops (pro before the transform, epi after it).
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
-                const PixOps& pro, const PixOps& epi, const FieldInfo& fi) {
+                const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const FftBand* band) {
   CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
             "FFT size must be a power of two in [64, 4096]");
   CSG_CHECK(F > 0 && (long long)F * n < (1LL << 31), CSG_E_SHAPE, "FFT: bad field count");
+  FftBand bd;
+  if (band) {
+    CSG_CHECK(fa && !pro.n && !epi.n && band->src && band->dst &&
+                  fft_band_supported(n, band->lo, band->n),
+              CSG_E_ARG, "FFT: unsupported band-limited transform");
+    bd = *band;
+  }
   cudaStream_t st = ctx->stream;
   const float2* tw = twiddles(ctx->device, n, st);
   CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
   const double pass_bytes = (double)F * n * n * 16.0;
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // the first pass only writes
-  ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0,
-               pass_bytes * ((fa ? 3.0 : 2.0) - (gen ? 0.5 : 0.0)));
+  const double total = band ? (double)F * band->n * (n + band->n) * 16.0 +
+                                  (double)F * n * band->n * 16.0
+                            : pass_bytes * ((fa ? 3.0 : 2.0) - (gen ? 0.5 : 0.0));
+  ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0, total);
   switch (n) {
-    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw);
-    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw);
-    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw);
-    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw);
-    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw);
-    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw);
-    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw);
+    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
+    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
+    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
+    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
+    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
+    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
+    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
   }
 }
 

@@ -109,61 +109,85 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
 
 // Data split: planar fp32 [F][2][R][C] -> (element ops `pre`) -> (times a
 // complex multiplier [n_mul][2][R][C] chosen by mul_idx[f]) -> bf16
-// [F][3][2][R][C]. Four pixels per thread (C is a multiple of 8); grid.y is
-// the field; field f reads input field in_idx[f] (f when in_idx is null).
-// The input is the R x C window at (r0, c0) of fields whose planes are
-// RT x PT (the element ops see the field's own coordinates and size).
+// [F][3][2][R][C]. Eight pixels of one row per thread (C is a multiple of
+// 8); grid.y is the field; field f reads input field in_idx[f] (f when
+// in_idx is null). The input is the R x C window at (r0, c0) of fields whose
+// planes are RT x PT (the element ops see the field's own coordinates and
+// size). The parts come from paired bf16 conversions (two values per
+// instruction), bit-identical to split3.
+__device__ __forceinline__ void split3_pair(float x0, float x1, uint32_t& h0, uint32_t& h1,
+                                            uint32_t& h2) {
+  const __nv_bfloat162 a = __floats2bfloat162_rn(x0, x1);
+  const float2 fa = __bfloat1622float2(a);
+  const float r0 = x0 - fa.x, r1 = x1 - fa.y;
+  const __nv_bfloat162 b = __floats2bfloat162_rn(r0, r1);
+  const float2 fb = __bfloat1622float2(b);
+  const __nv_bfloat162 c = __floats2bfloat162_rn(r0 - fb.x, r1 - fb.y);
+  h0 = *reinterpret_cast<const uint32_t*>(&a);
+  h1 = *reinterpret_cast<const uint32_t*>(&b);
+  h2 = *reinterpret_cast<const uint32_t*>(&c);
+}
+
 __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int R,
                               int C, int r0, int c0, int RT, int PT,
                               const float* __restrict__ mul,
-                              const int* __restrict__ mul_idx, PixOps pre, FieldInfo fi,
+                              const int* __restrict__ mul_idx,
+                              const __grid_constant__ PixOps pre, const __grid_constant__ FieldInfo fi,
                               const int* __restrict__ in_idx) {
+  __shared__ PixConsts shk;
   const int f = blockIdx.y;
   const int plane = R * C;
   const size_t fplane = (size_t)RT * PT;
   PixConsts k;
-  if (pre.n) pix_consts(pre, fi, f, RT, PT, k);
+  if (pre.n) pix_consts_cta(pre, fi, f, RT, PT, k, &shk);
   const float* ire = in + (size_t)(in_idx ? in_idx[f] : f) * 2 * fplane;
   const float* iim = ire + fplane;
   const float* mre = mul ? mul + (size_t)mul_idx[f] * 2 * plane : nullptr;
-  const int nv = plane / 4;
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
-    const int e0 = 4 * v;
-    const int r = e0 / C, c = e0 % C;
+  const int groups = C / 8;
+  const int ng = R * groups;
+  for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ng; gi += gridDim.x * blockDim.x) {
+    const int r = gi / groups, c = (gi - r * groups) * 8;
     const size_t g = (size_t)(r0 + r) * PT + c0 + c;  // 16-byte aligned: c0, C, PT % 4 == 0
-    const float4 a4 = *reinterpret_cast<const float4*>(ire + g);
-    const float4 b4 = *reinterpret_cast<const float4*>(iim + g);
-    float xr[4] = {a4.x, a4.y, a4.z, a4.w}, xi[4] = {b4.x, b4.y, b4.z, b4.w};
-    if (pre.n) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) pix_apply(pre, k, r0 + r, c0 + c + q, RT, PT, xr[q], xi[q]);
+    float xr[8], xi[8];
+    {
+      const float4 a0 = *reinterpret_cast<const float4*>(ire + g);
+      const float4 a1 = *reinterpret_cast<const float4*>(ire + g + 4);
+      const float4 b0 = *reinterpret_cast<const float4*>(iim + g);
+      const float4 b1 = *reinterpret_cast<const float4*>(iim + g + 4);
+      xr[0] = a0.x, xr[1] = a0.y, xr[2] = a0.z, xr[3] = a0.w;
+      xr[4] = a1.x, xr[5] = a1.y, xr[6] = a1.z, xr[7] = a1.w;
+      xi[0] = b0.x, xi[1] = b0.y, xi[2] = b0.z, xi[3] = b0.w;
+      xi[4] = b1.x, xi[5] = b1.y, xi[6] = b1.z, xi[7] = b1.w;
     }
+    if (pre.n) pix_apply_n<8>(pre, k, r0 + r, c0 + c, 0, 1, RT, PT, xr, xi);
+    const int e0 = r * C + c;
     if (mre) {
-      const float4 m4 = reinterpret_cast<const float4*>(mre)[v];
-      const float4 n4 = reinterpret_cast<const float4*>(mre + plane)[v];
-      const float mr[4] = {m4.x, m4.y, m4.z, m4.w}, mi[4] = {n4.x, n4.y, n4.z, n4.w};
+      float mr[8], mi[8];
+      const float4* m4 = reinterpret_cast<const float4*>(mre + e0);
+      const float4* n4 = reinterpret_cast<const float4*>(mre + plane + e0);
+      const float4 m0 = m4[0], m1 = m4[1], q0 = n4[0], q1 = n4[1];
+      mr[0] = m0.x, mr[1] = m0.y, mr[2] = m0.z, mr[3] = m0.w;
+      mr[4] = m1.x, mr[5] = m1.y, mr[6] = m1.z, mr[7] = m1.w;
+      mi[0] = q0.x, mi[1] = q0.y, mi[2] = q0.z, mi[3] = q0.w;
+      mi[4] = q1.x, mi[5] = q1.y, mi[6] = q1.z, mi[7] = q1.w;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < 8; ++q) {
         const float tr = xr[q] * mr[q] - xi[q] * mi[q];
         xi[q] = xr[q] * mi[q] + xi[q] * mr[q];
         xr[q] = tr;
       }
     }
-    __nv_bfloat16 a[3][4], b[3][4];
+    uint32_t hr[3][4], hi[3][4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      split3(xr[q], a[0][q], a[1][q], a[2][q]);
-      split3(xi[q], b[0][q], b[1][q], b[2][q]);
+      split3_pair(xr[2 * q], xr[2 * q + 1], hr[0][q], hr[1][q], hr[2][q]);
+      split3_pair(xi[2 * q], xi[2 * q + 1], hi[0][q], hi[1][q], hi[2][q]);
     }
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
       __nv_bfloat16* o = out + ((size_t)(f * 3 + p) * 2) * plane + e0;
-      *reinterpret_cast<uint2*>(o) = make_uint2(
-          (uint32_t)__bfloat16_as_ushort(a[p][0]) | ((uint32_t)__bfloat16_as_ushort(a[p][1]) << 16),
-          (uint32_t)__bfloat16_as_ushort(a[p][2]) | ((uint32_t)__bfloat16_as_ushort(a[p][3]) << 16));
-      *reinterpret_cast<uint2*>(o + plane) = make_uint2(
-          (uint32_t)__bfloat16_as_ushort(b[p][0]) | ((uint32_t)__bfloat16_as_ushort(b[p][1]) << 16),
-          (uint32_t)__bfloat16_as_ushort(b[p][2]) | ((uint32_t)__bfloat16_as_ushort(b[p][3]) << 16));
+      *reinterpret_cast<uint4*>(o) = make_uint4(hr[p][0], hr[p][1], hr[p][2], hr[p][3]);
+      *reinterpret_cast<uint4*>(o + plane) = make_uint4(hi[p][0], hi[p][1], hi[p][2], hi[p][3]);
     }
   }
 }
@@ -471,7 +495,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
   {
     ProfScope ps(ctx, "mft_split", 0, F * m->ny * m->nx * (8.0 + 12.0 + (in_mul ? 8.0 : 0.0)));
     CSG_CHECK(n_fields < 65536, CSG_E_SHAPE, "csg_mft_execute: too many fields in one call");
-    dim3 grid(grid_for((long long)m->ny * m->nx / 4, 256, 1024), n_fields);
+    dim3 grid(grid_for((long long)m->ny * m->nx / 8, 256, 1024), n_fields);
     k_split_field<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, inw.r0, inw.c0, inw.rows,
                                         inw.pitch, in_mul, mul_idx, pre, fi, in_idx);
     CSG_LAUNCH_CHECK();

@@ -260,10 +260,28 @@ int build_phasor_table(cudaStream_t st, const float* sag, int R, int C, const do
 int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, double z,
                         double ap_rad, float2* out);
 
+// Band-limited padded transform (with fa only): the n x n field src sits at
+// rows and columns [lo, lo + n) of zero-padded N x N fields. The first row
+// pass transforms only those rows, reading them straight from src (the zero
+// columns are generated); the column pass loads and stores only the band's
+// rows (the others are zero on input and unused on output); the last row
+// pass transforms the band's rows and writes their centre columns straight
+// to dst (n x n). lo and n must be multiples of the transform's threads per
+// row and column.
+struct FftBand {
+  int lo = 0, n = 0;
+  const float* src = nullptr;
+  float* dst = nullptr;
+};
+
 // 2-D FFT (direction -1 / +1) or, with fa, Fresnel propagation of F square
 // N x N fields with element ops fused before (pro) and after (epi).
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
-                const PixOps& pro, const PixOps& epi, const FieldInfo& fi);
+                const PixOps& pro, const PixOps& epi, const FieldInfo& fi,
+                const FftBand* band = nullptr);
+// Whether fft2d_fused can run an N-point padded transform band-limited to
+// [lo, lo + n).
+bool fft_band_supported(int N, int lo, int n);
 
 // A window of a field: rows x cols of the transform start at (r0, c0) of
 // planes that are `rows` x `pitch`.
