@@ -489,9 +489,9 @@ def main():
 
 # dram__bytes_read.sum + dram__bytes_write.sum per k_split_gemm launch,
 # averaged over the six GEMM launches of one step, keyed by fields per step:
-# an ncu capture at 32 fields (1222.8 MB per step) scaled by the field count
+# an ncu capture at 32 fields (1157.7 MB per step) scaled by the field count
 # (profiles/k_split_gemm_piaacmc1024_32fields.md).
-TRAFFIC: dict = {64: 407.6e6, 32: 203.8e6}
+TRAFFIC: dict = {64: 385.9e6, 32: 192.9e6}
 
 if __name__ == "__main__":
     sys.exit(main())
