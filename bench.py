@@ -8,12 +8,14 @@ on-axis source), each propagated through the full element walk
 candidate. Metric: field propagations per second.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                  [--workload piaacmc|plain_lyot|broadband]
+                  [--workload piaacmc|plain_lyot|broadband|de]
 
 The other workloads measure the plain Lyot coronagraph (512^2 pupil,
 2048^2 padded-FFT occulter, 128^2 image; a batch of off-axis sources) and
 the broadband batch (2048^2 segmented pupil + DM, 11 wavelengths x 3
-sources onto ragged 460^2..540^2 images in one launch).
+sources onto ragged 460^2..540^2 images in one launch) and differential
+evolution by full propagation (1261 hexes, 5 wavelengths, population 64:
+one generation = 320 fields, replayed as one CUDA graph).
 
 Under torchrun each rank runs its own batch (candidates are independent:
 weak scaling, no data-path collective); timing is the max over ranks.
@@ -282,7 +284,49 @@ def setup_broadband(args, ctx, W, cg, rank):
     return wl
 
 
-SETUP = {"piaacmc": setup_piaacmc, "plain_lyot": setup_plain_lyot, "broadband": setup_broadband}
+def setup_de(args, ctx, W, cg, rank):
+    """Differential evolution by full propagation: 1261 hexes (20 rings), 5
+    wavelengths over a 10% band at 650 nm, population 64, the PIAACMC chain at
+    1024^2; one step is one generation (trial generation, 320 propagated
+    fields, contrast per candidate, greedy selection) replayed as one CUDA
+    graph."""
+    import torch
+    from csim_gb300 import optimize as opt
+    wl = Workload()
+    lam = tuple(np.linspace(650e-9 * 0.95, 650e-9 * 1.05, 5))
+    spec = W.PiaacmcSpec(n_rings=20, wavelengths=lam, sag_range=0.6e-6)
+    P = 64
+    cor, inp = W.build_piaacmc(ctx, spec, precision=args.precision, support_crop=not args.no_crop)
+    reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 2.0, 8.0)
+    obj = opt.PropagatedObjective(cor, reg, P, use_graph=False)
+    cfg = opt.DEConfig(populationSize=P, globalBounds=(-0.6e-6, 0.6e-6),
+                       initBounds=(-0.6e-6, 0.6e-6), fWeight=0.7, crossoverProb=0.9,
+                       seed=11 + rank)
+    de = opt.DifferentialEvolution(ctx, spec.n_hex, cfg)
+    de.set_trial_buffer(obj.sags)
+    de.initialise(np.zeros(spec.n_hex), 1.0, obj)
+    stream = torch.cuda.current_stream()
+    wl.gen = opt.GraphedGeneration(de, "deRand1", obj, stream)
+    wl.de, wl.obj = de, obj
+    wl.cor, wl.inp, wl.reg, wl.B, wl.spec = cor, inp, None, obj.per * P, spec
+    wl.per_group = obj.per
+    wl.cmax = obj.cmax
+    # end to end: the population comes from the host every generation and
+    # the objective values go back
+    wl.host_in, wl.dev_in = de.pop.cpu(), de.pop
+    wl.cpu = None  # the CPU restatement of propagation is the piaacmc workload's baseline
+    wl.bound = "tensor"
+    wl.config = {"workload": "de-piaacmc-1024: DE/rand/1 (F 0.7, CR 0.9), population 64, "
+                             "1261 hexes (20 rings, U(+-0.6um)), 5 lambda (10% at 650 nm), one "
+                             "generation = 320 propagated fields + selection, CUDA graph",
+                 "fields_per_step": wl.B, "n": spec.n, "n_hex": spec.n_hex, "population": P,
+                 "precision": f"bf16x{args.precision}",
+                 "l2": "working set > L2 (320 fields x 8 MB)"}
+    return wl
+
+
+SETUP = {"piaacmc": setup_piaacmc, "plain_lyot": setup_plain_lyot, "broadband": setup_broadband,
+         "de": setup_de}
 
 
 def main():
@@ -293,7 +337,7 @@ def main():
     ap.add_argument("--fields", type=int, default=64)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="piaacmc", choices=sorted(SETUP),
-                    help="piaacmc (headline), plain_lyot, broadband")
+                    help="piaacmc (headline), plain_lyot, broadband, de")
     ap.add_argument("--precision", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-crop", action="store_true",
@@ -326,6 +370,9 @@ def main():
         contrast = torch.zeros(n_groups, dtype=torch.float64, device="cuda")
 
         def step():
+            if hasattr(wl, "gen"):  # one DE generation, replayed as one graph
+                wl.gen.replay()
+                return wl.de.f
             img = cor.execute(calibrating=False, use_graph=True)
             if wl.reg is not None:
                 ctx.region_reduce(img, wl.per_group, wl.reg.pix, mode=0, scale=1.0 / wl.cmax,
@@ -338,10 +385,13 @@ def main():
         # kernels per step, counted on an eager (non-graph) step after the
         # warm-up; graph replays launch exactly these kernels
         n0 = _lib.api["csg_launch_count"]()
-        img = cor.execute(use_graph=False)
-        if wl.reg is not None:
-            ctx.region_reduce(img, wl.per_group, wl.reg.pix, mode=0, scale=1.0 / wl.cmax,
-                              out=contrast)
+        if hasattr(wl, "gen"):
+            wl.de.generation("deRand1", wl.obj)
+        else:
+            img = cor.execute(use_graph=False)
+            if wl.reg is not None:
+                ctx.region_reduce(img, wl.per_group, wl.reg.pix, mode=0, scale=1.0 / wl.cmax,
+                                  out=contrast)
         launches_per_step = _lib.api["csg_launch_count"]() - n0
         ctx.sync()
 
@@ -380,12 +430,12 @@ def main():
     # ---- e2e through the C ABI with host buffers (pinned), every step: H2D
     # of the step's input (the candidates' sags, or the sources' offsets), the
     # walk, the contrast, D2H of the final image fields and the contrasts.
-    img0 = cor.execute(use_graph=True)
+    img0 = step()
     host_in = wl.host_in.pin_memory()
-    host_img = torch.empty(img0.shape, dtype=torch.float32).pin_memory()
+    host_img = torch.empty(img0.shape, dtype=img0.dtype).pin_memory()
     host_con = torch.empty(n_groups, dtype=torch.float64).pin_memory()
     h2d = host_in.numel() * host_in.element_size()
-    d2h = host_img.numel() * 4 + (n_groups * 8 if wl.reg is not None else 0)
+    d2h = host_img.numel() * host_img.element_size() + (n_groups * 8 if wl.reg is not None else 0)
     with torch.cuda.stream(stream):
         def e2e_step():
             _lib.call("csg_memcpy_h2d", ctx.h, C.c_void_p(wl.dev_in.data_ptr()),
@@ -396,7 +446,7 @@ def main():
                 wl.dev_split[1].copy_(wl.dev_in[half:])
             img = step()
             _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_img.data_ptr()),
-                      C.c_void_p(img.data_ptr()), host_img.numel() * 4)
+                      C.c_void_p(img.data_ptr()), host_img.numel() * host_img.element_size())
             if wl.reg is not None:
                 _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_con.data_ptr()),
                           C.c_void_p(contrast.data_ptr()), n_groups * 8)
@@ -462,7 +512,7 @@ def main():
         roofline["fresnel_frac_hbm"] = roofline["fresnel_gbs"] / hbm_peak
 
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu and wl.cpu is not None:
         v, n, dt = wl.cpu(15.0, 32)
         cpu = {"value": v, "unit": "fields/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{n} fields of the same workload in {dt:.1f} s ({wl.cpu_sample})"}

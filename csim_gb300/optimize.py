@@ -90,6 +90,34 @@ class PropagatedObjective:
 STRATEGIES = {"deRand1": 0, "deLocalToBest1": 1, "eitherOr": 2}
 
 
+class GraphedGeneration:
+    """One DE generation (trial generation, the objective's launches, greedy
+    selection) captured once as a CUDA graph on `stream` and replayed: the
+    generation counter and the random streams live on the device, so every
+    replay is the next generation. The objective must launch only (no host
+    synchronisation or allocation), e.g. PropagatedObjective(use_graph=False)
+    writing the trials in place through DifferentialEvolution.set_trial_buffer."""
+
+    def __init__(self, de: "DifferentialEvolution", strategy: str, objective,
+                 stream: torch.cuda.Stream):
+        self.de, self.graph = de, torch.cuda.CUDAGraph()
+        code = STRATEGIES[strategy]
+        cfg = de.cfg
+
+        def body():
+            call("csg_de_generate", de.h, code, cfg.fWeight, cfg.crossoverProb)
+            objective(de.trial, de.f_trial)
+            call("csg_de_select", de.h, 0)
+        with torch.cuda.stream(stream):
+            body()  # eager warm-up: first-use set-up happens outside the capture
+            stream.synchronize()
+        with torch.cuda.graph(self.graph, stream=stream):
+            body()
+
+    def replay(self):
+        self.graph.replay()
+
+
 @dataclass
 class DEConfig:
     """differentialEvolutionOptimizer settings (differentialEvolutionOptimizer.cpp:66-197)."""

@@ -110,3 +110,52 @@ def test_de_minimises_response_objective(ctx):
     assert abs(ref - best) / best < 1e-3      # the device value is the true objective
     assert best < 0.5 * f0                    # and it improved on the flat mask
     d.close()
+
+
+def test_graphed_generation_matches_eager(ctx):
+    """DE by full propagation: generations replayed from one captured CUDA
+    graph (trial generation, the chain walk, contrast reduction, selection)
+    give exactly the populations and values of eagerly launched generations."""
+    import torch
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import optimize as opt
+    from csim_gb300.workloads import PiaacmcSpec, build_piaacmc
+    spec = PiaacmcSpec(n=256, beam_px=200, wavelengths=(640e-9, 660e-9), S=128,
+                       fpm_sampling=8.0, n_rings=3, n_sub=8, design_size=512, n_out_fov=32.0,
+                       spl=4.0)
+    stream = torch.cuda.Stream()
+    ctx.bind_stream(stream)
+    results = []
+    try:
+        _run_graph_vs_eager(ctx, spec, stream, results, cg, opt, build_piaacmc)
+    finally:  # the session context goes back to torch's current stream
+        ctx.bind_stream(torch.cuda.current_stream())
+    (p0, f0, g0), (p1, f1, g1) = results
+    assert g0 == g1
+    assert torch.equal(p0, p1) and torch.equal(f0, f1)
+
+
+def _run_graph_vs_eager(ctx, spec, stream, results, cg, opt, build_piaacmc):
+    import torch
+    with torch.cuda.stream(stream):
+        for graphed in (False, True):
+            cor, inp = build_piaacmc(ctx, spec)
+            reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 2.0, 8.0)
+            P = 16
+            obj = opt.PropagatedObjective(cor, reg, P, use_graph=False)
+            cfg = opt.DEConfig(populationSize=P, globalBounds=(-5e-7, 5e-7),
+                               initBounds=(-5e-7, 5e-7), fWeight=0.7, crossoverProb=0.9, seed=9)
+            de = opt.DifferentialEvolution(ctx, inp["hex_x"].size, cfg)
+            de.set_trial_buffer(obj.sags)
+            de.initialise(np.zeros(inp["hex_x"].size), 1.0, obj)
+            if graphed:
+                g = opt.GraphedGeneration(de, "deRand1", obj, stream)  # runs one generation
+                for _ in range(3):
+                    g.replay()
+            else:
+                for _ in range(4):
+                    de.generation("deRand1", obj)
+            stream.synchronize()
+            results.append((de.pop.clone(), de.f.clone(), de.stats()[3]))
+            de.close()
+            cor.close()
