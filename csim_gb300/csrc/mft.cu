@@ -62,6 +62,25 @@ int make_map(CUtensorMap* m, const void* base, int k, int rows, long long planes
   return CSG_OK;
 }
 
+// 3-D fp32 map of an output window for the GEMM epilogue: (cols, rows,
+// planes) with origin base, row pitch `pitch` and plane stride
+// plane_rows * pitch elements; box (32, 32, 1), 128B swizzle. Returns false
+// (and leaves m unused) when the window breaks a TMA rule: the origin must
+// be 16-byte aligned and the pitch a multiple of 4 elements.
+bool make_map_f32_out(CUtensorMap* m, float* base, int cols, int rows, long long planes,
+                      int pitch, int plane_rows) {
+  if (get_encoder() != CSG_OK) return false;
+  if (((uintptr_t)base & 15) != 0 || (pitch & 3) != 0 || cols <= 0 || rows <= 0) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)pitch * 4, (cuuint64_t)pitch * 4 * plane_rows};
+  cuuint32_t box[3] = {32, 32, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 // ------------------------------------------------------------ kernels
 // Operator generator: op[slot][part][sel][r][k] for r < rows, k < K.
 // value = pref_s * exp(sgn 2 pi i frac(cout_r cin_k / lf_s)); sel 0/1/2 = re/im/-im.
@@ -192,20 +211,15 @@ __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __res
   }
 }
 
-// Product terms of the three-way split, largest first.
+// The GEMM issues a prefix of its fixed product order (tc::term_a, tc::term_b):
+// all six products for bf16x6, the three largest for bf16x3.
 void terms_for(int precision, tc::Params& p) {
-  static const int a6[6] = {0, 0, 1, 0, 1, 2};
-  static const int b6[6] = {0, 1, 0, 2, 1, 0};
   p.n_terms = precision == CSG_PREC_BF16X3 ? 3 : 6;
-  for (int i = 0; i < p.n_terms; ++i) {
-    p.term_a[i] = a6[i];
-    p.term_b[i] = b6[i];
-  }
 }
 
 template <int BN, bool OP_IS_A, int EPI>
 static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Params& p,
-                       int grid, cudaStream_t st) {
+                       int grid, cudaStream_t st, const CUtensorMap* o = nullptr) {
   auto kern = tc::k_split_gemm<BN, OP_IS_A, EPI>;
   constexpr size_t smem = tc::smem_bytes<BN>();
   static bool attr_set = false;  // per template instance
@@ -213,7 +227,9 @@ static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Par
     CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = true;
   }
-  kern<<<grid, tc::THREADS, smem, st>>>(a, b, p);
+  CSG_CHECK(o || !p.tma_out, CSG_E_ARG, "GEMM: TMA output without a tensor map");
+  static const CUtensorMap unused{};  // read only when p.tma_out
+  kern<<<grid, tc::THREADS, smem, st>>>(a, b, o ? *o : unused, p);
   CSG_LAUNCH_CHECK();
   return CSG_OK;
 }
@@ -555,10 +571,15 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.out_c0 = outw.c0;
     p.accumulate = accumulate;
     p.status = ctx->status;
+    CUtensorMap to;
+    p.tma_out = make_map_f32_out(&to, out + (size_t)outw.r0 * outw.pitch + outw.c0, m->no, m->mo,
+                                 (long long)n_fields * 2, outw.pitch, outw.rows)
+                    ? 1
+                    : 0;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->mo * m->no * m->ny);
-    rc = bn1 == 64 ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st)
-                   : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st);
+    rc = bn1 == 64 ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st, &to)
+                   : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st, &to);
     if (rc) return rc;
   }
   return CSG_OK;

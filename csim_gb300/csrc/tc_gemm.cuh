@@ -35,9 +35,7 @@ struct Params {
   int rows_valid;   // stage 1: Ny (data rows); stage 2: Mo (operator rows per comp)
   int cols_valid;   // No (valid output columns)
   int k_blocks;     // ceil(K / BK)
-  int n_terms;
-  int term_a[8];
-  int term_b[8];
+  int n_terms;      // products of the split issued (6: bf16x6, 3: bf16x3; see term_a)
   const int* slot;  // [n_fields] operator slot of each field
   void* out;
   int out_rows;     // EPI_T_SPLIT: No (rows of T^T); EPI_F32: Mo
@@ -47,6 +45,11 @@ struct Params {
   // stored at (out_r0 + v) * out_pitch + out_c0 + u of planes that are
   // out_plane_rows x out_pitch (a sub-rectangle of a larger field).
   int out_pitch, out_plane_rows, out_r0, out_c0;
+  // EPI_F32 through the output tensor map (fp32, origin at the window's
+  // (out_r0, out_c0), box 32 x 32, 128B swizzle): tiles are staged in the
+  // free operand ring and written by TMA stores, or by TMA add-reductions
+  // when accumulating. 0: per-thread stores.
+  int tma_out;
   int* status;
 };
 
@@ -94,6 +97,37 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, ui
       " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(tm)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
       : "memory");
+}
+
+// Shared -> global tile store, or element-wise fp32 add into global (the
+// reduction is applied at L2), of one box at (x, y, z); bulk-group completion.
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* tm, const void* src, int x, int y,
+                                             int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+          reinterpret_cast<uint64_t>(tm)),
+      "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+__device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap* tm, const void* src, int x,
+                                                  int y, int z) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group"
+      " [%0, {%2, %3, %4}], [%1];" ::"l"(reinterpret_cast<uint64_t>(tm)),
+      "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Waits until the committed bulk copies have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// Orders this thread's generic-proxy shared-memory writes before later
+// async-proxy (TMA) reads.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() {
@@ -167,8 +201,9 @@ __device__ __forceinline__ int sel_plane(int d, int c) {
 // the three-way split are therefore grouped by magnitude (part indices
 // pa + pb): group 0 (hi x hi) goes to a fresh tensor-memory slot every K
 // block (two slots rotate) and eight drain warps add each finished slot into
-// fp32 registers with round-to-nearest adds while the next block is
-// multiplied; group 1 (hi x mid, mid x hi, 2^-8 of the result) and group 2
+// fp32 registers with round-to-nearest adds while the rest of the block and
+// the next block are multiplied (each block issues group 0 first and commits
+// its slot before the smaller groups); group 1 (hi x mid, mid x hi, 2^-8 of the result) and group 2
 // (the 2^-16 terms) accumulate over the whole K range in two persistent
 // slots, where the truncation is relative to their own small magnitude, and
 // are added once at the end.
@@ -192,6 +227,7 @@ struct Cfg {
   static constexpr int STAGES = BN == 128 ? 2 : 3;  // 192 KB / 216 KB of operand ring
   static constexpr int TMEM_COLS = 4 * BN;          // group 1, group 2, two rotating slots
   static constexpr int COLS_PER_WARP = BN / 2;      // two warps share a lane quadrant
+  static constexpr int BN_ = BN;
   static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 512;
 };
 
@@ -215,12 +251,48 @@ __device__ __forceinline__ void drain_add(uint32_t taddr, float* acc) {
   }
 }
 
+// Split products in issue order: (A part, B part), hi x hi first, then
+// the 2^-8 group and the 2^-16 group. n_terms = 6 (bf16x6) or 3 (bf16x3)
+// takes a prefix.
+// (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
+__host__ __device__ constexpr int term_a(int i) { return i == 2 || i == 4 ? 1 : (i == 5 ? 2 : 0); }
+__host__ __device__ constexpr int term_b(int i) { return i == 1 || i == 4 ? 1 : (i == 3 ? 2 : 0); }
+__host__ __device__ constexpr int term_group(int i) {
+  return term_a(i) + term_b(i) < 2 ? term_a(i) + term_b(i) : 2;
+}
+__host__ __device__ constexpr bool first_of_group(int i) {
+  for (int j = 0; j < i; ++j)
+    if (term_group(j) == term_group(i)) return false;
+  return true;
+}
+
+// Every product of one K block: group 0 into the block's rotating slot d0
+// (fresh), groups 1 and 2 into their persistent slots (fresh only for the
+// first product of the first block).
+template <int I0, int NT, class CF>
+__device__ __forceinline__ void issue_block(uint64_t da, uint64_t db, uint32_t d0, uint32_t t_g1,
+                                            uint32_t t_g2, bool first_block) {
+  constexpr uint32_t idesc = instr_desc(BM, CF::BN_);
+#pragma unroll
+  for (int i = I0; i < NT; ++i) {
+    const int g = term_group(i);
+    const uint32_t dcol = g == 0 ? d0 : (g == 1 ? t_g1 : t_g2);
+    const uint64_t dA = da + (uint64_t)((term_a(i) * CF::A_BYTES) >> 4);
+    const uint64_t dB = db + (uint64_t)((term_b(i) * CF::B_BYTES) >> 4);
+#pragma unroll
+    for (int k = 0; k < BK / 16; ++k) {
+      const bool fresh = k == 0 && (g == 0 || (first_of_group(i) && first_block));
+      umma(dcol, dA + 2 * k, dB + 2 * k, idesc, fresh ? 0u : 1u);
+    }
+  }
+}
+
 // OP_IS_A = false: stage 1 (A = data rows y, B = operator rows u, d from N tile)
 // OP_IS_A = true : stage 2 (A = operator rows v, B = data rows u, d from M tile)
 template <int BN, bool OP_IS_A, int EPI>
 __global__ void __launch_bounds__(THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                 const Params p) {
+                 const __grid_constant__ CUtensorMap tmO, const Params p) {
   using CF = Cfg<BN>;
   constexpr int STAGES = CF::STAGES;
   constexpr int NSLOT = 2;  // rotating group-0 slots
@@ -258,9 +330,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     row_a0 = (mt % p.m_half) * BM;
     row_b0 = nt * BN;
   }
-  int n_parts = 1;
-  for (int i = 0; i < p.n_terms; ++i)
-    n_parts = max(n_parts, 1 + max(p.term_a[i], p.term_b[i]));
+  const int n_parts = p.n_terms > 3 ? 3 : 2;  // parts the issued products read
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -326,10 +396,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncwarp();
   } else if (warp == MMA_WARP) {
     if (lane == 0) {
-      constexpr uint32_t idesc = instr_desc(BM, BN);
       int stage = 0;
       uint32_t phase = 0;
-      bool g1_on = false, g2_on = false;  // persistent groups hold data
+      bool aborted = false;
       for (int it = 0; it < k_iters; ++it) {
         const int ts = it % NSLOT;
         const uint32_t round = (uint32_t)(it / NSLOT);
@@ -347,32 +416,35 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int s = 0; s < NSLOT; ++s)
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tfull[s]))
                          : "memory");
+          aborted = true;
           break;
         }
         tc_fence_after();
+        // descriptors of the stage's part tiles: the start-address field is
+        // (address >> 4), so offsets are added to it directly (shared
+        // addresses stay below 2^18: no carry out of the 14-bit field)
         const uint32_t a0 = smem_u32(sbase + stage * CF::STAGE_BYTES);
-        const uint32_t b0 = a0 + MAX_PARTS * CF::A_BYTES;
-        for (int i = 0; i < p.n_terms; ++i) {
-          const int pa = p.term_a[i], pb = p.term_b[i];
-          const int g = min(pa + pb, 2);
-          const uint32_t dcol = g == 0 ? t_rot + (uint32_t)(ts * BN) : (g == 1 ? t_g1 : t_g2);
-          bool on = g == 0 ? false : (g == 1 ? g1_on : g2_on);
-          const uint32_t aa = a0 + pa * CF::A_BYTES, bb = b0 + pb * CF::B_BYTES;
-#pragma unroll
-          for (int k = 0; k < BK / 16; ++k) {
-            umma(dcol, smem_desc(aa + k * 32), smem_desc(bb + k * 32), idesc, on ? 1u : 0u);
-            on = true;
-          }
-          if (g == 1) g1_on = true;
-          if (g == 2) g2_on = true;
-        }
-        umma_commit(&empty[stage]);
+        const uint64_t da = smem_desc(a0), db = smem_desc(a0 + MAX_PARTS * CF::A_BYTES);
+        // One thread issues every product of the block, so the issue loop is
+        // fully unrolled over the fixed term order (descriptor offsets and
+        // accumulate flags are constants; only the first products of the
+        // persistent groups depend on it). Group 0 goes first and its slot is
+        // committed to the drain warps while the smaller groups are multiplied.
+        const uint32_t d0 = t_rot + (uint32_t)(ts * BN);
+        issue_block<0, 1, CF>(da, db, d0, t_g1, t_g2, it == 0);
         umma_commit(&tfull[ts]);
+        if (p.n_terms == 6)
+          issue_block<1, 6, CF>(da, db, d0, t_g1, t_g2, it == 0);
+        else
+          issue_block<1, 3, CF>(da, db, d0, t_g1, t_g2, it == 0);
+        umma_commit(&empty[stage]);
         if (++stage == STAGES) {
           stage = 0;
           phase ^= 1;
         }
       }
+      // every product issued: the persistent groups are final once this fires
+      if (!aborted) umma_commit(quiesce);
     }
     __syncwarp();
   } else {
@@ -399,13 +471,19 @@ __global__ void __launch_bounds__(THREADS, 1)
                      : "memory");
     }
     if (ok) {
-      // the last commit covered every product: add the persistent groups
-      // (smaller first: g2 into g1, then into the accumulator)
+      // the persistent groups are complete once the MMA warp's final commit
+      // lands (the group-0 commits do not cover the later groups)
+      ok = mbar_wait(quiesce, 0);
+      ok = __all_sync(0xffffffffu, ok && !*abort_flag);
+    }
+    if (ok) {
+      // add the persistent groups (smaller first: g2 into g1, then into the
+      // accumulator)
       tc_fence_after();
       float gsum[CPW];
 #pragma unroll
       for (int j = 0; j < CPW; ++j) gsum[j] = 0.f;
-      drain_add<CPW>(t_g2 + lane_off, gsum);
+      if (p.n_terms > 3) drain_add<CPW>(t_g2 + lane_off, gsum);  // bf16x3 has no group 2
       drain_add<CPW>(t_g1 + lane_off, gsum);
 #pragma unroll
       for (int j = 0; j < CPW; ++j) acc[j] += gsum[j];
@@ -415,7 +493,34 @@ __global__ void __launch_bounds__(THREADS, 1)
     } else if (EPI == EPI_T_SPLIT) {
       // C[y][u] -> T^T parts [field][part][d][u][y] (bf16)
       const int y = row_a0 + row;
-      if (y < p.out_cols) {
+      if ((p.out_cols & 1) == 0) {
+        // Lane pairs (y, y + 1) swap one value per two columns, so each lane
+        // holds both rows of one column and stores them as one bf16x2 word:
+        // the even lane column u0 + j, the odd lane column u0 + j + 1. With
+        // an even row count y + 1 is in range whenever the even y is.
+        __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(p.out);
+        const size_t plane2 = (size_t)p.out_rows * p.out_cols / 2;
+        const int odd = lane & 1;
+        const int ye = y - odd;
+        const int u0 = row_b0 + h * CPW + odd;
+#pragma unroll
+        for (int j = 0; j < CPW; j += 2) {
+          const float send = odd ? acc[j] : acc[j + 1];
+          const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+          const float lo = odd ? recv : acc[j];
+          const float hi = odd ? acc[j + 1] : recv;
+          const int u = u0 + j;
+          if (ye < p.out_cols && u < p.cols_valid) {
+            __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+            split3(lo, a0, a1, a2);
+            split3(hi, b0, b1, b2);
+            const size_t off = ((size_t)u * p.out_cols + ye) / 2;
+            out[((size_t)(field * 3 + 0) * 2 + d) * plane2 + off] = __halves2bfloat162(a0, b0);
+            out[((size_t)(field * 3 + 1) * 2 + d) * plane2 + off] = __halves2bfloat162(a1, b1);
+            out[((size_t)(field * 3 + 2) * 2 + d) * plane2 + off] = __halves2bfloat162(a2, b2);
+          }
+        }
+      } else if (y < p.out_cols) {
         __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
         const size_t plane = (size_t)p.out_rows * p.out_cols;
         const int u0 = row_b0 + h * CPW;
@@ -432,6 +537,39 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
         }
       }
+    } else if (p.tma_out) {
+      // Every product has completed and every operand load was consumed, so
+      // the operand ring is free: each warp stages its 32 x CPW block as
+      // CPW / 32 boxes of 32 x 32 fp32 in the TMA 128B-swizzled layout (16-byte
+      // chunk c of row r at chunk c ^ (r & 7): conflict-free) and one lane
+      // stores them (or adds them into the window), clipped to the window.
+      uint8_t* stage_w = sbase + (size_t)warp * (CPW * 32 * 4);
+#pragma unroll
+      for (int b = 0; b < CPW / 32; ++b) {
+        uint8_t* box = stage_w + b * 4096 + lane * 128;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const float* a = acc + b * 32 + c * 4;
+          *reinterpret_cast<float4*>(box + ((c ^ (lane & 7)) << 4)) =
+              make_float4(a[0], a[1], a[2], a[3]);
+        }
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        const int v0 = row_a0 + q * 32, z = field * 2 + d;
+#pragma unroll
+        for (int b = 0; b < CPW / 32; ++b) {
+          const int u = row_b0 + h * CPW + b * 32;
+          if (p.accumulate)
+            tma_reduce_add_3d(&tmO, stage_w + b * 4096, u, v0, z);
+          else
+            tma_store_3d(&tmO, stage_w + b * 4096, u, v0, z);
+        }
+        bulk_commit();
+        bulk_wait_read_all();
+      }
+      __syncwarp();
     } else {
       // C[v][u] -> out fp32 [field][d][out_r0 + v][out_c0 + u] (pitch out_pitch)
       const int v = row_a0 + row;

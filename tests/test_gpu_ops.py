@@ -74,6 +74,34 @@ def test_mft_zoomfft_semantics(ctx, n_in, n_out):
         assert peak_err(got[f], ref) < RANDOM_PEAK_TOL
 
 
+def test_mft_bf16x3_and_unaligned_output(ctx):
+    """bf16x3 (the three largest split products: ~2^-16 relative) with an
+    odd output width, whose rows break the TMA store alignment and take the
+    per-thread epilogue; bf16x6 on the same plan shape stays fp32-class."""
+    from csim_gb300._lib import CSG_PREC_BF16X3
+    R = rt()
+    rng = np.random.default_rng(13)
+    n_in, n_out = 256, 127
+    gin = of.ArrayGeom.set_xy(n_in, n_in, 1e-5)
+    gout = of.ArrayGeom.set_xy(n_out, n_out, 2.1e-6)
+    lf = np.array([6.5e-7 * 40.0])
+    pref = gin.pixelSizeX * gin.pixelSizeY / (1j * lf)
+    e = rand_field(rng, 2, n_in, n_in)
+    ref = [of.mft(e[f], gin.pixelX, gin.pixelY, gout.pixelX, gout.pixelY, lf[0], pref[0])
+           for f in range(2)]
+    errs = {}
+    for prec in (CSG_PREC_BF16X3, R.CSG_PREC_BF16X6):
+        plan = R.Mft(ctx, gin.pixelY, gin.pixelX, gout.pixelY, gout.pixelX, lf, pref, -1.0,
+                     precision=prec)
+        out = plan(R.to_planar(e), R.dvec([0, 0], torch.int32))
+        ctx.sync()
+        got = R.from_planar(out)
+        plan.close()
+        errs[prec] = max(rms_err(got[f], ref[f]) for f in range(2))
+    assert errs[R.CSG_PREC_BF16X6] < RMS_TOL
+    assert 1e-7 < errs[CSG_PREC_BF16X3] < 1e-4
+
+
 def test_mft_accumulate_and_input_multiplier(ctx):
     R = rt()
     rng = np.random.default_rng(11)
