@@ -445,10 +445,12 @@ def main():
                 wl.dev_split[0].copy_(wl.dev_in[:half])
                 wl.dev_split[1].copy_(wl.dev_in[half:])
             img = step()
-            _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_img.data_ptr()),
+            # pipelined readout: the device-to-host copies run on the
+            # context's copy stream while the next step computes
+            _lib.call("csg_readout_d2h", ctx.h, C.c_void_p(host_img.data_ptr()),
                       C.c_void_p(img.data_ptr()), host_img.numel() * host_img.element_size())
             if wl.reg is not None:
-                _lib.call("csg_memcpy_d2h", ctx.h, C.c_void_p(host_con.data_ptr()),
+                _lib.call("csg_readout_d2h", ctx.h, C.c_void_p(host_con.data_ptr()),
                           C.c_void_p(contrast.data_ptr()), n_groups * 8)
         for _ in range(3):
             e2e_step()

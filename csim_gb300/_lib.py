@@ -47,6 +47,7 @@ SIGNATURES = {
     "csg_free": ([P, P], None),
     "csg_memcpy_h2d": ([P, P, P, SZ], None),
     "csg_memcpy_d2h": ([P, P, P, SZ], None),
+    "csg_readout_d2h": ([P, P, P, SZ], None),
     "csg_memset": ([P, P, I, SZ], None),
     "csg_version": ([], C.c_char_p),
     "csg_launch_count": ([], C.c_ulonglong),

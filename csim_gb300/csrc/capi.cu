@@ -139,7 +139,14 @@ int csg_destroy(csg_ctx* c) {
   if (!c) return CSG_OK;
   DeviceGuard g(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   for (void* p : c->allocations) cudaFree(p);
+  for (int k = 0; k < 2; ++k) {
+    if (c->ro_buf[k]) cudaFree(c->ro_buf[k]);
+    if (c->ro_ready[k]) cudaEventDestroy(c->ro_ready[k]);
+    if (c->ro_done[k]) cudaEventDestroy(c->ro_done[k]);
+  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   cudaFree(c->status);
   cudaStreamDestroy(c->own_stream);
   delete c;
@@ -150,6 +157,7 @@ int csg_sync(csg_ctx* c) {
   CSG_CHECK(c != nullptr, CSG_E_ARG, "csg_sync: null context");
   DeviceGuard g(c->device);
   CSG_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->copy_stream) CSG_CUDA(cudaStreamSynchronize(c->copy_stream));
   int st = 0;
   CSG_CUDA(cudaMemcpy(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost));
   if (st != 0) {
@@ -208,6 +216,43 @@ int csg_memcpy_d2h(csg_ctx* c, void* dst, const void* src, size_t bytes) {
   CSG_CHECK(c && dst && src, CSG_E_ARG, "csg_memcpy_d2h: null argument");
   DeviceGuard g(c->device);
   CSG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+  return CSG_OK;
+}
+
+int csg_readout_d2h(csg_ctx* c, void* dst, const void* src, size_t bytes) {
+  CSG_CHECK(c && dst && src, CSG_E_ARG, "csg_readout_d2h: null argument");
+  DeviceGuard g(c->device);
+  if (!bytes) return CSG_OK;
+  if (!c->copy_stream) {
+    CSG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      CSG_CUDA(cudaEventCreateWithFlags(&c->ro_ready[k], cudaEventDisableTiming));
+      CSG_CUDA(cudaEventCreateWithFlags(&c->ro_done[k], cudaEventDisableTiming));
+    }
+  }
+  const int k = c->ro_next;
+  c->ro_next ^= 1;
+  if (c->ro_cap[k] < bytes) {
+    // the buffer's last copy-out must finish before it is replaced
+    CSG_CUDA(cudaEventSynchronize(c->ro_done[k]));
+    if (c->ro_buf[k]) CSG_CUDA(cudaFree(c->ro_buf[k]));
+    c->ro_buf[k] = nullptr;
+    c->ro_cap[k] = 0;
+    if (cudaMalloc(&c->ro_buf[k], bytes) != cudaSuccess) {
+      cudaGetLastError();
+      c->ro_buf[k] = nullptr;
+      set_error("csg_readout_d2h: staging allocation failed");
+      return CSG_E_NOMEM;
+    }
+    c->ro_cap[k] = bytes;
+  }
+  // staging k is free once its previous copy-out has run
+  CSG_CUDA(cudaStreamWaitEvent(c->stream, c->ro_done[k], 0));
+  CSG_CUDA(cudaMemcpyAsync(c->ro_buf[k], src, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  CSG_CUDA(cudaEventRecord(c->ro_ready[k], c->stream));
+  CSG_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ro_ready[k], 0));
+  CSG_CUDA(cudaMemcpyAsync(dst, c->ro_buf[k], bytes, cudaMemcpyDeviceToHost, c->copy_stream));
+  CSG_CUDA(cudaEventRecord(c->ro_done[k], c->copy_stream));
   return CSG_OK;
 }
 

@@ -90,6 +90,8 @@ struct Elem {
   int P = 0;
   // per-wavelength tables (mirror phasors, Fresnel transfer function)
   float2* tab = nullptr;
+  // mirror right after a real mask: the mask times the phasor table
+  float2* tab_m = nullptr;
   // real mask: bounding box [sr0, sr1) x [sc0, sc1) of its nonzero pixels
   int sr0 = 0, sr1 = 0, sc0 = 0, sc1 = 0;
   // lazily built transforms: wavelength-f products, prefactors, window
@@ -199,6 +201,7 @@ int csg_chain_destroy(csg_chain* c) {
     cudaFree(e.hex_id);
     cudaFree(e.count);
     cudaFree(e.tab);
+    cudaFree(e.tab_m);
     csg_mft_destroy(e.mft1);
     csg_mft_destroy(e.mft2);
     csg_mft_destroy(e.mft);
@@ -240,6 +243,17 @@ int csg_chain_add_mask(csg_chain* c, const float* mask, int ref_quirk, int disab
   return CSG_OK;
 }
 
+// out[s][p] = mask[p] * tab[s][p] for every wavelength slot s.
+__global__ void k_mask_times_table(const float* __restrict__ mask, const float2* __restrict__ tab,
+                                   long long plane, long long total, float2* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float m = mask[i % plane];
+    const float2 w = tab[i];
+    out[i] = make_float2(m * w.x, m * w.y);
+  }
+}
+
 // mirror element (mirror.cpp:23-72): sag N x N (host fp32, metres).
 int csg_chain_add_mirror(csg_chain* c, const float* sag, double sign) {
   CSG_CHECK(c && sag, CSG_E_ARG, "csg_chain_add_mirror: null argument");
@@ -256,6 +270,15 @@ int csg_chain_add_mirror(csg_chain* c, const float* sag, double sign) {
   int rc = build_phasor_table(c->ctx->stream, e.a, c->n, c->n, c->lam_slots, c->n_lambda, sign,
                               e.tab);
   if (rc) return rc;
+  // after a real mask the walk applies both with one table read per pixel
+  if (!c->elems.empty() && c->elems.back().kind == E_MASK && !c->elems.back().quirk) {
+    e.tab_m = dev_copy<float2>(nullptr, plane * c->n_lambda, c->ctx->stream);
+    CSG_CHECK(e.tab_m, CSG_E_NOMEM, "csg_chain_add_mirror: allocation failed");
+    const long long total = (long long)plane * c->n_lambda;
+    k_mask_times_table<<<grid_for(total, 256), 256, 0, c->ctx->stream>>>(
+        c->elems.back().a, e.tab, (long long)plane, total, e.tab_m);
+    CSG_LAUNCH_CHECK();
+  }
   c->elems.push_back(e);
   c->planned = false;
   drop_graph(c);
@@ -702,6 +725,7 @@ struct Step {
   enum Kind { PIX, FRESNEL, FPM, FINAL, FFT_FPM } kind;
   PixOps pro, epi;
   const Elem* e = nullptr;
+  int sup0 = 0, sup1 = 1 << 30;  // FRESNEL: rows that can be nonzero on input
 };
 
 static bool push_op(PixOps& o, int kind, const float* a, const float* b, float param, int mr,
@@ -722,32 +746,53 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
   PixOps pend;
   push_op(pend, OP_SOURCE, nullptr, nullptr, 0.f, 0, 0);
   bool epi_open = false;  // the last step is a Fresnel that can still take ops
-  for (const auto& e : c->elems) {
+  // rows of the field that can be nonzero: real masks applied since the last
+  // transform zero everything outside their row support
+  int sup0 = 0, sup1 = c->n;
+  const size_t ne = c->elems.size();
+  for (size_t ei = 0; ei < ne; ++ei) {
+    const Elem& e = c->elems[ei];
     if (calibrating && e.disable_for_calibration) continue;
     int kind = 0;
     float param = 0.f;
+    const float* a = e.a;
     if (e.kind == E_MASK) {
       kind = OP_MASK;
       param = e.quirk ? 1.f : 0.f;
+      sup0 = std::max(sup0, e.sr0);
+      sup1 = std::min(sup1, e.sr1);
+      // a real mask followed by a mirror: one op with the mirror's
+      // mask-multiplied phasor table
+      if (ei + 1 < ne && c->elems[ei + 1].kind == E_MIRROR && c->elems[ei + 1].tab_m &&
+          !(calibrating && c->elems[ei + 1].disable_for_calibration)) {
+        kind = OP_PHASOR;
+        param = 0.f;
+        a = reinterpret_cast<const float*>(c->elems[ei + 1].tab_m);
+        ++ei;
+      }
     } else if (e.kind == E_MIRROR) {
       kind = OP_PHASOR;  // reads the element's per-wavelength phasor table
+      a = reinterpret_cast<const float*>(e.tab);
     } else if (e.kind == E_CMASK) {
       kind = OP_CMASK;
     }
     if (kind) {
-      const float* a = kind == OP_PHASOR ? reinterpret_cast<const float*>(e.tab) : e.a;
-      if (epi_open && push_op(prog.back().epi, kind, a, e.b, param, e.mrows, e.mcols)) continue;
+      const float* b = kind == OP_PHASOR ? nullptr : e.b;
+      if (epi_open && push_op(prog.back().epi, kind, a, b, param, e.mrows, e.mcols)) continue;
       epi_open = false;
-      if (!push_op(pend, kind, a, e.b, param, e.mrows, e.mcols)) {
+      if (!push_op(pend, kind, a, b, param, e.mrows, e.mcols)) {
         Step s{Step::PIX, pend, PixOps(), nullptr};
         prog.push_back(s);
         pend = PixOps();
-        push_op(pend, kind, a, e.b, param, e.mrows, e.mcols);
+        push_op(pend, kind, a, b, param, e.mrows, e.mcols);
       }
       continue;
     }
     if (e.kind == E_FRESNEL) {
-      prog.push_back(Step{Step::FRESNEL, pend, PixOps(), &e});
+      Step s{Step::FRESNEL, pend, PixOps(), &e};
+      s.sup0 = sup0;
+      s.sup1 = sup1;
+      prog.push_back(s);
       pend = PixOps();
       epi_open = true;
     } else if (e.kind == E_FPM_HEX) {
@@ -764,6 +809,8 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
       pend = PixOps();
       epi_open = false;
     }
+    sup0 = 0;  // after a transform every row can be nonzero
+    sup1 = c->n;
   }
   if (pend.n) prog.push_back(Step{Step::PIX, pend, PixOps(), nullptr});
   return prog;
@@ -781,7 +828,11 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         break;
       case Step::FRESNEL: {
         FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad, s.e->tab, c->slot};
-        rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi);
+        FftBand sup;  // rows a mask left nonzero, widened to the transform's row groups
+        if (fft_row_support(n, s.sup0, std::min(s.sup1, n), &sup.lo, &sup.n) && sup.n < n)
+          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, &sup);
+        else
+          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi);
         break;
       }
       case Step::FPM: {

@@ -33,6 +33,14 @@ struct csg_ctx {
   int* status = nullptr;            // device int, 0 = ok
   std::set<void*> allocations;
   int sm_count = 0;
+  // pipelined readout (csg_readout_d2h): two device staging buffers, each
+  // copied to the host on copy_stream while the context's stream runs on
+  cudaStream_t copy_stream = nullptr;
+  void* ro_buf[2] = {nullptr, nullptr};
+  size_t ro_cap[2] = {0, 0};
+  cudaEvent_t ro_ready[2] = {nullptr, nullptr};  // staging filled (context stream)
+  cudaEvent_t ro_done[2] = {nullptr, nullptr};   // staging copied out (copy stream)
+  int ro_next = 0;
   // opt-in per-kernel timing (CUDA events on the launching stream)
   bool prof = false;
   std::vector<csg::ProfPending> pending;

@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
   // band: element s is in the n-wide centre iff s0 <= s < s1
   const int s0 = band.lo / TPT, s1 = (band.lo + band.n) / TPT;
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // source overwrites: skip the read
-  if (band.n && !INV) {  // rows of the n x n source, zero outside its columns
+  if (band.n && band.src && !INV) {  // rows of the n x n source, zero outside its columns
     const size_t np = (size_t)band.n * band.n;
     const float* sre = band.src + (size_t)f * 2 * np + (size_t)(row - band.lo) * band.n + u -
                        band.lo;
@@ -310,11 +310,13 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
   PixConsts kp, ke;
   if (pro.n) pix_consts_cta(pro, fi, f, N, N, kp, &shk[0]);
   if (epi.n) pix_consts_cta(epi, fi, f, N, N, ke, &shk[1]);
-  // element ops in groups of 8 (bounds the live table values)
+  // element ops in groups (bounds the live table values; the prologue's
+  // wider groups put more table loads in flight at once)
   if (pro.n) {
+    constexpr int G = E >= 16 ? 16 : E;
 #pragma unroll
-    for (int h = 0; h < E; h += 8)
-      pix_apply_n<8>(pro, kp, row, u + h * TPT, 0, TPT, N, N, xr + h, xi + h);
+    for (int h = 0; h < E; h += G)
+      pix_apply_n<G>(pro, kp, row, u + h * TPT, 0, TPT, N, N, xr + h, xi + h);
   }
   fft_regs<N, E, INV, A>(xr, xi, re, im, t, u, tw);
 #pragma unroll
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
     for (int h = 0; h < E; h += 8)
       pix_apply_n<8>(epi, ke, row, u + h * TPT, 0, TPT, N, N, xr + h, xi + h);
   }
-  if (band.n && INV) {  // the centre n columns straight to the n x n field
+  if (band.n && band.dst && INV) {  // the centre n columns straight to the n x n field
     const size_t np = (size_t)band.n * band.n;
     float* dre = band.dst + (size_t)f * 2 * np + (size_t)(row - band.lo) * band.n + u - band.lo;
 #pragma unroll
@@ -406,7 +408,7 @@ int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, d
 template <int N, int E, int MODE, int COLS>
 __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS>::MIN_BLOCKS)
     k_fft_cols(float* __restrict__ field, const float2* __restrict__ tw,
-               const __grid_constant__ FresnelArgs fa, int band_lo, int band_n) {
+               const __grid_constant__ FresnelArgs fa, int band_lo, int band_n, int store_all) {
   using CF = ColCfg<N, E, COLS>;
   using A = ColAddr<COLS, E>;
   constexpr int TPT = CF::TPT;
@@ -422,8 +424,9 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS
   float* fim = fre + plane;
   float xr[E], xi[E];
   // band: rows u + s N/E outside [band_lo, band_lo + band_n) are zero on
-  // input and not stored (band_n = 0: every row)
+  // input and, unless store_all, not stored (band_n = 0: every row)
   const int s0 = band_n ? band_lo / TPT : 0, s1 = band_n ? (band_lo + band_n) / TPT : E;
+  const int w0 = store_all ? 0 : s0, w1 = store_all ? E : s1;
 #pragma unroll
   for (int s = 0; s < E; ++s) {
     const bool in = s >= s0 && s < s1;
@@ -464,7 +467,7 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS
   }
 #pragma unroll
   for (int s = 0; s < E; ++s)
-    if (s >= s0 && s < s1) {
+    if (s >= w0 && s < w1) {
       fre[(size_t)s * TPT * N] = xr[s];
       fim[(size_t)s * TPT * N] = xi[s];
     }
@@ -481,22 +484,22 @@ static int prep_smem(K kern, size_t bytes) {
 
 template <int N, int E, int COLS>
 static int launch_cols(cudaStream_t st, float* field, int F, int mode, const float2* tw,
-                       const FresnelArgs* fa, const FftBand& band) {
+                       const FresnelArgs* fa, const FftBand& band, int store_all) {
   using CC = ColCfg<N, E, COLS>;
   const int grid = F * (N / COLS);
   int rc;
   if (mode == 2) {
     if ((rc = prep_smem(k_fft_cols<N, E, 2, COLS>, CC::SMEM))) return rc;
     k_fft_cols<N, E, 2, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa, band.lo,
-                                                                   band.n);
+                                                                   band.n, store_all);
   } else if (mode == 1) {
     if ((rc = prep_smem(k_fft_cols<N, E, 1, COLS>, CC::SMEM))) return rc;
     k_fft_cols<N, E, 1, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{}, 0,
-                                                                   0);
+                                                                   0, 0);
   } else {
     if ((rc = prep_smem(k_fft_cols<N, E, 0, COLS>, CC::SMEM))) return rc;
     k_fft_cols<N, E, 0, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{}, 0,
-                                                                   0);
+                                                                   0, 0);
   }
   CSG_LAUNCH_CHECK();
   return CSG_OK;
@@ -533,44 +536,56 @@ static int env_choice(const char* name, std::initializer_list<int> allowed) {
 template <int N>
 static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const FresnelArgs* fa,
                    const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw,
-                   const FftBand& band) {
+                   const FftBand& band, const FftBand& sup) {
   cudaStream_t st = ctx->stream;
   const float inv_scale = 1.f / ((float)N * (float)N);
   // a band-limited pass moves n rows of N (the first and last touch n x n)
   const double pass_bytes = (double)F * N * (band.n ? band.n : N) * 16.0;
   const double edge_bytes = band.n ? (double)F * band.n * (N + band.n) * 8.0 : pass_bytes;
   const PixOps none;
-  const bool e16 = (N == 1024) && !band.n && env_choice("CSG_FFT_E", {16}) == 16;
+  const bool e16 = (N == 1024) && !band.n && !sup.n && env_choice("CSG_FFT_E", {16}) == 16;
   const int c_over = env_choice("CSG_FFT_COLS", {4, 16});
   int rc;
-  auto rows = [&](bool inv, float scale, const PixOps& p, const PixOps& e) -> int {
+  auto rows = [&](bool inv, float scale, const PixOps& p, const PixOps& e,
+                  const FftBand& bd) -> int {
     const bool gen = p.n && p.kind[0] == OP_SOURCE;
-    ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, edge_bytes * (gen ? 0.5 : 1.0));
+    const double bytes = bd.n && !bd.src && !bd.dst ? (double)F * N * bd.n * 16.0 : edge_bytes;
+    ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, bytes * (gen ? 0.5 : 1.0));
     if constexpr (N == 1024)
-      if (e16) return launch_rows<N, 16>(st, field, F, inv, scale, tw, p, e, fi, band);
-    return launch_rows<N, default_e(N)>(st, field, F, inv, scale, tw, p, e, fi, band);
+      if (e16) return launch_rows<N, 16>(st, field, F, inv, scale, tw, p, e, fi, bd);
+    return launch_rows<N, default_e(N)>(st, field, F, inv, scale, tw, p, e, fi, bd);
   };
-  auto cols = [&](int mode) -> int {
-    ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, pass_bytes);
+  auto cols = [&](int mode, const FftBand& bd, int store_all) -> int {
+    const double bytes = store_all ? (double)F * N * (N + bd.n) * 8.0 : pass_bytes;
+    ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, bytes);
     if constexpr (N == 1024) {
-      if (e16) return launch_cols<N, 16, 8>(st, field, F, mode, tw, fa, band);
-      if (c_over == 4) return launch_cols<N, 32, 4>(st, field, F, mode, tw, fa, band);
-      if (c_over == 16) return launch_cols<N, 32, 16>(st, field, F, mode, tw, fa, band);
+      if (e16) return launch_cols<N, 16, 8>(st, field, F, mode, tw, fa, bd, store_all);
+      if (c_over == 4) return launch_cols<N, 32, 4>(st, field, F, mode, tw, fa, bd, store_all);
+      if (c_over == 16) return launch_cols<N, 32, 16>(st, field, F, mode, tw, fa, bd, store_all);
     }
-    return launch_cols<N, default_e(N), default_cols(N)>(st, field, F, mode, tw, fa, band);
+    return launch_cols<N, default_e(N), default_cols(N)>(st, field, F, mode, tw, fa, bd,
+                                                         store_all);
   };
-  if (fa) {
-    if ((rc = rows(false, 1.f, pro, none))) return rc;
-    if ((rc = cols(2))) return rc;
-    return rows(true, inv_scale, none, epi);
+  const FftBand whole;
+  if (fa && sup.n) {
+    // rows outside the prologue's support are zero: the first row pass
+    // skips them (leaving them unwritten) and the column pass reads only
+    // the support's rows and writes every row
+    if ((rc = rows(false, 1.f, pro, none, sup))) return rc;
+    if ((rc = cols(2, sup, 1))) return rc;
+    return rows(true, inv_scale, none, epi, whole);
+  } else if (fa) {
+    if ((rc = rows(false, 1.f, pro, none, band))) return rc;
+    if ((rc = cols(2, band, 0))) return rc;
+    return rows(true, inv_scale, none, epi, band);
   } else if (direction < 0) {
-    if ((rc = rows(false, 1.f, pro, none))) return rc;
-    if ((rc = cols(0))) return rc;
+    if ((rc = rows(false, 1.f, pro, none, band))) return rc;
+    if ((rc = cols(0, band, 0))) return rc;
     if (epi.n) return pixops_pass(st, field, F, N, N, epi, fi);
   } else {
     if (pro.n && (rc = pixops_pass(st, field, F, N, N, pro, fi))) return rc;
-    if ((rc = cols(1))) return rc;
-    return rows(true, inv_scale, none, epi);
+    if ((rc = cols(1, band, 0))) return rc;
+    return rows(true, inv_scale, none, epi, band);
   }
   return CSG_OK;
 }
@@ -580,37 +595,55 @@ bool fft_band_supported(int N, int lo, int n) {
   return n > 0 && lo >= 0 && lo + n <= N && lo % TPT == 0 && n % TPT == 0 && n % rows == 0;
 }
 
+bool fft_row_support(int N, int r0, int r1, int* lo, int* n) {
+  const int TPT = N / default_e(N);
+  if (r0 < 0 || r1 > N || r0 >= r1) return false;
+  *lo = r0 / TPT * TPT;
+  *n = (r1 + TPT - 1) / TPT * TPT - *lo;
+  return fft_band_supported(N, *lo, *n);
+}
+
 // 2-D FFT or Fresnel propagation of F square N x N fields with fused element
 // ops (pro before the transform, epi after it).
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
-                const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const FftBand* band) {
+                const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const FftBand* band,
+                const FftBand* support) {
   CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
             "FFT size must be a power of two in [64, 4096]");
   CSG_CHECK(F > 0 && (long long)F * n < (1LL << 31), CSG_E_SHAPE, "FFT: bad field count");
-  FftBand bd;
+  FftBand bd, sp;
   if (band) {
-    CSG_CHECK(fa && !pro.n && !epi.n && band->src && band->dst &&
+    CSG_CHECK(fa && !pro.n && !epi.n && band->src && band->dst && !support &&
                   fft_band_supported(n, band->lo, band->n),
               CSG_E_ARG, "FFT: unsupported band-limited transform");
     bd = *band;
+  }
+  if (support) {
+    CSG_CHECK(fa && !support->src && !support->dst &&
+                  fft_band_supported(n, support->lo, support->n),
+              CSG_E_ARG, "FFT: unsupported row support");
+    sp = *support;
   }
   cudaStream_t st = ctx->stream;
   const float2* tw = twiddles(ctx->device, n, st);
   CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
   const double pass_bytes = (double)F * n * n * 16.0;
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // the first pass only writes
-  const double total = band ? (double)F * band->n * (n + band->n) * 16.0 +
-                                  (double)F * n * band->n * 16.0
-                            : pass_bytes * ((fa ? 3.0 : 2.0) - (gen ? 0.5 : 0.0));
+  double total = pass_bytes * ((fa ? 3.0 : 2.0) - (gen ? 0.5 : 0.0));
+  if (band)
+    total = (double)F * band->n * (n + band->n) * 16.0 + (double)F * n * band->n * 16.0;
+  else if (support)
+    total = (double)F * n * support->n * 16.0 * (gen ? 0.5 : 1.0) +
+            (double)F * n * (n + support->n) * 8.0 + pass_bytes;
   ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0, total);
   switch (n) {
-    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
-    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
-    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
-    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
-    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
-    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
-    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd);
+    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
+    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
+    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
+    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
+    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
+    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
+    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
   }
 }
 

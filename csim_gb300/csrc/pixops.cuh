@@ -276,12 +276,19 @@ struct FftBand {
 
 // 2-D FFT (direction -1 / +1) or, with fa, Fresnel propagation of F square
 // N x N fields with element ops fused before (pro) and after (epi).
+// support (with fa only; lo and n, no src or dst): the field is zero outside
+// rows [lo, lo + n) once pro is applied (a mask's support), so the first row
+// pass transforms only those rows and the column pass reads only them; the
+// other rows of the field are not read before they are overwritten.
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi,
-                const FftBand* band = nullptr);
+                const FftBand* band = nullptr, const FftBand* support = nullptr);
 // Whether fft2d_fused can run an N-point padded transform band-limited to
 // [lo, lo + n).
 bool fft_band_supported(int N, int lo, int n);
+// Rows [r0, r1) widened to a band fft2d_fused accepts as a row support
+// (false: none).
+bool fft_row_support(int N, int r0, int r1, int* lo, int* n);
 
 // A window of a field: rows x cols of the transform start at (r0, c0) of
 // planes that are `rows` x `pitch`.

@@ -76,6 +76,13 @@ int csg_alloc(csg_ctx* ctx, size_t bytes, void** dptr);
 int csg_free(csg_ctx* ctx, void* dptr);
 int csg_memcpy_h2d(csg_ctx* ctx, void* dst, const void* src, size_t bytes);
 int csg_memcpy_d2h(csg_ctx* ctx, void* dst, const void* src, size_t bytes);
+/* Pipelined readout of a result: src (device) is copied on the context's
+ * stream into one of two context-owned staging buffers (a device-to-device
+ * copy), and from there to dst (host, pinned for overlap) on a separate copy
+ * stream, so the device-to-host transfer overlaps the work queued after this
+ * call. dst holds the data after the next csg_sync, which also waits for the
+ * copy stream. Not usable inside stream capture. */
+int csg_readout_d2h(csg_ctx* ctx, void* dst, const void* src, size_t bytes);
 int csg_memset(csg_ctx* ctx, void* dst, int value, size_t bytes);
 /* Version string of the library build. */
 const char* csg_version(void);

@@ -283,3 +283,27 @@ def test_intensity_and_region(ctx):
             ig = (np.abs(ee[3 * g:3 * g + 3]) ** 2).sum(0).ravel()[pix]
             red = ig.mean() if mode == 0 else ig.max()
             assert abs(out[g].item() - 0.5 * red) < 1e-12 * red
+
+
+def test_pipelined_readout(ctx):
+    """csg_readout_d2h: results copied out through the two staging buffers
+    while later work overwrites the source are the values at call time."""
+    import ctypes as C
+    from csim_gb300._lib import call
+    n = 1 << 20
+    src = torch.empty(n, dtype=torch.float32, device="cuda")
+    hosts = [torch.empty(n, dtype=torch.float32).pin_memory() for _ in range(3)]
+    stream = torch.cuda.Stream()
+    ctx.bind_stream(stream)
+    try:
+        with torch.cuda.stream(stream):
+            for i, h in enumerate(hosts):
+                src.fill_(float(i + 1))
+                call("csg_readout_d2h", ctx.h, C.c_void_p(h.data_ptr()),
+                     C.c_void_p(src.data_ptr()), n * 4)
+            src.fill_(-1.0)  # later work on the source does not reach the host copies
+        ctx.sync()
+    finally:
+        ctx.bind_stream(torch.cuda.current_stream())
+    for i, h in enumerate(hosts):
+        assert bool((h == float(i + 1)).all())
