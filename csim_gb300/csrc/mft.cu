@@ -221,7 +221,7 @@ template <int BN, bool OP_IS_A, int EPI>
 static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Params& p,
                        int grid, cudaStream_t st, const CUtensorMap* o = nullptr) {
   auto kern = tc::k_split_gemm<BN, OP_IS_A, EPI>;
-  constexpr size_t smem = tc::smem_bytes<BN>();
+  constexpr size_t smem = tc::smem_bytes<BN, EPI>();
   static bool attr_set = false;  // per template instance
   if (!attr_set) {
     CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -229,7 +229,14 @@ static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Par
   }
   CSG_CHECK(o || !p.tma_out, CSG_E_ARG, "GEMM: TMA output without a tensor map");
   static const CUtensorMap unused{};  // read only when p.tma_out
-  kern<<<grid, tc::THREADS, smem, st>>>(a, b, o ? *o : unused, p);
+  // persistent CTAs, one per SM (the kernel walks tiles with a grid stride)
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    CSG_CUDA(cudaGetDevice(&dev));
+    CSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  kern<<<std::min(grid, sms), tc::THREADS, smem, st>>>(a, b, o ? *o : unused, p);
   CSG_LAUNCH_CHECK();
   return CSG_OK;
 }

@@ -218,22 +218,30 @@ constexpr int PRODUCER_WARP = DRAIN_WARPS;
 constexpr int MMA_WARP = DRAIN_WARPS + 1;
 constexpr int MAX_PARTS = 3;
 
-template <int BN>
+// Persistent CTAs: each CTA walks the tiles blockIdx.x, blockIdx.x + grid,
+// ... with the operand ring, the rotating slots and their barriers running
+// on across tiles, so the producer loads the next tile while the current
+// one finishes and its epilogue runs. The fp32 epilogue stages its boxes in
+// a region of its own (4 KB per drain warp), apart from the ring.
+template <int BN, int EPI>
 struct Cfg {
   static_assert(BN == 64 || BN == 128, "N tile must be 64 or 128");
   static constexpr uint32_t A_BYTES = BM * BK * 2;
   static constexpr uint32_t B_BYTES = BN * BK * 2;
   static constexpr uint32_t STAGE_BYTES = MAX_PARTS * (A_BYTES + B_BYTES);
-  static constexpr int STAGES = BN == 128 ? 2 : 3;  // 192 KB / 216 KB of operand ring
+  static constexpr uint32_t STAGING_BYTES = EPI == 1 ? DRAIN_WARPS * 4096 : 0;
+  // 192 KB (+ 32 KB staging) at N = 128; 216 KB or 144 KB (+ 32 KB) at 64
+  static constexpr int STAGES = BN == 128 ? 2 : (EPI == 1 ? 2 : 3);
   static constexpr int TMEM_COLS = 4 * BN;          // group 1, group 2, two rotating slots
   static constexpr int COLS_PER_WARP = BN / 2;      // two warps share a lane quadrant
   static constexpr int BN_ = BN;
-  static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 512;
+  static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + STAGING_BYTES + 1024 + 512;
+  static_assert(SMEM <= 232448, "shared memory per CTA");
 };
 
-template <int BN>
+template <int BN, int EPI>
 constexpr size_t smem_bytes() {
-  return Cfg<BN>::SMEM;
+  return Cfg<BN, EPI>::SMEM;
 }
 
 // Drain one lane quadrant's CPW columns at taddr into acc (+=).
@@ -289,11 +297,37 @@ __device__ __forceinline__ void issue_block(uint64_t da, uint64_t db, uint32_t d
 
 // OP_IS_A = false: stage 1 (A = data rows y, B = operator rows u, d from N tile)
 // OP_IS_A = true : stage 2 (A = operator rows v, B = data rows u, d from M tile)
+struct TileCoord {
+  int field, d, row_a0, row_b0;
+};
+template <int BN, bool OP_IS_A>
+__device__ __forceinline__ TileCoord tile_coord(const Params& p, int t) {
+  TileCoord c;
+  const int nt = t % p.n_tiles;
+  t /= p.n_tiles;
+  const int mt = t % p.m_tiles;
+  c.field = t / p.m_tiles;
+  if (!OP_IS_A) {
+    c.d = nt / p.n_half;
+    c.row_a0 = mt * BM;
+    c.row_b0 = (nt % p.n_half) * BN;
+  } else {
+    c.d = mt / p.m_half;
+    c.row_a0 = (mt % p.m_half) * BM;
+    c.row_b0 = nt * BN;
+  }
+  return c;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 template <int BN, bool OP_IS_A, int EPI>
 __global__ void __launch_bounds__(THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const __grid_constant__ CUtensorMap tmO, const Params p) {
-  using CF = Cfg<BN>;
+  using CF = Cfg<BN, EPI>;
   constexpr int STAGES = CF::STAGES;
   constexpr int NSLOT = 2;  // rotating group-0 slots
   constexpr int CPW = CF::COLS_PER_WARP;
@@ -301,36 +335,22 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
-  uint64_t* full = reinterpret_cast<uint64_t*>(sbase + STAGES * CF::STAGE_BYTES);
+  uint8_t* staging = sbase + STAGES * CF::STAGE_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(staging + CF::STAGING_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* tfull = empty + STAGES;   // slot filled by the MMA warp
   uint64_t* tempty = tfull + NSLOT;   // slot drained by the drain warps
-  uint64_t* quiesce = tempty + NSLOT;  // abort path: in-flight products done
+  uint64_t* gdone = tempty + NSLOT;   // a tile's products all complete (per tile)
+  uint64_t* gfree = gdone + 1;        // a tile's persistent groups read (per tile)
+  uint64_t* quiesce = gfree + 1;      // abort path: in-flight products done
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(quiesce + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-
-  int t = blockIdx.x;
-  const int nt = t % p.n_tiles;
-  t /= p.n_tiles;
-  const int mt = t % p.m_tiles;
-  const int field = t / p.m_tiles;
-  if (field >= p.n_fields) return;
-  const int slot = p.slot[field];
-
-  int d, row_a0, row_b0;
-  if (!OP_IS_A) {
-    d = nt / p.n_half;
-    row_a0 = mt * BM;
-    row_b0 = (nt % p.n_half) * BN;
-  } else {
-    d = mt / p.m_half;
-    row_a0 = (mt % p.m_half) * BM;
-    row_b0 = nt * BN;
-  }
+  const int n_tiles_total = p.n_fields * p.m_tiles * p.n_tiles;
   const int n_parts = p.n_terms > 3 ? 3 : 2;  // parts the issued products read
+  const int k_iters = 2 * p.k_blocks;         // (data component c, K block) per tile
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -341,6 +361,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&tfull[s], 1);
       mbar_init(&tempty[s], DRAIN_WARPS);
     }
+    mbar_init(gdone, 1);
+    mbar_init(gfree, DRAIN_WARPS);
     mbar_init(quiesce, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -357,94 +379,92 @@ __global__ void __launch_bounds__(THREADS, 1)
   const uint32_t tmem = *tmem_slot;
   const uint32_t t_g1 = tmem, t_g2 = tmem + BN, t_rot = tmem + 2 * BN;
 
-  const int k_iters = 2 * p.k_blocks;  // (data component c, K block)
-
   if (warp == PRODUCER_WARP) {
     if (lane == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
-      for (int it = 0; it < k_iters; ++it) {
-        if (it >= STAGES && !mbar_wait(&empty[stage], phase ^ 1)) {
-          atomicExch(p.status, 1);
-          *abort_flag = 1;
-          break;
-        }
-        if (*abort_flag) break;
-        const int kb = it % p.k_blocks;
-        const int c = it / p.k_blocks;
-        uint8_t* sA = sbase + stage * CF::STAGE_BYTES;
-        uint8_t* sB = sA + MAX_PARTS * CF::A_BYTES;
-        mbar_expect_tx(&full[stage], n_parts * (CF::A_BYTES + CF::B_BYTES));
-        for (int pp = 0; pp < n_parts; ++pp) {
-          int za, zb;
-          if (!OP_IS_A) {
-            za = (field * 3 + pp) * 2 + c;
-            zb = (slot * 3 + pp) * 3 + sel_plane(d, c);
-          } else {
-            za = (slot * 3 + pp) * 3 + sel_plane(d, c);
-            zb = (field * 3 + pp) * 2 + c;
+      long long g = 0;  // iterations over all of this CTA's tiles
+      for (int t = blockIdx.x; t < n_tiles_total && !*abort_flag; t += gridDim.x) {
+        const TileCoord tc = tile_coord<BN, OP_IS_A>(p, t);
+        const int slot = p.slot[tc.field];
+        for (int it = 0; it < k_iters; ++it, ++g) {
+          const int stage = (int)(g % STAGES);
+          const uint32_t phase = (uint32_t)((g / STAGES) & 1);
+          if (g >= STAGES && !mbar_wait(&empty[stage], phase ^ 1)) {
+            atomicExch(p.status, 1);
+            *abort_flag = 1;
           }
-          tma_load_3d(sA + pp * CF::A_BYTES, &tmA, &full[stage], kb * BK, row_a0, za);
-          tma_load_3d(sB + pp * CF::B_BYTES, &tmB, &full[stage], kb * BK, row_b0, zb);
-        }
-        if (++stage == STAGES) {
-          stage = 0;
-          phase ^= 1;
+          if (*abort_flag) break;
+          const int kb = it % p.k_blocks;
+          const int c = it / p.k_blocks;
+          uint8_t* sA = sbase + stage * CF::STAGE_BYTES;
+          uint8_t* sB = sA + MAX_PARTS * CF::A_BYTES;
+          mbar_expect_tx(&full[stage], n_parts * (CF::A_BYTES + CF::B_BYTES));
+          for (int pp = 0; pp < n_parts; ++pp) {
+            int za, zb;
+            if (!OP_IS_A) {
+              za = (tc.field * 3 + pp) * 2 + c;
+              zb = (slot * 3 + pp) * 3 + sel_plane(tc.d, c);
+            } else {
+              za = (slot * 3 + pp) * 3 + sel_plane(tc.d, c);
+              zb = (tc.field * 3 + pp) * 2 + c;
+            }
+            tma_load_3d(sA + pp * CF::A_BYTES, &tmA, &full[stage], kb * BK, tc.row_a0, za);
+            tma_load_3d(sB + pp * CF::B_BYTES, &tmB, &full[stage], kb * BK, tc.row_b0, zb);
+          }
         }
       }
     }
     __syncwarp();
   } else if (warp == MMA_WARP) {
     if (lane == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
-      bool aborted = false;
-      for (int it = 0; it < k_iters; ++it) {
-        const int ts = it % NSLOT;
-        const uint32_t round = (uint32_t)(it / NSLOT);
-        bool ok = true;
-        if (it >= NSLOT) ok = mbar_wait(&tempty[ts], (round & 1u) ^ 1u);
-        if (ok) ok = mbar_wait(&full[stage], phase);
-        if (!ok || *abort_flag) {
-          atomicExch(p.status, 2);
-          *abort_flag = 1;
-          // let the products already issued finish before tensor memory is
-          // released (bounded wait), then release every drain wait so nobody
-          // waits for the full budget again
-          umma_commit(quiesce);
-          mbar_wait(quiesce, 0);
-          for (int s = 0; s < NSLOT; ++s)
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tfull[s]))
-                         : "memory");
-          aborted = true;
-          break;
+      long long g = 0;
+      int j = 0;  // tiles done by this CTA
+      bool ok = true;
+      for (int t = blockIdx.x; t < n_tiles_total && ok; t += gridDim.x, ++j) {
+        for (int it = 0; it < k_iters; ++it, ++g) {
+          const int stage = (int)(g % STAGES);
+          const uint32_t phase = (uint32_t)((g / STAGES) & 1);
+          const int ts = (int)(g % NSLOT);
+          const uint32_t round = (uint32_t)((g / NSLOT) & 1);
+          if (g >= NSLOT) ok = mbar_wait(&tempty[ts], round ^ 1u);
+          if (ok) ok = mbar_wait(&full[stage], phase);
+          // the previous tile's persistent groups must be read before this
+          // tile's first products overwrite them
+          if (ok && it == 0 && j > 0) ok = mbar_wait(gfree, (uint32_t)((j - 1) & 1));
+          if (!ok || *abort_flag) {
+            ok = false;
+            atomicExch(p.status, 2);
+            *abort_flag = 1;
+            // let the products already issued finish before tensor memory
+            // is released (bounded wait), then release the drain warps' waits
+            umma_commit(quiesce);
+            mbar_wait(quiesce, 0);
+            for (int s = 0; s < NSLOT; ++s) mbar_arrive(&tfull[s]);
+            mbar_arrive(gdone);
+            break;
+          }
+          tc_fence_after();
+          // descriptors of the stage's part tiles: the start-address field is
+          // (address >> 4), so offsets are added to it directly (shared
+          // addresses stay below 2^18: no carry out of the 14-bit field)
+          const uint32_t a0 = smem_u32(sbase + stage * CF::STAGE_BYTES);
+          const uint64_t da = smem_desc(a0), db = smem_desc(a0 + MAX_PARTS * CF::A_BYTES);
+          // One thread issues every product of the block, so the issue loop
+          // is fully unrolled over the fixed term order (descriptor offsets
+          // and accumulate flags are constants; only the first products of
+          // the persistent groups depend on it). Group 0 goes first and its
+          // slot is committed to the drain warps while the smaller groups
+          // are multiplied.
+          const uint32_t d0 = t_rot + (uint32_t)(ts * BN);
+          issue_block<0, 1, CF>(da, db, d0, t_g1, t_g2, it == 0);
+          umma_commit(&tfull[ts]);
+          if (p.n_terms == 6)
+            issue_block<1, 6, CF>(da, db, d0, t_g1, t_g2, it == 0);
+          else
+            issue_block<1, 3, CF>(da, db, d0, t_g1, t_g2, it == 0);
+          umma_commit(&empty[stage]);
         }
-        tc_fence_after();
-        // descriptors of the stage's part tiles: the start-address field is
-        // (address >> 4), so offsets are added to it directly (shared
-        // addresses stay below 2^18: no carry out of the 14-bit field)
-        const uint32_t a0 = smem_u32(sbase + stage * CF::STAGE_BYTES);
-        const uint64_t da = smem_desc(a0), db = smem_desc(a0 + MAX_PARTS * CF::A_BYTES);
-        // One thread issues every product of the block, so the issue loop is
-        // fully unrolled over the fixed term order (descriptor offsets and
-        // accumulate flags are constants; only the first products of the
-        // persistent groups depend on it). Group 0 goes first and its slot is
-        // committed to the drain warps while the smaller groups are multiplied.
-        const uint32_t d0 = t_rot + (uint32_t)(ts * BN);
-        issue_block<0, 1, CF>(da, db, d0, t_g1, t_g2, it == 0);
-        umma_commit(&tfull[ts]);
-        if (p.n_terms == 6)
-          issue_block<1, 6, CF>(da, db, d0, t_g1, t_g2, it == 0);
-        else
-          issue_block<1, 3, CF>(da, db, d0, t_g1, t_g2, it == 0);
-        umma_commit(&empty[stage]);
-        if (++stage == STAGES) {
-          stage = 0;
-          phase ^= 1;
-        }
+        if (ok) umma_commit(gdone);  // the tile's persistent groups are final
       }
-      // every product issued: the persistent groups are final once this fires
-      if (!aborted) umma_commit(quiesce);
     }
     __syncwarp();
   } else {
@@ -452,156 +472,168 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int q = warp & 3, h = warp >> 2;
     const int row = q * 32 + lane;
     const uint32_t lane_off = ((uint32_t)(q * 32) << 16) + (uint32_t)(h * CPW);
-    float acc[CPW];
-#pragma unroll
-    for (int j = 0; j < CPW; ++j) acc[j] = 0.f;
+    uint8_t* stage_w = staging + warp * 4096;  // this warp's fp32 box
+    long long g = 0;
+    int j = 0;
     bool ok = true;
-    for (int it = 0; it < k_iters; ++it) {
-      const int ts = it % NSLOT;
-      const uint32_t round = (uint32_t)(it / NSLOT);
-      ok = mbar_wait(&tfull[ts], round & 1u);
-      ok = __all_sync(0xffffffffu, ok && !*abort_flag);
-      if (!ok) break;
-      tc_fence_after();
-      drain_add<CPW>(t_rot + (uint32_t)(ts * BN) + lane_off, acc);
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0)
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[ts]))
-                     : "memory");
-    }
-    if (ok) {
-      // the persistent groups are complete once the MMA warp's final commit
-      // lands (the group-0 commits do not cover the later groups)
-      ok = mbar_wait(quiesce, 0);
-      ok = __all_sync(0xffffffffu, ok && !*abort_flag);
-    }
-    if (ok) {
-      // add the persistent groups (smaller first: g2 into g1, then into the
-      // accumulator)
-      tc_fence_after();
-      float gsum[CPW];
+    for (int t = blockIdx.x; t < n_tiles_total && ok; t += gridDim.x, ++j) {
+      const TileCoord tc = tile_coord<BN, OP_IS_A>(p, t);
+      const int field = tc.field, d = tc.d, row_a0 = tc.row_a0, row_b0 = tc.row_b0;
+      float acc[CPW];
 #pragma unroll
-      for (int j = 0; j < CPW; ++j) gsum[j] = 0.f;
-      if (p.n_terms > 3) drain_add<CPW>(t_g2 + lane_off, gsum);  // bf16x3 has no group 2
-      drain_add<CPW>(t_g1 + lane_off, gsum);
+      for (int jj = 0; jj < CPW; ++jj) acc[jj] = 0.f;
+      for (int it = 0; it < k_iters; ++it, ++g) {
+        const int ts = (int)(g % NSLOT);
+        const uint32_t round = (uint32_t)((g / NSLOT) & 1);
+        ok = mbar_wait(&tfull[ts], round);
+        ok = __all_sync(0xffffffffu, ok && !*abort_flag);
+        if (!ok) break;
+        tc_fence_after();
+        drain_add<CPW>(t_rot + (uint32_t)(ts * BN) + lane_off, acc);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[ts]);
+      }
+      if (ok) {
+        // the tile's persistent groups are complete once its last commit lands
+        ok = mbar_wait(gdone, (uint32_t)(j & 1));
+        ok = __all_sync(0xffffffffu, ok && !*abort_flag);
+      }
+      if (!ok) {
+        atomicExch(p.status, 3);
+        break;
+      }
+      {
+        // add the persistent groups (smaller first: g2 into g1, then into
+        // the accumulator), then hand their slots to the next tile
+        tc_fence_after();
+        float gsum[CPW];
 #pragma unroll
-      for (int j = 0; j < CPW; ++j) acc[j] += gsum[j];
-    }
-    if (!ok) {
-      atomicExch(p.status, 3);
-    } else if (EPI == EPI_T_SPLIT) {
-      // C[y][u] -> T^T parts [field][part][d][u][y] (bf16)
-      const int y = row_a0 + row;
-      if ((p.out_cols & 1) == 0) {
-        // Lane pairs (y, y + 1) swap one value per two columns, so each lane
-        // holds both rows of one column and stores them as one bf16x2 word:
-        // the even lane column u0 + j, the odd lane column u0 + j + 1. With
-        // an even row count y + 1 is in range whenever the even y is.
-        __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(p.out);
-        const size_t plane2 = (size_t)p.out_rows * p.out_cols / 2;
-        const int odd = lane & 1;
-        const int ye = y - odd;
-        const int u0 = row_b0 + h * CPW + odd;
+        for (int jj = 0; jj < CPW; ++jj) gsum[jj] = 0.f;
+        if (p.n_terms > 3) drain_add<CPW>(t_g2 + lane_off, gsum);  // bf16x3 has no group 2
+        drain_add<CPW>(t_g1 + lane_off, gsum);
 #pragma unroll
-        for (int j = 0; j < CPW; j += 2) {
-          const float send = odd ? acc[j] : acc[j + 1];
-          const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-          const float lo = odd ? recv : acc[j];
-          const float hi = odd ? acc[j + 1] : recv;
-          const int u = u0 + j;
-          if (ye < p.out_cols && u < p.cols_valid) {
-            __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-            split3(lo, a0, a1, a2);
-            split3(hi, b0, b1, b2);
-            const size_t off = ((size_t)u * p.out_cols + ye) / 2;
-            out[((size_t)(field * 3 + 0) * 2 + d) * plane2 + off] = __halves2bfloat162(a0, b0);
-            out[((size_t)(field * 3 + 1) * 2 + d) * plane2 + off] = __halves2bfloat162(a1, b1);
-            out[((size_t)(field * 3 + 2) * 2 + d) * plane2 + off] = __halves2bfloat162(a2, b2);
+        for (int jj = 0; jj < CPW; ++jj) acc[jj] += gsum[jj];
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(gfree);
+      }
+      if (EPI == EPI_T_SPLIT) {
+        // C[y][u] -> T^T parts [field][part][d][u][y] (bf16)
+        const int y = row_a0 + row;
+        if ((p.out_cols & 1) == 0) {
+          // Lane pairs (y, y + 1) swap one value per two columns, so each
+          // lane holds both rows of one column and stores them as one bf16x2
+          // word: the even lane column u0 + jj, the odd lane column
+          // u0 + jj + 1. With an even row count y + 1 is in range whenever
+          // the even y is.
+          __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(p.out);
+          const size_t plane2 = (size_t)p.out_rows * p.out_cols / 2;
+          const int odd = lane & 1;
+          const int ye = y - odd;
+          const int u0 = row_b0 + h * CPW + odd;
+#pragma unroll
+          for (int jj = 0; jj < CPW; jj += 2) {
+            const float send = odd ? acc[jj] : acc[jj + 1];
+            const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+            const float lo = odd ? recv : acc[jj];
+            const float hi = odd ? acc[jj + 1] : recv;
+            const int u = u0 + jj;
+            if (ye < p.out_cols && u < p.cols_valid) {
+              __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+              split3(lo, a0, a1, a2);
+              split3(hi, b0, b1, b2);
+              const size_t off = ((size_t)u * p.out_cols + ye) / 2;
+              out[((size_t)(field * 3 + 0) * 2 + d) * plane2 + off] = __halves2bfloat162(a0, b0);
+              out[((size_t)(field * 3 + 1) * 2 + d) * plane2 + off] = __halves2bfloat162(a1, b1);
+              out[((size_t)(field * 3 + 2) * 2 + d) * plane2 + off] = __halves2bfloat162(a2, b2);
+            }
+          }
+        } else if (y < p.out_cols) {
+          __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+          const size_t plane = (size_t)p.out_rows * p.out_cols;
+          const int u0 = row_b0 + h * CPW;
+#pragma unroll
+          for (int jj = 0; jj < CPW; ++jj) {
+            const int u = u0 + jj;
+            if (u < p.cols_valid) {
+              __nv_bfloat16 h0, h1, h2;
+              split3(acc[jj], h0, h1, h2);
+              const size_t off = (size_t)u * p.out_cols + y;
+              out[((size_t)(field * 3 + 0) * 2 + d) * plane + off] = h0;
+              out[((size_t)(field * 3 + 1) * 2 + d) * plane + off] = h1;
+              out[((size_t)(field * 3 + 2) * 2 + d) * plane + off] = h2;
+            }
           }
         }
-      } else if (y < p.out_cols) {
-        __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
-        const size_t plane = (size_t)p.out_rows * p.out_cols;
-        const int u0 = row_b0 + h * CPW;
-#pragma unroll
-        for (int j = 0; j < CPW; ++j) {
-          const int u = u0 + j;
-          if (u < p.cols_valid) {
-            __nv_bfloat16 h0, h1, h2;
-            split3(acc[j], h0, h1, h2);
-            const size_t off = (size_t)u * p.out_cols + y;
-            out[((size_t)(field * 3 + 0) * 2 + d) * plane + off] = h0;
-            out[((size_t)(field * 3 + 1) * 2 + d) * plane + off] = h1;
-            out[((size_t)(field * 3 + 2) * 2 + d) * plane + off] = h2;
-          }
-        }
-      }
-    } else if (p.tma_out) {
-      // Every product has completed and every operand load was consumed, so
-      // the operand ring is free: each warp stages its 32 x CPW block as
-      // CPW / 32 boxes of 32 x 32 fp32 in the TMA 128B-swizzled layout (16-byte
-      // chunk c of row r at chunk c ^ (r & 7): conflict-free) and one lane
-      // stores them (or adds them into the window), clipped to the window.
-      uint8_t* stage_w = sbase + (size_t)warp * (CPW * 32 * 4);
-#pragma unroll
-      for (int b = 0; b < CPW / 32; ++b) {
-        uint8_t* box = stage_w + b * 4096 + lane * 128;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          const float* a = acc + b * 32 + c * 4;
-          *reinterpret_cast<float4*>(box + ((c ^ (lane & 7)) << 4)) =
-              make_float4(a[0], a[1], a[2], a[3]);
-        }
-      }
-      fence_proxy_async_smem();
-      __syncwarp();
-      if (lane == 0) {
-        const int v0 = row_a0 + q * 32, z = field * 2 + d;
+      } else if (p.tma_out) {
+        // Each warp stages its 32 x CPW block one 32 x 32 fp32 box at a time
+        // in its own 4 KB of the staging region, in the TMA 128B-swizzled
+        // layout (16-byte chunk c of row r at chunk c ^ (r & 7):
+        // conflict-free), and one lane stores the box (or adds it into the
+        // window), clipped to the window; the box is rewritten only after
+        // the previous copy has read it.
 #pragma unroll
         for (int b = 0; b < CPW / 32; ++b) {
-          const int u = row_b0 + h * CPW + b * 32;
-          if (p.accumulate)
-            tma_reduce_add_3d(&tmO, stage_w + b * 4096, u, v0, z);
-          else
-            tma_store_3d(&tmO, stage_w + b * 4096, u, v0, z);
-        }
-        bulk_commit();
-        bulk_wait_read_all();
-      }
-      __syncwarp();
-    } else {
-      // C[v][u] -> out fp32 [field][d][out_r0 + v][out_c0 + u] (pitch out_pitch)
-      const int v = row_a0 + row;
-      if (v < p.rows_valid) {
-        float* out = reinterpret_cast<float*>(p.out) +
-                     ((size_t)(field * 2 + d) * p.out_plane_rows + p.out_r0 + v) * p.out_pitch +
-                     p.out_c0;
-        const int u0 = row_b0 + h * CPW;
-        if (u0 + CPW <= p.cols_valid && ((p.out_pitch | p.out_c0) & 3) == 0) {
-          float4* o4 = reinterpret_cast<float4*>(out + u0);
+          if (lane == 0) bulk_wait_read_all();
+          __syncwarp();
+          uint8_t* box = stage_w + lane * 128;
 #pragma unroll
-          for (int j = 0; j < CPW / 4; ++j) {
-            float4 val = make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]);
-            if (p.accumulate) {
-              const float4 old = o4[j];
-              val.x += old.x; val.y += old.y; val.z += old.z; val.w += old.w;
-            }
-            o4[j] = val;
+          for (int c = 0; c < 8; ++c) {
+            const float* a = acc + b * 32 + c * 4;
+            *reinterpret_cast<float4*>(box + ((c ^ (lane & 7)) << 4)) =
+                make_float4(a[0], a[1], a[2], a[3]);
           }
-        } else {
+          fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) {
+            const int u = row_b0 + h * CPW + b * 32;
+            const int v0 = row_a0 + q * 32, z = field * 2 + d;
+            if (p.accumulate)
+              tma_reduce_add_3d(&tmO, stage_w, u, v0, z);
+            else
+              tma_store_3d(&tmO, stage_w, u, v0, z);
+            bulk_commit();
+          }
+        }
+      } else {
+        // C[v][u] -> out fp32 [field][d][out_r0 + v][out_c0 + u] (pitch out_pitch)
+        const int v = row_a0 + row;
+        if (v < p.rows_valid) {
+          float* out = reinterpret_cast<float*>(p.out) +
+                       ((size_t)(field * 2 + d) * p.out_plane_rows + p.out_r0 + v) *
+                           p.out_pitch +
+                       p.out_c0;
+          const int u0 = row_b0 + h * CPW;
+          if (u0 + CPW <= p.cols_valid && ((p.out_pitch | p.out_c0) & 3) == 0) {
+            float4* o4 = reinterpret_cast<float4*>(out + u0);
 #pragma unroll
-          for (int j = 0; j < CPW; ++j) {
-            const int u = u0 + j;
-            if (u < p.cols_valid) {
-              float val = acc[j];
-              if (p.accumulate) val += out[u];
-              out[u] = val;
+            for (int jj = 0; jj < CPW / 4; ++jj) {
+              float4 val = make_float4(acc[4 * jj], acc[4 * jj + 1], acc[4 * jj + 2],
+                                       acc[4 * jj + 3]);
+              if (p.accumulate) {
+                const float4 old = o4[jj];
+                val.x += old.x; val.y += old.y; val.z += old.z; val.w += old.w;
+              }
+              o4[jj] = val;
+            }
+          } else {
+#pragma unroll
+            for (int jj = 0; jj < CPW; ++jj) {
+              const int u = u0 + jj;
+              if (u < p.cols_valid) {
+                float val = acc[jj];
+                if (p.accumulate) val += out[u];
+                out[u] = val;
+              }
             }
           }
         }
       }
     }
+    // the staged boxes must be read before the CTA's shared memory goes
+    if (EPI == EPI_F32 && lane == 0) bulk_wait_read_all();
+    __syncwarp();
   }
   tc_fence_before();
   __syncthreads();
