@@ -541,9 +541,8 @@ def main():
 
 # dram__bytes_read.sum + dram__bytes_write.sum per k_split_gemm launch,
 # averaged over the six GEMM launches of one step, keyed by fields per step:
-# an ncu capture at 32 fields (1157.7 MB per step) scaled by the field count
-# (profiles/k_split_gemm_piaacmc1024_32fields.md).
-TRAFFIC: dict = {64: 385.9e6, 32: 192.9e6}
+# an ncu capture at 32 fields (1153.1 MB per step) scaled by the field count.
+TRAFFIC: dict = {64: 384.4e6, 32: 192.2e6}
 
 if __name__ == "__main__":
     sys.exit(main())

@@ -243,14 +243,16 @@ int csg_chain_add_mask(csg_chain* c, const float* mask, int ref_quirk, int disab
   return CSG_OK;
 }
 
-// out[s][p] = mask[p] * tab[s][p] for every wavelength slot s.
+// out[s][p] = mask[p] * tab[s][p] for every wavelength slot s; with quirk
+// the mask multiplies as m (1 + i), as the mask element applies it.
 __global__ void k_mask_times_table(const float* __restrict__ mask, const float2* __restrict__ tab,
-                                   long long plane, long long total, float2* __restrict__ out) {
+                                   long long plane, long long total, int quirk,
+                                   float2* __restrict__ out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const float m = mask[i % plane];
     const float2 w = tab[i];
-    out[i] = make_float2(m * w.x, m * w.y);
+    out[i] = quirk ? make_float2(m * (w.x - w.y), m * (w.x + w.y)) : make_float2(m * w.x, m * w.y);
   }
 }
 
@@ -271,12 +273,12 @@ int csg_chain_add_mirror(csg_chain* c, const float* sag, double sign) {
                               e.tab);
   if (rc) return rc;
   // after a real mask the walk applies both with one table read per pixel
-  if (!c->elems.empty() && c->elems.back().kind == E_MASK && !c->elems.back().quirk) {
+  if (!c->elems.empty() && c->elems.back().kind == E_MASK) {
     e.tab_m = dev_copy<float2>(nullptr, plane * c->n_lambda, c->ctx->stream);
     CSG_CHECK(e.tab_m, CSG_E_NOMEM, "csg_chain_add_mirror: allocation failed");
     const long long total = (long long)plane * c->n_lambda;
     k_mask_times_table<<<grid_for(total, 256), 256, 0, c->ctx->stream>>>(
-        c->elems.back().a, e.tab, (long long)plane, total, e.tab_m);
+        c->elems.back().a, e.tab, (long long)plane, total, c->elems.back().quirk, e.tab_m);
     CSG_LAUNCH_CHECK();
   }
   c->elems.push_back(e);
