@@ -201,12 +201,14 @@ def setup_piaacmc(args, ctx, W, cg, rank):
 def setup_plain_lyot(args, ctx, W, cg, rank):
     """Plain Lyot coronagraph (512^2 pupil, 2048^2 padded-FFT occulter, 0.9
     Lyot stop, 128^2 final MFT): a batch of point sources at random offsets
-    within 4 lambda/D, uploaded every step."""
+    within 4 lambda/D, uploaded every step. The occulter runs in its Babinet
+    form (an MFT pair over the support of 1 - mask) unless --fft-occulter."""
     import torch
     wl = Workload()
     spec = W.PlainLyotSpec()
     B = args.fields
-    cor, inp = W.build_plain_lyot(ctx, spec, precision=args.precision)
+    cor, inp = W.build_plain_lyot(ctx, spec, precision=args.precision,
+                                  fft_fpm_babinet=not args.fft_occulter)
     cor.batch_all(1)
     cal = cor.execute(calibrating=True)
     reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 3.0, 12.0)
@@ -234,12 +236,16 @@ def setup_plain_lyot(args, ctx, W, cg, rank):
         return n / dt, n, dt
     wl.cpu = cpu
     wl.cpu_sample = "FP64 numpy/scipy: 2048^2 FFT occulter + direct MFT"
-    wl.bound = "hbm"
+    # the occulter's Babinet form runs on the MFT GEMMs; its padded FFT on the FFT passes
+    wl.bound = "hbm" if args.fft_occulter else "tensor"
     wl.config = {"workload": "plain-lyot-512: 512^2 pupil (r = 200 px, 0.3 obstruction), "
                              "Zernike 4-15 at 10 nm RMS, 2048^2 FFT, 3 lambda/D occulter, "
                              "Lyot 0.9, 128^2 MFT at 0.25 lambda/D",
                  "fields_per_step": B, "n": spec.n, "pad": spec.pad, "image": cor.n_out,
-                 "l2": "working set > L2 (padded fields 2 GB at 64 fields)"}
+                 "occulter": ("padded 2048^2 FFT" if args.fft_occulter else
+                              "Babinet form: MFT pair over the support box of 1 - mask"),
+                 "l2": "working set > L2 (fields 134 MB at 64 fields; padded 2 GB with the "
+                       "FFT occulter)"}
     return wl
 
 
@@ -340,6 +346,9 @@ def main():
                     help="piaacmc (headline), plain_lyot, broadband, de")
     ap.add_argument("--precision", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fft-occulter", action="store_true",
+                    help="plain_lyot: keep the occulter as a padded 2048^2 FFT instead of its "
+                         "Babinet form (the MFT pair over the support of 1 - mask)")
     ap.add_argument("--no-crop", action="store_true",
                     help="transform the whole 512^2 FPM grid instead of the mask's support")
     args = ap.parse_args()

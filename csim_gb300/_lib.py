@@ -93,6 +93,7 @@ SIGNATURES = {
     "csg_dm_destroy": ([P], None),
     "csg_dm_surface": ([P, P, P], None),
     "csg_chain_set_support_crop": ([P, I], None),
+    "csg_chain_set_fft_fpm_babinet": ([P, I], None),
     "csg_chain_fpm_region": ([P, I, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)], None),
     "csg_chain_set_batch": ([P, I, P, P, P, P, P], None),
     "csg_chain_sags": ([P, I, I, C.POINTER(P)], None),

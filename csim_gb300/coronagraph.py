@@ -124,7 +124,8 @@ class Coronagraph:
     image fields as a planar fp32 tensor [F, 2, n_out, n_out]."""
 
     def __init__(self, ctx: Context, tel: Telescope, ef: EField, elements: list,
-                 precision: int = CSG_PREC_BF16X6, support_crop: bool = True):
+                 precision: int = CSG_PREC_BF16X6, support_crop: bool = True,
+                 fft_fpm_babinet: bool = True):
         self.ctx, self.tel, self.ef, self.elements = ctx, tel, ef, elements
         lam = np.ascontiguousarray(ef.wavelengths, dtype=np.float64)
         h = C.c_void_p()
@@ -132,6 +133,7 @@ class Coronagraph:
              lam.ctypes.data_as(C.c_void_p), precision)
         self.h = h
         call("csg_chain_set_support_crop", self.h, int(support_crop))
+        call("csg_chain_set_fft_fpm_babinet", self.h, int(fft_fpm_babinet))
         self.n_hex = None
         self.n_out = None
         self.out_pixel = None

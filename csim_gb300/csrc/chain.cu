@@ -88,6 +88,13 @@ struct Elem {
   std::vector<int> n_out_l;  // ragged: per-wavelength image size (n_out = the largest)
   // padded-FFT focal-plane mask: P x P grid
   int P = 0;
+  // its Babinet form: 1 - M vanishes outside the mask-index box
+  // [br0, br0 + bR) x [bc0, bc0 + bC); bab = 1 runs it as a pair of MFTs
+  // (mft1: field -> box spectrum, mft2: back, times 1 - M, subtracted),
+  // bab = 2: M = 1 everywhere (the identity), bab = 0: the padded FFT
+  int bab = 0;
+  int br0 = 0, bc0 = 0, bR = 0, bC = 0;
+  float* dmask = nullptr;  // [L][2][bR][bC] planar: 1 - M on the box
   // per-wavelength tables (mirror phasors, Fresnel transfer function)
   float2* tab = nullptr;
   // mirror right after a real mask: the mask times the phasor table
@@ -114,6 +121,7 @@ struct csg_chain {
   double* lam_slots = nullptr;  // device copy of lambda (one per slot)
   int precision = 6;
   bool crop_support = true;
+  bool fft_fpm_babinet = true;  // padded-FFT occulters in Babinet form when compact
   bool planned = false;  // lazily built transforms are up to date
   std::vector<Elem> elems;
   // batch description (device)
@@ -202,6 +210,7 @@ int csg_chain_destroy(csg_chain* c) {
     cudaFree(e.count);
     cudaFree(e.tab);
     cudaFree(e.tab_m);
+    cudaFree(e.dmask);
     csg_mft_destroy(e.mft1);
     csg_mft_destroy(e.mft2);
     csg_mft_destroy(e.mft);
@@ -449,7 +458,63 @@ int csg_chain_add_fft_fpm(csg_chain* c, int pad, const float* mask_re, const flo
       }
   e.tab = dev_copy(h.data(), h.size(), c->ctx->stream);
   CSG_CHECK(e.tab, CSG_E_NOMEM, "csg_chain_add_fft_fpm: allocation failed");
-  CSG_CUDA(cudaStreamSynchronize(c->ctx->stream));  // the host staging buffer goes away
+  if (c->fft_fpm_babinet) {
+    // Babinet form: E - crop(ifft((1 - M) fft(embed(E)))). Where 1 - M has a
+    // small support only those frequencies enter, and both transforms are
+    // exact DFT sums over them: an MFT from the field's padded-grid pixels
+    // to the support box and one back (integer coordinates, period pad).
+    int r0 = pad, r1 = 0, c0 = pad, c1 = 0;
+    for (int l = 0; l < c->n_lambda; ++l)
+      for (int r = 0; r < pad; ++r)
+        for (int cc = 0; cc < pad; ++cc) {
+          const size_t src = l * plane + (size_t)r * pad + cc;
+          if (mask_re[src] != 1.f || (mask_im && mask_im[src] != 0.f)) {
+            r0 = std::min(r0, r);
+            r1 = std::max(r1, r + 1);
+            c0 = std::min(c0, cc);
+            c1 = std::max(c1, cc + 1);
+          }
+        }
+    if (r1 <= r0) {
+      e.bab = 2;
+    } else {
+      // box sides rounded up to multiples of 8 (the transforms' TMA extents)
+      const int R = std::min(pad, (r1 - r0 + 7) / 8 * 8), C = std::min(pad, (c1 - c0 + 7) / 8 * 8);
+      r0 = std::min(r0, pad - R);
+      c0 = std::min(c0, pad - C);
+      if ((size_t)R * C * 16 <= plane && R <= 1024 && C <= 1024) {
+        e.bab = 1;
+        e.br0 = r0;
+        e.bc0 = c0;
+        e.bR = R;
+        e.bC = C;
+        const int L = c->n_lambda;
+        std::vector<float> d((size_t)L * 2 * R * C);
+        for (int l = 0; l < L; ++l)
+          for (int r = 0; r < R; ++r)
+            for (int cc = 0; cc < C; ++cc) {
+              const size_t src = l * plane + (size_t)(r0 + r) * pad + (c0 + cc);
+              const size_t o = ((size_t)l * 2 * R + r) * C + cc;
+              d[o] = (float)(1.0 - (double)mask_re[src]);
+              d[o + (size_t)R * C] = mask_im ? -mask_im[src] : 0.f;
+            }
+        e.dmask = dev_copy(d.data(), d.size(), c->ctx->stream);
+        CSG_CHECK(e.dmask, CSG_E_NOMEM, "csg_chain_add_fft_fpm: allocation failed");
+        // field pixel y sits at padded index (pad - n)/2 + y; mask index j is
+        // frequency j - pad/2
+        const int n = c->n, lo = (pad - n) / 2;
+        std::vector<double> pin(n), fy(R), fx(C), lf(L, (double)pad), pref(2 * L, 0.0);
+        for (int y = 0; y < n; ++y) pin[y] = lo + y;
+        for (int r = 0; r < R; ++r) fy[r] = r0 + r - pad / 2;
+        for (int cc = 0; cc < C; ++cc) fx[cc] = c0 + cc - pad / 2;
+        for (int l = 0; l < L; ++l) pref[2 * l] = 1.0;
+        int rc = csg_mft_create(c->ctx, &e.mft1, n, n, R, C, pin.data(), pin.data(), fy.data(),
+                                fx.data(), L, lf.data(), pref.data(), -1.0, c->precision);
+        if (rc) return rc;
+      }
+    }
+  }
+  CSG_CUDA(cudaStreamSynchronize(c->ctx->stream));  // the host staging buffers go away
   c->elems.push_back(e);
   c->planned = false;
   drop_graph(c);
@@ -458,6 +523,12 @@ int csg_chain_add_fft_fpm(csg_chain* c, int pad, const float* mask_re, const flo
 
 // Whether hex focal-plane masks added after this call run their transforms on
 // the mask's support only (default on; the result is the same either way).
+int csg_chain_set_fft_fpm_babinet(csg_chain* c, int enable) {
+  CSG_CHECK(c, CSG_E_ARG, "csg_chain_set_fft_fpm_babinet: null chain");
+  c->fft_fpm_babinet = enable != 0;
+  return CSG_OK;
+}
+
 int csg_chain_set_support_crop(csg_chain* c, int enable) {
   CSG_CHECK(c, CSG_E_ARG, "csg_chain_set_support_crop: null chain");
   c->crop_support = enable != 0;
@@ -576,6 +647,26 @@ static int build_plans(csg_chain* c) {
       e.win = MftWindow{w.r0, w.c0, n, n};  // output window of the n x n field
       e.win_rows = w.rows;
       e.win_cols = w.pitch;
+    } else if (e.kind == E_FFT_FPM && e.bab == 1) {
+      int j = i + 1;
+      while (j < ne && is_pointwise(c->elems[j].kind)) ++j;
+      MftWindow w = (j < ne && c->elems[j].kind == E_FRAUNHOFER) ? stop_window(c, i, j)
+                                                                 : MftWindow{0, 0, n, n};
+      const int lo = (e.P - n) / 2;
+      std::vector<double> fy(e.bR), fx(e.bC), py(w.rows), px(w.pitch), lf(L, (double)e.P);
+      std::vector<double> pref(2 * L, 0.0);
+      for (int r = 0; r < e.bR; ++r) fy[r] = e.br0 + r - e.P / 2;
+      for (int cc = 0; cc < e.bC; ++cc) fx[cc] = e.bc0 + cc - e.P / 2;
+      for (int r = 0; r < w.rows; ++r) py[r] = lo + w.r0 + r;
+      for (int cc = 0; cc < w.pitch; ++cc) px[cc] = lo + w.c0 + cc;
+      for (int l = 0; l < L; ++l) pref[2 * l] = -1.0 / ((double)e.P * e.P);  // E - ifft(...)
+      csg_mft_destroy(e.mft2);
+      e.mft2 = nullptr;
+      int rc = csg_mft_create(c->ctx, &e.mft2, e.bR, e.bC, w.rows, w.pitch, fy.data(), fx.data(),
+                              py.data(), px.data(), L, lf.data(), pref.data(), +1.0,
+                              c->precision);
+      if (rc) return rc;
+      e.win = MftWindow{w.r0, w.c0, n, n};  // output window of the n x n field
     } else if (e.kind == E_FRAUNHOFER) {
       int k = i - 1;
       while (k >= 0 && is_pointwise(c->elems[k].kind)) --k;
@@ -701,7 +792,12 @@ static int prepare(csg_chain* c) {
       int rc = csg_mft_reserve(e.mft1, c->n_fields);
       if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
       if (rc) return rc;
-    } else if (e.kind == E_FFT_FPM) {
+    } else if (e.kind == E_FFT_FPM && e.bab == 1) {
+      fpm_need = std::max(fpm_need, F * 2 * (size_t)e.bR * e.bC * sizeof(float));
+      int rc = csg_mft_reserve(e.mft1, c->n_fields);
+      if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
+      if (rc) return rc;
+    } else if (e.kind == E_FFT_FPM && e.bab == 0) {
       pad_need = std::max(pad_need, F * 2 * (size_t)e.P * e.P * sizeof(float));
     } else if (e.kind == E_FRAUNHOFER) {
       img_need = std::max(img_need, F * 2 * e.n_out * e.n_out * sizeof(float));
@@ -858,6 +954,16 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         break;
       case Step::FFT_FPM: {
         const Elem& e = *s.e;
+        if (e.bab) {
+          // the element's ops first (the Babinet term subtracts from E itself)
+          if (s.pro.n) rc = pixops_pass(ctx->stream, c->field, F, n, n, s.pro, fi);
+          if (!rc && e.bab == 1)
+            rc = csg_mft_execute(ctx, e.mft1, c->field, c->fpm, F, c->slot, 0, nullptr, nullptr);
+          if (!rc && e.bab == 1)
+            rc = mft_execute_ops(ctx, e.mft2, c->fpm, c->field, F, c->slot, 1, e.dmask, c->slot,
+                                 PixOps(), fi, nullptr, &e.win);
+          break;
+        }
         FresnelArgs fa{c->lam_f, 0.0, 1.0, e.tab, c->slot};  // H = the mask table
         const int lo = (e.P - n) / 2;
         if (fft_band_supported(e.P, lo, n)) {

@@ -59,9 +59,11 @@ def build_piaacmc(ctx: Context, spec: PiaacmcSpec, sources=None, precision: int 
     return cor, a
 
 
-def build_plain_lyot(ctx: Context, spec: PlainLyotSpec, sources=None, precision: int = 6):
+def build_plain_lyot(ctx: Context, spec: PlainLyotSpec, sources=None, precision: int = 6,
+                     fft_fpm_babinet: bool = True):
     """Plain Lyot coronagraph chain: pupil -> aberration -> padded-FFT
-    occulter -> Lyot stop -> final MFT. Returns (coronagraph, inputs)."""
+    occulter -> Lyot stop -> final MFT. Returns (coronagraph, inputs).
+    fft_fpm_babinet = False keeps the occulter as a padded FFT."""
     a = plain_lyot_arrays(spec, sources)
     elems = [
         cg.Mask(a["pupil"]),
@@ -70,7 +72,8 @@ def build_plain_lyot(ctx: Context, spec: PlainLyotSpec, sources=None, precision:
         cg.Mask(a["lyot"]),
         cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov),
     ]
-    cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision)
+    cor = cg.Coronagraph(ctx, a["tel"], a["ef"], elems, precision,
+                         fft_fpm_babinet=fft_fpm_babinet)
     return cor, a
 
 

@@ -278,6 +278,14 @@ int csg_chain_fpm_region(csg_chain* chain, int idx, int* r0, int* c0, int* rows,
  * focal coordinates (index pad/2 is zero frequency); pad a power of two >= N. */
 int csg_chain_add_fft_fpm(csg_chain* chain, int pad, const float* mask_re, const float* mask_im,
                           int disable_for_calibration);
+/* Padded-FFT occulters added after this call run in Babinet form when
+ * 1 - mask is nonzero only on a box of at most 1/16 of the pad x pad grid
+ * (sides rounded up to multiples of 8): E - crop(ifft((1 - M) fft(embed(E))))
+ * with both transforms evaluated as exact DFT sums over the box's
+ * frequencies (two MFTs, the return one writing only the window of the stops
+ * that follow, as for hex FPMs); a mask of ones is the identity. enable = 0
+ * keeps the padded FFT. Default 1. */
+int csg_chain_set_fft_fpm_babinet(csg_chain* chain, int enable);
 /* fraunhoferFocal (fraunhoferFocal.cpp:23-72): zoomFft to n_out x n_out at
  * out_pixel (= loD / samplesPerflD), lambda f = lambda lf_scale with
  * lf_scale = 2 beamRadius primaryfRatio. Must be the last element. */

@@ -18,8 +18,11 @@ def _cplx(t):
     return t[:, 0].double().cpu().numpy() + 1j * t[:, 1].double().cpu().numpy()
 
 
-@pytest.mark.parametrize("full", [False, True])
-def test_plain_lyot_matches_oracle(ctx, full):
+@pytest.mark.parametrize("full,babinet", [(False, True), (False, False), (True, True),
+                                          (True, False)])
+def test_plain_lyot_matches_oracle(ctx, full, babinet):
+    """Both forms of the occulter: the Babinet pair of MFTs over the support
+    of 1 - M (the default for a compact occulter) and the padded FFT."""
     from csim_gb300 import coronagraph as cg
     from csim_gb300 import workloads as W
     if full:
@@ -29,7 +32,7 @@ def test_plain_lyot_matches_oracle(ctx, full):
         spec = W.PlainLyotSpec(n=128, pad=512, radius_px=50.0, wavelengths=(530e-9, 570e-9),
                                n_out_fov=16.0)
         sources = [cg.PointSource(1.0, 0.0, 0.0), cg.PointSource(0.5, 0.3, -0.2)]
-    cor, inp = W.build_plain_lyot(ctx, spec, sources)
+    cor, inp = W.build_plain_lyot(ctx, spec, sources, fft_fpm_babinet=babinet)
     F = cor.batch_all(1)
     img_t = cor.execute(calibrating=False).clone()
     img = _cplx(img_t)
