@@ -199,14 +199,15 @@ __device__ __forceinline__ int sel_plane(int d, int c) {
 // every instruction, so a long chain of the dominant product in tensor
 // memory would shrink the result by ~2^-24 per instruction. The products of
 // the three-way split are therefore grouped by magnitude (part indices
-// pa + pb): group 0 (hi x hi) goes to a fresh tensor-memory slot every K
-// block (two slots rotate) and eight drain warps add each finished slot into
-// fp32 registers with round-to-nearest adds while the rest of the block and
-// the next block are multiplied (each block issues group 0 first and commits
-// its slot before the smaller groups); group 1 (hi x mid, mid x hi, 2^-8 of the result) and group 2
-// (the 2^-16 terms) accumulate over the whole K range in two persistent
-// slots, where the truncation is relative to their own small magnitude, and
-// are added once at the end.
+// pa + pb): hi x hi goes to a fresh tensor-memory slot every K block (three
+// slots rotate) and eight drain warps add each finished slot into fp32
+// registers with round-to-nearest adds while the rest of the block and the
+// next blocks are multiplied (each block issues hi x hi first and commits
+// its slot before the smaller products); the smaller products (hi x mid,
+// mid x hi: 2^-8 of the result; the 2^-16 terms) accumulate over the whole K
+// range in one persistent slot, where the truncation is relative to their
+// own small magnitude (the 2^-16 terms lose only bits below 2^-32 of the
+// result there), and are added once at the end of the tile.
 //
 // Operand traffic. A pipeline stage holds every split part of the A and B
 // tiles of one K block (3 + 3 tiles for bf16x6), and all the products of
@@ -232,7 +233,7 @@ struct Cfg {
   static constexpr uint32_t STAGING_BYTES = EPI == 1 ? DRAIN_WARPS * 4096 : 0;
   // 192 KB (+ 32 KB staging) at N = 128; 216 KB or 144 KB (+ 32 KB) at 64
   static constexpr int STAGES = BN == 128 ? 2 : (EPI == 1 ? 2 : 3);
-  static constexpr int TMEM_COLS = 4 * BN;          // group 1, group 2, two rotating slots
+  static constexpr int TMEM_COLS = 4 * BN;          // small groups, three rotating slots
   static constexpr int COLS_PER_WARP = BN / 2;      // two warps share a lane quadrant
   static constexpr int BN_ = BN;
   static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + STAGING_BYTES + 1024 + 512;
@@ -265,9 +266,8 @@ __device__ __forceinline__ void drain_add(uint32_t taddr, float* acc) {
 // (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
 __host__ __device__ constexpr int term_a(int i) { return i == 2 || i == 4 ? 1 : (i == 5 ? 2 : 0); }
 __host__ __device__ constexpr int term_b(int i) { return i == 1 || i == 4 ? 1 : (i == 3 ? 2 : 0); }
-__host__ __device__ constexpr int term_group(int i) {
-  return term_a(i) + term_b(i) < 2 ? term_a(i) + term_b(i) : 2;
-}
+// hi x hi (group 0) and the smaller products (groups 1 and 2, one slot)
+__host__ __device__ constexpr int term_group(int i) { return term_a(i) + term_b(i) == 0 ? 0 : 1; }
 __host__ __device__ constexpr bool first_of_group(int i) {
   for (int j = 0; j < i; ++j)
     if (term_group(j) == term_group(i)) return false;
@@ -275,16 +275,16 @@ __host__ __device__ constexpr bool first_of_group(int i) {
 }
 
 // Every product of one K block: group 0 into the block's rotating slot d0
-// (fresh), groups 1 and 2 into their persistent slots (fresh only for the
-// first product of the first block).
+// (fresh), the smaller products into the persistent slot t_gs (fresh only
+// for the first of them in the first block).
 template <int I0, int NT, class CF>
-__device__ __forceinline__ void issue_block(uint64_t da, uint64_t db, uint32_t d0, uint32_t t_g1,
-                                            uint32_t t_g2, bool first_block) {
+__device__ __forceinline__ void issue_block(uint64_t da, uint64_t db, uint32_t d0, uint32_t t_gs,
+                                            bool first_block) {
   constexpr uint32_t idesc = instr_desc(BM, CF::BN_);
 #pragma unroll
   for (int i = I0; i < NT; ++i) {
     const int g = term_group(i);
-    const uint32_t dcol = g == 0 ? d0 : (g == 1 ? t_g1 : t_g2);
+    const uint32_t dcol = g == 0 ? d0 : t_gs;
     const uint64_t dA = da + (uint64_t)((term_a(i) * CF::A_BYTES) >> 4);
     const uint64_t dB = db + (uint64_t)((term_b(i) * CF::B_BYTES) >> 4);
 #pragma unroll
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                  const __grid_constant__ CUtensorMap tmO, const Params p) {
   using CF = Cfg<BN, EPI>;
   constexpr int STAGES = CF::STAGES;
-  constexpr int NSLOT = 2;  // rotating group-0 slots
+  constexpr int NSLOT = 3;  // rotating group-0 slots
   constexpr int CPW = CF::COLS_PER_WARP;
   extern __shared__ uint8_t smem_raw[];
 
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint64_t* tfull = empty + STAGES;   // slot filled by the MMA warp
   uint64_t* tempty = tfull + NSLOT;   // slot drained by the drain warps
   uint64_t* gdone = tempty + NSLOT;   // a tile's products all complete (per tile)
-  uint64_t* gfree = gdone + 1;        // a tile's persistent groups read (per tile)
+  uint64_t* gfree = gdone + 1;        // a tile's persistent slot read (per tile)
   uint64_t* quiesce = gfree + 1;      // abort path: in-flight products done
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(quiesce + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t t_g1 = tmem, t_g2 = tmem + BN, t_rot = tmem + 2 * BN;
+  const uint32_t t_gs = tmem, t_rot = tmem + BN;
 
   if (warp == PRODUCER_WARP) {
     if (lane == 0) {
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint32_t round = (uint32_t)((g / NSLOT) & 1);
           if (g >= NSLOT) ok = mbar_wait(&tempty[ts], round ^ 1u);
           if (ok) ok = mbar_wait(&full[stage], phase);
-          // the previous tile's persistent groups must be read before this
+          // the previous tile's persistent slot must be read before this
           // tile's first products overwrite them
           if (ok && it == 0 && j > 0) ok = mbar_wait(gfree, (uint32_t)((j - 1) & 1));
           if (!ok || *abort_flag) {
@@ -450,20 +450,20 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint64_t da = smem_desc(a0), db = smem_desc(a0 + MAX_PARTS * CF::A_BYTES);
           // One thread issues every product of the block, so the issue loop
           // is fully unrolled over the fixed term order (descriptor offsets
-          // and accumulate flags are constants; only the first products of
-          // the persistent groups depend on it). Group 0 goes first and its
-          // slot is committed to the drain warps while the smaller groups
-          // are multiplied.
+          // and accumulate flags are constants; only the first smaller
+          // product depends on it). hi x hi goes first and its slot is
+          // committed to the drain warps while the smaller products are
+          // multiplied.
           const uint32_t d0 = t_rot + (uint32_t)(ts * BN);
-          issue_block<0, 1, CF>(da, db, d0, t_g1, t_g2, it == 0);
+          issue_block<0, 1, CF>(da, db, d0, t_gs, it == 0);
           umma_commit(&tfull[ts]);
           if (p.n_terms == 6)
-            issue_block<1, 6, CF>(da, db, d0, t_g1, t_g2, it == 0);
+            issue_block<1, 6, CF>(da, db, d0, t_gs, it == 0);
           else
-            issue_block<1, 3, CF>(da, db, d0, t_g1, t_g2, it == 0);
+            issue_block<1, 3, CF>(da, db, d0, t_gs, it == 0);
           umma_commit(&empty[stage]);
         }
-        if (ok) umma_commit(gdone);  // the tile's persistent groups are final
+        if (ok) umma_commit(gdone);  // the tile's persistent slot is final
       }
     }
     __syncwarp();
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) mbar_arrive(&tempty[ts]);
       }
       if (ok) {
-        // the tile's persistent groups are complete once its last commit lands
+        // the tile's persistent slot is complete once its last commit lands
         ok = mbar_wait(gdone, (uint32_t)(j & 1));
         ok = __all_sync(0xffffffffu, ok && !*abort_flag);
       }
@@ -504,14 +504,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       {
-        // add the persistent groups (smaller first: g2 into g1, then into
-        // the accumulator), then hand their slots to the next tile
+        // add the persistent slot of the smaller products, then hand it to
+        // the next tile
         tc_fence_after();
         float gsum[CPW];
 #pragma unroll
         for (int jj = 0; jj < CPW; ++jj) gsum[jj] = 0.f;
-        if (p.n_terms > 3) drain_add<CPW>(t_g2 + lane_off, gsum);  // bf16x3 has no group 2
-        drain_add<CPW>(t_g1 + lane_off, gsum);
+        drain_add<CPW>(t_gs + lane_off, gsum);
 #pragma unroll
         for (int jj = 0; jj < CPW; ++jj) acc[jj] += gsum[jj];
         tc_fence_before();
