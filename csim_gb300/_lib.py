@@ -48,6 +48,8 @@ SIGNATURES = {
     "csg_memcpy_h2d": ([P, P, P, SZ], None),
     "csg_memcpy_d2h": ([P, P, P, SZ], None),
     "csg_readout_d2h": ([P, P, P, SZ], None),
+    "csg_contrast_curve": ([P, P, I, D, D, D, P, I, P, P], None),
+    "csg_fd_jacobian": ([P, P, I, I, I, P, I, D, P], None),
     "csg_memset": ([P, P, I, SZ], None),
     "csg_version": ([], C.c_char_p),
     "csg_launch_count": ([], C.c_ulonglong),

@@ -323,3 +323,49 @@ class RegionContrast:
 
     def contrast(self, image: torch.Tensor, per_group: int, calib_max: float, mode: int = 0):
         return self.ctx.region_reduce(image, per_group, self.pix, mode=mode, scale=1.0 / calib_max)
+
+
+def linspace_reference(start: float, end: float, n: int) -> np.ndarray:
+    """arma::linspace: start + i (end - start) / (n - 1), the last value end."""
+    if n < 2:
+        return np.array([end], dtype=np.float64)[:n]
+    d = (end - start) / (n - 1)
+    out = start + np.arange(n, dtype=np.float64) * d
+    out[-1] = end
+    return out
+
+
+class ContrastCurve:
+    """contrastCurve (contrastCurve.cpp:68-158): the radial profile of the
+    image intensity (summed over the batch's fields) normalised by the
+    calibration maximum, averaged over overlapping annuli on the GPU. Sample
+    points linspace(0, max(pixelX / loD), (n - 2) / pixelSampling); the
+    reference writes bins 1 .. end as "%f %e" lines (`lines`)."""
+
+    def __init__(self, ctx: Context, n_out: int, out_pixel: float, loD: float,
+                 pixel_sampling: int = 1):
+        self.ctx, self.n, self.pixel, self.loD = ctx, n_out, out_pixel, loD
+        x_max = (-(out_pixel * n_out - out_pixel) / 2.0 + (n_out - 1) * out_pixel) / loD
+        k = int((n_out - 2) / pixel_sampling)
+        if k < 3:
+            raise ValueError("contrast curve: too few sample points")
+        self.samples = linspace_reference(0.0, x_max, k)
+        self._s = dvec(self.samples)
+        self._work = torch.empty(2 * (k - 2), dtype=torch.float64, device="cuda")
+        self._mean = torch.empty(k - 2, dtype=torch.float64, device="cuda")
+        self._inten = torch.empty((n_out, n_out), dtype=torch.float64, device="cuda")
+        self._max = torch.empty(1, dtype=torch.float64, device="cuda")
+
+    def compute(self, image: torch.Tensor, n_fields: int, calib_max: float):
+        """(positions, means) of bins 1 .. K-2 for the image fields [F][2][n][n]."""
+        call("csg_intensity", self.ctx.h, ptr(image), self.n, self.n, n_fields, ptr(self._inten),
+             ptr(self._max))
+        call("csg_contrast_curve", self.ctx.h, ptr(self._inten), self.n, self.pixel, self.loD,
+             1.0 / calib_max, ptr(self._s), self.samples.size, ptr(self._work), ptr(self._mean))
+        self.ctx.sync()
+        return self.samples[1:-1].copy(), self._mean.cpu().numpy()
+
+    @staticmethod
+    def lines(pos: np.ndarray, mean: np.ndarray) -> str:
+        """The reference's output file body (contrastCurve.cpp:148-151)."""
+        return "".join(f"{p:f} {m:e}\n" for p, m in zip(pos[1:], mean[1:]))

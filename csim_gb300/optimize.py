@@ -258,3 +258,24 @@ class DifferentialEvolution:
             self.close()
         except Exception:
             pass
+
+
+def fd_jacobian(cor, sags0: np.ndarray, dx: float, pix_idx: np.ndarray) -> torch.Tensor:
+    """linearOptimizer::compute_jacobian (linearOptimizer.cpp:420-495) with
+    the N + 1 propagations batched into one walk: candidate 0 carries sags0,
+    candidate i + 1 sags0 with variable i moved by dx. Returns the device
+    Jacobian [2 n_base n_pix][N] (FP64): column i = (E_{i+1} - E_0) / dx at the
+    region pixels, rows [Re; Im] per base field (sources x wavelengths)."""
+    sags0 = np.asarray(sags0, dtype=np.float64)
+    n_var = sags0.size
+    cand = np.repeat(sags0[None, :], n_var + 1, axis=0)
+    cand[np.arange(1, n_var + 1), np.arange(n_var)] += dx
+    cor.sags(n_var + 1).copy_(torch.as_tensor(cand))
+    cor.batch_all(n_var + 1)
+    img = cor.execute()
+    n_base = cor.n_fields // (n_var + 1)
+    pix = torch.as_tensor(np.ascontiguousarray(pix_idx, np.int32), device="cuda")
+    jac = torch.empty((2 * n_base * pix.numel(), n_var), dtype=torch.float64, device="cuda")
+    call("csg_fd_jacobian", cor.ctx.h, ptr(img), img.shape[-1], n_base, n_var, ptr(pix),
+         pix.numel(), float(dx), ptr(jac))
+    return jac

@@ -394,6 +394,27 @@ int csg_region_reduce(csg_ctx* ctx, const float* field, int rows, int cols, int 
 int csg_intensity(csg_ctx* ctx, const float* field, int rows, int cols, int n_fields,
                   double* out, double* out_max);
 
+/* contrastCurve::make_contrast_curve (contrastCurve.cpp:127-146): the mean
+ * of intensity[n][n] * scale (device FP64; scale = 1 / calibration max) over
+ * overlapping annuli s[i-1] < R < s[i+1], i = 1 .. n_samples - 2, where R is
+ * the distance of each pixel centre (-(pixel n - pixel) / 2 + k pixel) from
+ * the axis divided by lod, and samples (device, n_samples) are the
+ * reference's linspace(0, max(pixelX / loD), n_samples). out_mean (device,
+ * n_samples - 2): bin means (NaN for an empty bin). work: device scratch of
+ * 2 (n_samples - 2) doubles. */
+int csg_contrast_curve(csg_ctx* ctx, const double* intensity, int n, double pixel, double lod,
+                       double scale, const double* samples, int n_samples, double* work,
+                       double* out_mean);
+/* linearOptimizer::compute_jacobian (linearOptimizer.cpp:420-495) over one
+ * batched walk: image (device, fp32 planar [(n_var + 1) * n_base][2][n_out][n_out])
+ * holds candidate 0 (unperturbed) and candidates 1 .. n_var (variable i - 1
+ * moved by dx), each as n_base consecutive fields (sources x wavelengths).
+ * jac (device FP64, row-major [2 n_base n_pix][n_var]): column i is
+ * (E_{i+1} - E_0) / dx at the region pixels pix_idx (flat row-major indices),
+ * rows [Re; Im] per base field, base fields in order. */
+int csg_fd_jacobian(csg_ctx* ctx, const float* image, int n_out, int n_base, int n_var,
+                    const int* pix_idx, int n_pix, double dx, double* jac);
+
 /* ---------------------------------------- response-matrix objective */
 /* optHexRespObjective (optObjective.cpp:24-69): M cubes for every (s, p, l)
  * as complex<double> interleaved host row-major [n_mat][npix][ncol]
