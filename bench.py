@@ -194,7 +194,7 @@ def setup_piaacmc(args, ctx, W, cg, rank):
                  "n_hex": spec.n_hex, "image": cor.n_out,
                  "precision": f"bf16x{args.precision}", "fpm_support_crop": not args.no_crop,
                  "fpm_transformed_box": list(cor.fpm_region()),
-                 "l2": "working set > L2 (fields + MFT operands ~1.5 GB per step)"}
+                 "l2": f"working set > L2 (fields + MFT operands ~{0.024 * B:.1f} GB per step)"}
     return wl
 
 
@@ -340,7 +340,10 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--fields", type=int, default=64)
+    # 152 fields (candidates) per step: with 152 SMs every MFT GEMM launch is a
+    # whole number of persistent-CTA rounds (16, 2, 12, 72, 24 and 8 tiles per
+    # field) and every FFT grid a whole number of waves
+    ap.add_argument("--fields", type=int, default=152)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="piaacmc", choices=sorted(SETUP),
                     help="piaacmc (headline), plain_lyot, broadband, de")
@@ -500,7 +503,7 @@ def main():
         roofline = {"bound": "tensor", "kernel": "k_split_gemm (tcgen05 split-bf16 MFT)",
                     "achieved": gemm_tflops, "peak": tc_peak, "unit": "TFLOP/s",
                     "frac": gemm_tflops / tc_peak, "peak_kind": f"{peak_kind} bf16 sustained",
-                    "traffic": TRAFFIC.get(B) if args.workload == "piaacmc" else None,
+                    "traffic": TRAFFIC_PER_FIELD * B if args.workload == "piaacmc" else None,
                     "algorithmic_flops_per_launch": g["flops"] / g["count"],
                     "avg_launch_ms": g["ms"] / g["count"],
                     "executed_bf16_tflops": gemm_tflops * args.precision,
@@ -549,9 +552,10 @@ def main():
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per k_split_gemm launch,
-# averaged over the six GEMM launches of one step, keyed by fields per step:
-# an ncu capture at 32 fields (1153.1 MB per step) scaled by the field count.
-TRAFFIC: dict = {64: 384.4e6, 32: 192.2e6}
+# averaged over the six GEMM launches of one step, per field of the step: an
+# ncu capture at 32 fields (1149.1 MB per step), which scales with the field
+# count (the 64-field step moved 2 x its traffic).
+TRAFFIC_PER_FIELD = 1149.1e6 / 32 / 6
 
 if __name__ == "__main__":
     sys.exit(main())
