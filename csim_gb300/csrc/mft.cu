@@ -260,6 +260,7 @@ struct csg_mft {
   __nv_bfloat16* op2 = nullptr;  // [slot][3][3][mo][ny]
   Scratch split_in;               // [F][3][2][ny][nx] bf16
   Scratch tt;                     // [F][3][2][no][ny] bf16
+  int* valid = nullptr;           // ragged plans: outputs per slot (device)
   int bn = 0;                     // tile width chosen by the autotuner (0: default)
   int tuned_fields = 0;           // batch size the choice was measured at
   float tuned_ms[2] = {0, 0};     // measured time of BN = 128, 64
@@ -423,6 +424,17 @@ static int create_plan(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int
   CSG_LAUNCH_CHECK();
   CSG_CUDA(cudaStreamSynchronize(st));
   cudaFree(dvec);
+  if (n_out) {  // per-slot output extents, for skipping the all-zero tiles
+    if (cudaMalloc(&m->valid, sizeof(int) * n_slots) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(m->op1);
+      cudaFree(m->op2);
+      delete m;
+      set_error("csg_mft_create: allocation failed");
+      return CSG_E_NOMEM;
+    }
+    CSG_CUDA(cudaMemcpy(m->valid, n_out, sizeof(int) * n_slots, cudaMemcpyHostToDevice));
+  }
   *plan = m;
   return CSG_OK;
 }
@@ -457,6 +469,7 @@ int csg_mft_destroy(csg_mft* m) {
   cudaStreamSynchronize(m->ctx->stream);
   cudaFree(m->op1);
   cudaFree(m->op2);
+  cudaFree(m->valid);
   m->split_in.release();
   m->tt.release();
   delete m;
@@ -546,6 +559,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.out_cols = m->ny;
     p.accumulate = 0;
     p.status = ctx->status;
+    p.valid = m->valid;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     // algorithmic work: 8 flops per complex multiply-add of the contraction
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->ny * m->no * m->nx);
@@ -578,6 +592,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.out_c0 = outw.c0;
     p.accumulate = accumulate;
     p.status = ctx->status;
+    p.valid = m->valid;
     CUtensorMap to;
     p.tma_out = make_map_f32_out(&to, out + (size_t)outw.r0 * outw.pitch + outw.c0, m->no, m->mo,
                                  (long long)n_fields * 2, outw.pitch, outw.rows)

@@ -50,6 +50,10 @@ struct Params {
   // free operand ring and written by TMA stores, or by TMA add-reductions
   // when accumulating. 0: per-thread stores.
   int tma_out;
+  // ragged plans: slot s's outputs are zero beyond valid[s] rows and columns
+  // (its operator rows there are zero), so tiles starting beyond it are not
+  // computed (stage 2 writes their zeros); nullptr: every tile
+  const int* valid;
   int* status;
 };
 
@@ -300,6 +304,16 @@ __device__ __forceinline__ void issue_block(uint64_t da, uint64_t db, uint32_t d
 struct TileCoord {
   int field, d, row_a0, row_b0;
 };
+
+// Whether a tile of a ragged plan lies wholly beyond its slot's outputs:
+// stage 1 by its output columns (rows of T), stage 2 by its output rows or
+// columns.
+template <bool OP_IS_A>
+__device__ __forceinline__ bool tile_beyond(const Params& p, const TileCoord& tc) {
+  if (!p.valid) return false;
+  const int v = p.valid[p.slot[tc.field]];
+  return OP_IS_A ? (tc.row_a0 >= v || tc.row_b0 >= v) : tc.row_b0 >= v;
+}
 template <int BN, bool OP_IS_A>
 __device__ __forceinline__ TileCoord tile_coord(const Params& p, int t) {
   TileCoord c;
@@ -384,6 +398,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       long long g = 0;  // iterations over all of this CTA's tiles
       for (int t = blockIdx.x; t < n_tiles_total && !*abort_flag; t += gridDim.x) {
         const TileCoord tc = tile_coord<BN, OP_IS_A>(p, t);
+        if (tile_beyond<OP_IS_A>(p, tc)) continue;
         const int slot = p.slot[tc.field];
         for (int it = 0; it < k_iters; ++it, ++g) {
           const int stage = (int)(g % STAGES);
@@ -419,7 +434,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       long long g = 0;
       int j = 0;  // tiles done by this CTA
       bool ok = true;
-      for (int t = blockIdx.x; t < n_tiles_total && ok; t += gridDim.x, ++j) {
+      for (int t = blockIdx.x; t < n_tiles_total && ok; t += gridDim.x) {
+        if (tile_beyond<OP_IS_A>(p, tile_coord<BN, OP_IS_A>(p, t))) continue;
         for (int it = 0; it < k_iters; ++it, ++g) {
           const int stage = (int)(g % STAGES);
           const uint32_t phase = (uint32_t)((g / STAGES) & 1);
@@ -464,6 +480,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           umma_commit(&empty[stage]);
         }
         if (ok) umma_commit(gdone);  // the tile's persistent slot is final
+        ++j;
       }
     }
     __syncwarp();
@@ -476,13 +493,16 @@ __global__ void __launch_bounds__(THREADS, 1)
     long long g = 0;
     int j = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < n_tiles_total && ok; t += gridDim.x, ++j) {
+    for (int t = blockIdx.x; t < n_tiles_total && ok; t += gridDim.x) {
       const TileCoord tc = tile_coord<BN, OP_IS_A>(p, t);
       const int field = tc.field, d = tc.d, row_a0 = tc.row_a0, row_b0 = tc.row_b0;
       float acc[CPW];
 #pragma unroll
       for (int jj = 0; jj < CPW; ++jj) acc[jj] = 0.f;
-      for (int it = 0; it < k_iters; ++it, ++g) {
+      // a ragged tile beyond its slot: nothing computed; stage 2 stores zeros
+      const bool beyond = tile_beyond<OP_IS_A>(p, tc);
+      if (beyond && EPI == EPI_T_SPLIT) continue;
+      for (int it = 0; it < (beyond ? 0 : k_iters); ++it, ++g) {
         const int ts = (int)(g % NSLOT);
         const uint32_t round = (uint32_t)((g / NSLOT) & 1);
         ok = mbar_wait(&tfull[ts], round);
@@ -494,7 +514,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&tempty[ts]);
       }
-      if (ok) {
+      if (ok && !beyond) {
         // the tile's persistent slot is complete once its last commit lands
         ok = mbar_wait(gdone, (uint32_t)(j & 1));
         ok = __all_sync(0xffffffffu, ok && !*abort_flag);
@@ -503,7 +523,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         atomicExch(p.status, 3);
         break;
       }
-      {
+      if (!beyond) {
         // add the persistent slot of the smaller products, then hand it to
         // the next tile
         tc_fence_after();
@@ -516,6 +536,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(gfree);
+        ++j;
       }
       if (EPI == EPI_T_SPLIT) {
         // C[y][u] -> T^T parts [field][part][d][u][y] (bf16)
