@@ -27,12 +27,16 @@ def test_dm_surface_matches_oracle(ctx, n, n_act, sigma):
     assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max()
 
 
-def test_ragged_mft_matches_oracle(ctx):
+@pytest.mark.parametrize("sizes", [[40, 56, 48], [100, 300, 140]])
+def test_ragged_mft_matches_oracle(ctx, sizes):
+    """One launch for every wavelength's grid; with grids spanning several
+    128-wide tiles the tiles wholly beyond a wavelength's grid are skipped and
+    must still come out zero (the output buffer starts as NaN)."""
     from csim_gb300 import _lib
     from csim_gb300.runtime import dvec, from_planar, to_planar
     import ctypes as C
     rng = np.random.default_rng(5)
-    n_in, sizes = 96, [40, 56, 48]
+    n_in = 96
     n_max = max(sizes)
     L = len(sizes)
     gin = of.ArrayGeom.set_xy(n_in, n_in, 1e-5)
@@ -56,7 +60,7 @@ def test_ragged_mft_matches_oracle(ctx):
         slots = np.array([0, 1, 2, 2, 1, 0], np.int32)
         e = rng.standard_normal((F, n_in, n_in)) + 1j * rng.standard_normal((F, n_in, n_in))
         inp = to_planar(e)
-        out = torch.empty((F, 2, n_max, n_max), dtype=torch.float32, device="cuda")
+        out = torch.full((F, 2, n_max, n_max), float("nan"), dtype=torch.float32, device="cuda")
         sl = dvec(slots, torch.int32)
         _lib.call("csg_mft_execute", ctx.h, h, C.c_void_p(inp.data_ptr()),
                   C.c_void_p(out.data_ptr()), F, C.c_void_p(sl.data_ptr()), 0, None, None)
