@@ -209,6 +209,7 @@ class ScriptChain:
 class _Builder:
     def __init__(self, ctx, base_dir: str, precision: int):
         self.ctx, self.base, self.precision = ctx, base_dir, precision
+        self.sags = None  # the hex FPM's sags, once its block is read
 
     def path(self, v: str) -> str:
         p = v.strip()
@@ -362,7 +363,6 @@ def load(path: str, ctx, base_dir: str | None = None, precision: int = 6) -> Scr
     with open(path) as fh:
         blocks = parse(fh.read())
     b = _Builder(ctx, base_dir or os.path.dirname(os.path.abspath(path)), precision)
-    b.sags = None
     by_kind, tools = {}, []
     for blk in blocks:
         if blk.kind in ("regionContrast", "makeContrastCurve"):
