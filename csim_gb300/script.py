@@ -296,6 +296,9 @@ class _Builder:
     def fpm(self, blk: Block, ef: EField, dis: bool):
         from .workloads import hex_tables
         _check_keys(blk, _COMMON | {"focalRatio", "fRatioSign", "zoomFftSign"})
+        if self.sags is not None:
+            raise ScriptError("fpmPupToLyot: one hex FPM per chain (its sags are the "
+                              "optimisation vector)")
         if len(blk.blocks) != 1 or blk.blocks[0].kind != "fpmIntHexCMCForPupToLyot":
             raise ScriptError("fpmPupToLyot: only an fpmIntHexCMCForPupToLyot mask is supported")
         ad = blk.blocks[0]
