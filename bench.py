@@ -188,6 +188,11 @@ def setup_piaacmc(args, ctx, W, cg, rank):
     # every step the candidates' sags come from the host
     wl.host_in, wl.dev_in = torch.as_tensor(sags_h), sags_d
     wl.cpu = lambda budget, nmax: cpu_fields_per_s(spec, inp, sags_h, budget, nmax)
+
+    def fp64(budget, nmax):  # the plain FP64 GPU path on the same inputs
+        from baseline.fp64_gpu import Fp64Piaacmc, throughput
+        return throughput(Fp64Piaacmc(inp, spec), sags_h[:8], budget, nmax)
+    wl.fp64 = fp64
     wl.cpu_sample = ("FP64, reference algorithm: chirp-Z mask hat + 2048^2 FFT convolution")
     wl.bound = "tensor"
     wl.config = {"workload": WORKLOAD, "fields_per_step": B, "n": spec.n, "fpm_grid": spec.S,
@@ -531,6 +536,14 @@ def main():
         cpu = {"value": v, "unit": "fields/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{n} fields of the same workload in {dt:.1f} s ({wl.cpu_sample})"}
 
+    # the comparator: the plain FP64 GPU path (complex128, one field per call,
+    # cuFFT + cuBLAS ZGEMM), a bounded sample on the same inputs
+    fp64 = None
+    if rank == 0 and ws == 1 and not args.no_cpu and getattr(wl, "fp64", None) is not None:
+        v, n, dt = wl.fp64(10.0, 400)
+        fp64 = {"value": v, "unit": "fields/s", "sample": f"{n} fields in {dt:.1f} s",
+                "speedup": value / v, "e2e_speedup": e2e_value / v}
+
     wl.config["parallelism"] = f"fields sharded over {ws} rank(s)"
     line = {"metric": "field propagations/s", "value": value, "unit": "fields/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -542,6 +555,8 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches_per_step * args.steps,
             "roofline": roofline, "clocks": clk, "cpu_baseline": cpu}
+    if fp64 is not None:
+        line["fp64_gpu_path"] = fp64
     if wl.reg is not None:
         line["contrast_sample"] = float(contrast[0].item())
     if rank == 0:
