@@ -103,6 +103,7 @@ SIGNATURES = {
     "csg_chain_image": ([P, C.POINTER(P), C.POINTER(I)], None),
     "csg_chain_field": ([P, C.POINTER(P)], None),
     "csg_mft_reserve": ([P, I], None),
+    "csg_mft_set_tile": ([P, I], None),
     "csg_mft_tuning": ([P, C.POINTER(I), C.POINTER(C.c_float), C.POINTER(C.c_float)], None),
     "csg_mft_tuning_log": ([C.c_char_p, SZ], None),
     "csg_region_reduce": ([P, P, I, I, I, I, P, I, I, D, P], None),

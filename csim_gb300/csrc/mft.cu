@@ -42,24 +42,32 @@ static int get_encoder() {
   return rc;
 }
 
-// 3-D bf16 map: (k inner, rows, planes), box (64, box_rows, 1), 128B swizzle.
-int make_map(CUtensorMap* m, const void* base, int k, int rows, long long planes,
-             int box_rows) {
+// 3-D bf16 map: (k inner, rows, planes), box (box_k, box_rows, 1), with the
+// swizzle of a box_k-wide row: 128 bytes (64 elements) or 64 bytes (32).
+int make_map_k(CUtensorMap* m, const void* base, int k, int rows, long long planes,
+               int box_rows, int box_k) {
   int rc = get_encoder();
   if (rc) return rc;
   CSG_CHECK(((uintptr_t)base & 15) == 0, CSG_E_ARG, "TMA base not 16-byte aligned");
   CSG_CHECK((k % 8) == 0, CSG_E_SHAPE, "TMA inner extent must be a multiple of 8 elements");
+  CSG_CHECK(box_k == 64 || box_k == 32, CSG_E_ARG, "TMA box K must be 64 or 32");
   cuuint64_t dims[3] = {(cuuint64_t)k, (cuuint64_t)rows, (cuuint64_t)planes};
   cuuint64_t strides[2] = {(cuuint64_t)k * 2, (cuuint64_t)k * 2 * rows};
-  cuuint32_t box[3] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t box[3] = {(cuuint32_t)box_k, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                        box_k == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   CSG_CHECK(r == CUDA_SUCCESS, CSG_E_CUDA,
             "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return CSG_OK;
+}
+
+// The same with 64-wide K boxes (128B swizzle).
+int make_map(CUtensorMap* m, const void* base, int k, int rows, long long planes,
+             int box_rows) {
+  return make_map_k(m, base, k, rows, planes, box_rows, tc::BK);
 }
 
 // 3-D fp32 map of an output window for the GEMM epilogue: (cols, rows,
@@ -262,8 +270,8 @@ struct csg_mft {
   Scratch tt;                     // [F][3][2][no][ny] bf16
   int* valid = nullptr;           // ragged plans: outputs per slot (device)
   int bn = 0;                     // tile width chosen by the autotuner (0: default)
-  int tuned_fields = 0;           // batch size the choice was measured at
-  float tuned_ms[2] = {0, 0};     // measured time of BN = 128, 64
+  int tuned_fields = 0;           // batch size the choice was measured at (-1: fixed)
+  float tuned_ms[3] = {0, 0, 0};  // measured time of BN = 128, 64, 256 (0: not tried)
 };
 
 namespace {
@@ -273,7 +281,7 @@ std::string g_tune_log;
 // batch size it will run at (zero input, every field on slot 0) and keeps the
 // faster. Runs outside graph capture (csg_mft_reserve is called before).
 int autotune(csg_mft* m, int F) {
-  if (m->tuned_fields == F) return CSG_OK;
+  if (m->tuned_fields == F || m->tuned_fields == -1) return CSG_OK;
   const char* env = getenv("CSG_MFT_AUTOTUNE");
   if (env && env[0] == '0') {
     m->bn = 0;
@@ -300,12 +308,14 @@ int autotune(csg_mft* m, int F) {
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  const int cand[2] = {128, 64};
+  const int cand[3] = {128, 64, 256};
   float best = 1e30f;
   int best_bn = 0, rc = CSG_OK;
   const bool prof = m->ctx->prof;
   m->ctx->prof = false;
-  const int n_cand = 2;
+  // 256-wide tiles only where the output is at least that wide per component
+  const int n_cand = m->no >= 256 ? 3 : 2;
+  m->tuned_ms[2] = 0;
   for (int i = 0; i < n_cand && !rc; ++i) {
     m->bn = cand[i];
     rc = mft_execute_ops(m->ctx, m, in, out, F, slot, 0, nullptr, nullptr, PixOps(), FieldInfo());
@@ -333,9 +343,9 @@ int autotune(csg_mft* m, int F) {
   m->tuned_fields = F;
   char line[200];
   snprintf(line, sizeof(line), "%s{\"in\": [%d, %d], \"out\": [%d, %d], \"fields\": %d, "
-           "\"bn\": %d, \"ms_bn128\": %.4f, \"ms_bn64\": %.4f}",
+           "\"bn\": %d, \"ms_bn128\": %.4f, \"ms_bn64\": %.4f, \"ms_bn256\": %.4f}",
            g_tune_log.empty() ? "" : ", ", m->ny, m->nx, m->mo, m->no, F, best_bn,
-           m->tuned_ms[0], m->tuned_ms[1]);
+           m->tuned_ms[0], m->tuned_ms[1], m->tuned_ms[2]);
   g_tune_log += line;
   return rc;
 }
@@ -485,6 +495,17 @@ int csg_mft_reserve(csg_mft* m, int n_fields) {
   return rc;
 }
 
+int csg_mft_set_tile(csg_mft* m, int bn) {
+  CSG_CHECK(m, CSG_E_ARG, "csg_mft_set_tile: null plan");
+  CSG_CHECK(bn == 0 || bn == 64 || bn == 128 || bn == 256, CSG_E_ARG,
+            "csg_mft_set_tile: width must be 0, 64, 128 or 256");
+  CSG_CHECK(bn != 256 || m->no >= 256, CSG_E_ARG,
+            "csg_mft_set_tile: 256-wide tiles need at least 256 output columns");
+  m->bn = bn;
+  m->tuned_fields = bn ? -1 : 0;  // -1: fixed by the caller, never retuned
+  return CSG_OK;
+}
+
 // Tile width the autotuner chose for the last reserved batch size and the
 // times it measured (ms per transform for widths 128 and 256).
 int csg_mft_tuning(csg_mft* m, int* bn, float* ms128, float* ms64) {
@@ -538,11 +559,13 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
   }
 
   const int bn1 = m->bn ? m->bn : 128;
+  const int kb = bn1 == 256 ? 32 : tc::BK;  // K block of the tile width
   // ---- stage 1: T^T = split(in . B_x^T)^T
   {
     CUtensorMap ta, tb;
-    if ((rc = make_map(&ta, sin, m->nx, m->ny, (long long)n_fields * 6, tc::BM))) return rc;
-    if ((rc = make_map(&tb, m->op1, m->nx, m->no, (long long)m->n_slots * 9, bn1))) return rc;
+    if ((rc = make_map_k(&ta, sin, m->nx, m->ny, (long long)n_fields * 6, tc::BM, kb))) return rc;
+    if ((rc = make_map_k(&tb, m->op1, m->nx, m->no, (long long)m->n_slots * 9, bn1, kb)))
+      return rc;
     tc::Params p{};
     p.n_fields = n_fields;
     p.m_tiles = (m->ny + tc::BM - 1) / tc::BM;
@@ -551,7 +574,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.m_half = p.m_tiles;
     p.rows_valid = m->ny;
     p.cols_valid = m->no;
-    p.k_blocks = (m->nx + tc::BK - 1) / tc::BK;
+    p.k_blocks = (m->nx + kb - 1) / kb;
     terms_for(m->precision, p);
     p.slot = slot;
     p.out = tt;
@@ -563,15 +586,17 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     // algorithmic work: 8 flops per complex multiply-add of the contraction
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->ny * m->no * m->nx);
-    rc = bn1 == 64 ? launch_gemm<64, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
-                   : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
+    rc = bn1 == 64    ? launch_gemm<64, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
+         : bn1 == 256 ? launch_gemm<256, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
+                      : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
     if (rc) return rc;
   }
   // ---- stage 2: out = (pref A_y) . T
   {
     CUtensorMap ta, tb;
-    if ((rc = make_map(&ta, m->op2, m->ny, m->mo, (long long)m->n_slots * 9, tc::BM))) return rc;
-    if ((rc = make_map(&tb, tt, m->ny, m->no, (long long)n_fields * 6, bn1))) return rc;
+    if ((rc = make_map_k(&ta, m->op2, m->ny, m->mo, (long long)m->n_slots * 9, tc::BM, kb)))
+      return rc;
+    if ((rc = make_map_k(&tb, tt, m->ny, m->no, (long long)n_fields * 6, bn1, kb))) return rc;
     tc::Params p{};
     p.n_fields = n_fields;
     p.m_half = (m->mo + tc::BM - 1) / tc::BM;
@@ -580,7 +605,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.n_half = p.n_tiles;
     p.rows_valid = m->mo;
     p.cols_valid = m->no;
-    p.k_blocks = (m->ny + tc::BK - 1) / tc::BK;
+    p.k_blocks = (m->ny + kb - 1) / kb;
     terms_for(m->precision, p);
     p.slot = slot;
     p.out = out;
@@ -600,8 +625,9 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
                     : 0;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->mo * m->no * m->ny);
-    rc = bn1 == 64 ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st, &to)
-                   : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st, &to);
+    rc = bn1 == 64    ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st, &to)
+         : bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st, &to)
+                      : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st, &to);
     if (rc) return rc;
   }
   return CSG_OK;

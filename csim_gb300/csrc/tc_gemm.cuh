@@ -34,7 +34,7 @@ struct Params {
   int n_half;       // stage 1: tiles per component along N
   int rows_valid;   // stage 1: Ny (data rows); stage 2: Mo (operator rows per comp)
   int cols_valid;   // No (valid output columns)
-  int k_blocks;     // ceil(K / BK)
+  int k_blocks;     // ceil(K / K block): 64 elements, 32 for N = 256 tiles
   int n_terms;      // products of the split issued (6: bf16x6, 3: bf16x3; see term_a)
   const int* slot;  // [n_fields] operator slot of each field
   void* out;
@@ -152,6 +152,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
   return d;
 }
 
+// K-major, 64-byte swizzle: 8-row atoms of 512 bytes (32-wide K blocks).
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(512 >> 4) << 32;        // stride byte offset: next 8-row atom
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;                 // SWIZZLE_64B
+  return d;
+}
+
 // kind::f16 instruction descriptor: bf16 x bf16 -> f32, both K-major.
 __host__ __device__ constexpr uint32_t instr_desc(int m, int n) {
   return (1u << 4)                 // D format f32
@@ -228,16 +239,26 @@ constexpr int MAX_PARTS = 3;
 // on across tiles, so the producer loads the next tile while the current
 // one finishes and its epilogue runs. The fp32 epilogue stages its boxes in
 // a region of its own (4 KB per drain warp), apart from the ring.
+//
+// N = 256 tiles issue 256-wide products (which keep the tensor pipe busier
+// than 128-wide ones for the same shared-memory operand traffic per FLOP).
+// Their three-part stages use 32-wide K blocks (64-byte swizzle) to leave
+// room for two or three stages, and tensor memory holds one 256-column
+// rotating hi x hi slot beside the small products' slot: hi x hi is
+// committed first, so its drain overlaps the rest of the block.
 template <int BN, int EPI>
 struct Cfg {
-  static_assert(BN == 64 || BN == 128, "N tile must be 64 or 128");
-  static constexpr uint32_t A_BYTES = BM * BK * 2;
-  static constexpr uint32_t B_BYTES = BN * BK * 2;
+  static_assert(BN == 64 || BN == 128 || BN == 256, "N tile must be 64, 128 or 256");
+  static constexpr int KB = BN == 256 ? 32 : BK;  // K elements per pipeline stage
+  static constexpr uint32_t A_BYTES = BM * KB * 2;
+  static constexpr uint32_t B_BYTES = BN * KB * 2;
   static constexpr uint32_t STAGE_BYTES = MAX_PARTS * (A_BYTES + B_BYTES);
   static constexpr uint32_t STAGING_BYTES = EPI == 1 ? DRAIN_WARPS * 4096 : 0;
   // 192 KB (+ 32 KB staging) at N = 128; 216 KB or 144 KB (+ 32 KB) at 64
+  // and at 256
   static constexpr int STAGES = BN == 128 ? 2 : (EPI == 1 ? 2 : 3);
-  static constexpr int TMEM_COLS = 4 * BN;          // small groups, three rotating slots
+  static constexpr int NSLOT = BN == 256 ? 1 : 3;  // rotating hi x hi slots
+  static constexpr int TMEM_COLS = BN * (1 + NSLOT);  // small products + rotating
   static constexpr int COLS_PER_WARP = BN / 2;      // two warps share a lane quadrant
   static constexpr int BN_ = BN;
   static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + STAGING_BYTES + 1024 + 512;
@@ -292,7 +313,7 @@ __device__ __forceinline__ void issue_block(uint64_t da, uint64_t db, uint32_t d
     const uint64_t dA = da + (uint64_t)((term_a(i) * CF::A_BYTES) >> 4);
     const uint64_t dB = db + (uint64_t)((term_b(i) * CF::B_BYTES) >> 4);
 #pragma unroll
-    for (int k = 0; k < BK / 16; ++k) {
+    for (int k = 0; k < CF::KB / 16; ++k) {
       const bool fresh = k == 0 && (g == 0 || (first_of_group(i) && first_block));
       umma(dcol, dA + 2 * k, dB + 2 * k, idesc, fresh ? 0u : 1u);
     }
@@ -343,7 +364,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                  const __grid_constant__ CUtensorMap tmO, const Params p) {
   using CF = Cfg<BN, EPI>;
   constexpr int STAGES = CF::STAGES;
-  constexpr int NSLOT = 3;  // rotating group-0 slots
+  constexpr int NSLOT = CF::NSLOT;  // rotating group-0 slots
   constexpr int CPW = CF::COLS_PER_WARP;
   extern __shared__ uint8_t smem_raw[];
 
@@ -422,8 +443,8 @@ __global__ void __launch_bounds__(THREADS, 1)
               za = (slot * 3 + pp) * 3 + sel_plane(tc.d, c);
               zb = (tc.field * 3 + pp) * 2 + c;
             }
-            tma_load_3d(sA + pp * CF::A_BYTES, &tmA, &full[stage], kb * BK, tc.row_a0, za);
-            tma_load_3d(sB + pp * CF::B_BYTES, &tmB, &full[stage], kb * BK, tc.row_b0, zb);
+            tma_load_3d(sA + pp * CF::A_BYTES, &tmA, &full[stage], kb * CF::KB, tc.row_a0, za);
+            tma_load_3d(sB + pp * CF::B_BYTES, &tmB, &full[stage], kb * CF::KB, tc.row_b0, zb);
           }
         }
       }
@@ -463,7 +484,9 @@ __global__ void __launch_bounds__(THREADS, 1)
           // (address >> 4), so offsets are added to it directly (shared
           // addresses stay below 2^18: no carry out of the 14-bit field)
           const uint32_t a0 = smem_u32(sbase + stage * CF::STAGE_BYTES);
-          const uint64_t da = smem_desc(a0), db = smem_desc(a0 + MAX_PARTS * CF::A_BYTES);
+          const uint32_t b0 = a0 + MAX_PARTS * CF::A_BYTES;
+          const uint64_t da = CF::KB == 64 ? smem_desc(a0) : smem_desc_sw64(a0);
+          const uint64_t db = CF::KB == 64 ? smem_desc(b0) : smem_desc_sw64(b0);
           // One thread issues every product of the block, so the issue loop
           // is fully unrolled over the fixed term order (descriptor offsets
           // and accumulate flags are constants; only the first smaller
@@ -527,12 +550,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         // add the persistent slot of the smaller products, then hand it to
         // the next tile
         tc_fence_after();
-        float gsum[CPW];
-#pragma unroll
-        for (int jj = 0; jj < CPW; ++jj) gsum[jj] = 0.f;
-        drain_add<CPW>(t_gs + lane_off, gsum);
-#pragma unroll
-        for (int jj = 0; jj < CPW; ++jj) acc[jj] += gsum[jj];
+        drain_add<CPW>(t_gs + lane_off, acc);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(gfree);

@@ -150,6 +150,10 @@ class Mft:
              int(precision))
         self.h = h
 
+    def set_tile(self, bn: int):
+        """Fix the tensor-core tile width (64, 128 or 256; 0: default / autotuned)."""
+        call("csg_mft_set_tile", self.h, int(bn))
+
     def __call__(self, field_in, slot, out=None, accumulate=False, in_mul=None, mul_idx=None):
         F = field_in.shape[0]
         if out is None:

@@ -329,9 +329,14 @@ int csg_chain_image(csg_chain* chain, float** dev_image, int* n_out);
 int csg_chain_field(csg_chain* chain, float** dev_field);
 /* Pre-size an MFT plan's scratch for n_fields (so graph capture allocates
  * nothing) and autotune its tensor-core tile width (128 or 64 output
- * columns per tile) by timing both at that batch size. Set the environment
- * variable CSG_MFT_AUTOTUNE=0 to keep the default width (128). */
+ * columns per tile, and 256 where the output is at least 256 wide) by
+ * timing each at that batch size. Set the environment variable
+ * CSG_MFT_AUTOTUNE=0 to keep the default width (128). */
 int csg_mft_reserve(csg_mft* plan, int n_fields);
+/* Fix the plan's tile width (64, 128 or 256 output columns per tile, 256
+ * only for outputs at least 256 wide; 0 returns to the default and lets
+ * csg_mft_reserve autotune it again). */
+int csg_mft_set_tile(csg_mft* plan, int bn);
 /* The chosen tile width and the measured ms per transform of each width. */
 int csg_mft_tuning(csg_mft* plan, int* bn, float* ms128, float* ms64);
 /* Every autotuning decision of the process as a JSON list. */

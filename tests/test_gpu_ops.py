@@ -307,3 +307,37 @@ def test_pipelined_readout(ctx):
         ctx.bind_stream(torch.cuda.current_stream())
     for i, h in enumerate(hosts):
         assert bool((h == float(i + 1)).all())
+
+
+@pytest.mark.parametrize("bn", [64, 128, 256])
+def test_mft_tile_widths(ctx, bn):
+    """Every tensor-core tile width (64 and 128 with 64-wide K blocks, 256
+    with 32-wide K blocks and 256-wide products) gives the same fp32-class
+    transform, for a plain and an accumulating launch."""
+    R = rt()
+    rng = np.random.default_rng(14)
+    n_in, n_out = 256, 320
+    gin = of.ArrayGeom.set_xy(n_in, n_in, 1e-5)
+    gout = of.ArrayGeom.set_xy(n_out, n_out, 2.1e-6)
+    lf = np.array([6.5e-7 * 40.0, 6.9e-7 * 40.0])
+    pref = gin.pixelSizeX * gin.pixelSizeY / (1j * lf)
+    e = rand_field(rng, 3, n_in, n_in)
+    slots = np.array([0, 1, 1], dtype=np.int32)
+    plan = R.Mft(ctx, gin.pixelY, gin.pixelX, gout.pixelY, gout.pixelX, lf, pref, -1.0)
+    plan.set_tile(bn)
+    refs = [of.mft(e[f], gin.pixelX, gin.pixelY, gout.pixelX, gout.pixelY, lf[slots[f]],
+                   pref[slots[f]]) for f in range(3)]
+    got = R.from_planar(plan(R.to_planar(e), R.dvec(slots, torch.int32)))
+    # accumulating onto a base of the result's own magnitude (fp32 sums of
+    # very different magnitudes would hide the transform's error)
+    scale = float(np.sqrt(np.mean(np.abs(refs[0]) ** 2)))
+    base = scale * rand_field(rng, 3, n_out, n_out)
+    out = R.to_planar(base)
+    plan(R.to_planar(e), R.dvec(slots, torch.int32), out=out, accumulate=True)
+    ctx.sync()
+    acc = R.from_planar(out)
+    for f in range(3):
+        assert rms_err(got[f], refs[f]) < RMS_TOL
+        assert peak_err(got[f], refs[f]) < RANDOM_PEAK_TOL
+        assert rms_err(acc[f], base[f] + refs[f]) < 2 * RMS_TOL
+    plan.close()
