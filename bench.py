@@ -376,6 +376,7 @@ def main():
     from csim_gb300 import coronagraph as cg
     from csim_gb300 import workloads as W
     from csim_gb300.runtime import Context
+    from csim_gb300.sharding import max_over_ranks
 
     ctx = Context(local)
     stream = torch.cuda.Stream(local)
@@ -436,11 +437,7 @@ def main():
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), "cuda")
     ctx.sync()
     value = B * args.steps * ws / (ms / 1e3)
 
@@ -479,10 +476,7 @@ def main():
             e2e_step()
         ctx.sync()
         e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, "cuda")
     e2e_value = B * args.steps * ws / e2e_s
 
     # ---- dominant kernel, timed live with CUDA events on its stream
