@@ -37,10 +37,13 @@ def _mft_ops(xin, xout, lf: float, sign: float, dev) -> torch.Tensor:
 
 
 class Fp64Piaacmc:
-    """The PIAACMC chain of the bench on complex128, one field per call."""
+    """The PIAACMC chain of the bench on complex128, one field per call.
+    dtype=torch.complex64 gives the same plain path in single precision
+    (every table, field and product complex64): the precision comparator."""
 
-    def __init__(self, inp: dict, spec, device: str = "cuda"):
+    def __init__(self, inp: dict, spec, device: str = "cuda", dtype=torch.complex128):
         self.dev = torch.device(device)
+        self.dtype = dtype
         ef, tel = inp["ef"], inp["tel"]
         n, dx = ef.n, inp["dx"]
         self.n = n
@@ -84,17 +87,25 @@ class Fp64Piaacmc:
             self.n_sub * self.n_sub)
         return torch.flip(m, dims=[1]) - 1.0
 
-    def field(self, li: int, amp: float, sags: torch.Tensor) -> torch.Tensor:
+    def field(self, li: int, amp: float, sags: torch.Tensor,
+              calibrating: bool = False) -> torch.Tensor:
         """Final image field of an on-axis source of amplitude amp at
-        wavelength index li with the candidate's sags (complex128)."""
+        wavelength index li with the candidate's sags (calibrating: without
+        the focal-plane mask)."""
         p = self.per_lam[li]
-        e = amp * p["pre"]
-        e = torch.fft.ifft2(torch.fft.fft2(e) * p["H"])
-        e = e * p["m2"]
-        f = p["A1"] @ e @ p["A1"].T  # square grids: the same operator on both axes
-        g = p["c"] * (p["A2"] @ (self.mask(sags, p["lam"]) * f) @ p["A2"].T)
-        e = (e + g) * self.lyot
-        return p["pref3"] * (p["A3"] @ e @ p["A3"].T)
+        d = self.dtype
+        c = (lambda t: t.to(d)) if d != torch.complex128 else (lambda t: t)
+        e = amp * c(p["pre"])
+        e = torch.fft.ifft2(torch.fft.fft2(e) * c(p["H"]))
+        e = e * c(p["m2"])
+        if not calibrating:
+            A1, A2 = c(p["A1"]), c(p["A2"])
+            f = A1 @ e @ A1.T  # square grids: the same operator on both axes
+            g = complex(p["c"]) * (A2 @ (c(self.mask(sags, p["lam"])) * f) @ A2.T)
+            e = e + g
+        e = e * c(self.lyot)
+        A3 = c(p["A3"])
+        return complex(p["pref3"]) * (A3 @ e @ A3.T)
 
 
 def throughput(model: Fp64Piaacmc, sags: np.ndarray, budget_s: float, n_max: int):

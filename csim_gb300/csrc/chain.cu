@@ -6,6 +6,7 @@
 // replayed (csg_chain_capture / csg_chain_replay).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <memory>
 #include <string>
 #include <vector>
@@ -824,6 +825,10 @@ struct Step {
   PixOps pro, epi;
   const Elem* e = nullptr;
   int sup0 = 0, sup1 = 1 << 30;  // FRESNEL: rows that can be nonzero on input
+  // FRESNEL followed by a hex FPM: the last row pass also writes the FPM's
+  // forward-transform operand split (split_to), and the FPM skips its split
+  csg_mft* split_to = nullptr;
+  bool presplit = false;
 };
 
 static bool push_op(PixOps& o, int kind, const float* a, const float* b, float param, int mr,
@@ -911,6 +916,18 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
     sup1 = c->n;
   }
   if (pend.n) prog.push_back(Step{Step::PIX, pend, PixOps(), nullptr});
+  // a Fresnel straight before a hex FPM hands over its result already split
+  const char* env = getenv("CSG_FRESNEL_SPLIT");
+  if (!(env && env[0] == '0'))
+    for (size_t i = 0; i + 1 < prog.size(); ++i)
+      if (prog[i].kind == Step::FRESNEL && prog[i + 1].kind == Step::FPM) {
+        int ny = 0, nx = 0;
+        mft_input_shape(prog[i + 1].e->mft1, &ny, &nx);
+        if (ny == c->n && nx == c->n) {
+          prog[i].split_to = prog[i + 1].e->mft1;
+          prog[i + 1].presplit = true;
+        }
+      }
   return prog;
 }
 
@@ -927,10 +944,16 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
       case Step::FRESNEL: {
         FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad, s.e->tab, c->slot};
         FftBand sup;  // rows a mask left nonzero, widened to the transform's row groups
+        __nv_bfloat16* split = nullptr;
+        if (s.split_to) {
+          split = mft_split_buffer(s.split_to, F);
+          CSG_CHECK(split, CSG_E_NOMEM, "Fresnel: FPM operand buffer allocation failed");
+        }
         if (fft_row_support(n, s.sup0, std::min(s.sup1, n), &sup.lo, &sup.n) && sup.n < n)
-          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, &sup);
+          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, &sup, split);
         else
-          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi);
+          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, nullptr,
+                           split);
         break;
       }
       case Step::FPM: {
@@ -941,8 +964,9 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         rc = hex_mask_region(ctx, e.hex_id, e.count, e.S, e.r0, e.c0, e.RR, e.CC, e.n_sub,
                              c->sags, e.n_hex, F, c->cand, c->lam_f, e.phase_sign, 1, 1.0,
                              c->fpm_mask, c->phasors);
-        if (!rc) rc = csg_mft_execute(ctx, e.mft1, c->field, c->fpm, F, c->slot, 0, nullptr,
-                                      nullptr);
+        if (!rc)
+          rc = mft_execute_ops(ctx, e.mft1, c->field, c->fpm, F, c->slot, 0, nullptr, nullptr,
+                               PixOps(), fi, nullptr, nullptr, nullptr, s.presplit);
         // E + MFT2[...] on the window of the stops that follow (accumulate)
         if (!rc) rc = mft_execute_ops(ctx, e.mft2, c->fpm, c->field, F, c->slot, 1, c->fpm_mask,
                                       c->ident, PixOps(), fi, nullptr, &e.win);
@@ -1165,7 +1189,8 @@ int csg_chain_response(csg_chain* c, int fpm_index, const int* pix_idx, int n_pi
   FieldInfo fi{c->lam_f, c->amp, c->tip, c->tilt, c->slot};
   for (int i = 0; i < fi_step && !rc; ++i) rc = run_step(c, prog[i], fi, B);
   if (rc) return rc;
-  rc = csg_mft_execute(ctx, e.mft1, c->field, c->fpm, B, c->slot, 0, nullptr, nullptr);
+  rc = mft_execute_ops(ctx, e.mft1, c->field, c->fpm, B, c->slot, 0, nullptr, nullptr, PixOps(),
+                       fi, nullptr, nullptr, nullptr, prog[fi_step].presplit);
   if (rc) return rc;
 
   // chunks of columns x base fields

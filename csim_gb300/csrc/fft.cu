@@ -342,6 +342,22 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
     fre[s * TPT] = xr[s];
     fim[s * TPT] = xi[s];
   }
+  if constexpr (INV) {
+    if (band.split) {  // the next MFT's operand parts, straight from the registers
+      uint16_t* sp = reinterpret_cast<uint16_t*>(band.split) + (size_t)f * 6 * plane +
+                     (size_t)row * N + u;
+#pragma unroll
+      for (int s = 0; s < E; ++s) {
+        uint32_t h[3];
+        split3_pair(xr[s], xi[s], h[0], h[1], h[2]);  // low half re, high half im
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          sp[(size_t)(2 * p) * plane + s * TPT] = (uint16_t)(h[p] & 0xffffu);
+          sp[(size_t)(2 * p + 1) * plane + s * TPT] = (uint16_t)(h[p] >> 16);
+        }
+      }
+    }
+  }
 }
 
 // Angular-spectrum transfer function (csim_fft.cpp:377-386):
@@ -536,7 +552,7 @@ static int env_choice(const char* name, std::initializer_list<int> allowed) {
 template <int N>
 static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const FresnelArgs* fa,
                    const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw,
-                   const FftBand& band, const FftBand& sup) {
+                   const FftBand& band, const FftBand& sup, __nv_bfloat16* split_out) {
   cudaStream_t st = ctx->stream;
   const float inv_scale = 1.f / ((float)N * (float)N);
   // a band-limited pass moves n rows of N (the first and last touch n x n)
@@ -549,8 +565,10 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
   auto rows = [&](bool inv, float scale, const PixOps& p, const PixOps& e,
                   const FftBand& bd) -> int {
     const bool gen = p.n && p.kind[0] == OP_SOURCE;
-    const double bytes = bd.n && !bd.src && !bd.dst ? (double)F * N * bd.n * 16.0 : edge_bytes;
-    ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, bytes * (gen ? 0.5 : 1.0));
+    const double bytes = (bd.n && !bd.src && !bd.dst ? (double)F * N * bd.n * 16.0 : edge_bytes) *
+                             (gen ? 0.5 : 1.0) +
+                         (bd.split ? (double)F * N * N * 12.0 : 0.0);
+    ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, bytes);
     if constexpr (N == 1024)
       if (e16) return launch_rows<N, 16>(st, field, F, inv, scale, tw, p, e, fi, bd);
     return launch_rows<N, default_e(N)>(st, field, F, inv, scale, tw, p, e, fi, bd);
@@ -566,7 +584,8 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
     return launch_cols<N, default_e(N), default_cols(N)>(st, field, F, mode, tw, fa, bd,
                                                          store_all);
   };
-  const FftBand whole;
+  FftBand whole, last = band;
+  whole.split = last.split = split_out;  // the last pass also writes the split
   if (fa && sup.n) {
     // rows outside the prologue's support are zero: the first row pass
     // skips them (leaving them unwritten) and the column pass reads only
@@ -577,7 +596,7 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
   } else if (fa) {
     if ((rc = rows(false, 1.f, pro, none, band))) return rc;
     if ((rc = cols(2, band, 0))) return rc;
-    return rows(true, inv_scale, none, epi, band);
+    return rows(true, inv_scale, none, epi, last);
   } else if (direction < 0) {
     if ((rc = rows(false, 1.f, pro, none, band))) return rc;
     if ((rc = cols(0, band, 0))) return rc;
@@ -607,19 +626,21 @@ bool fft_row_support(int N, int r0, int r1, int* lo, int* n) {
 // ops (pro before the transform, epi after it).
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const FftBand* band,
-                const FftBand* support) {
+                const FftBand* support, __nv_bfloat16* split_out) {
   CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
             "FFT size must be a power of two in [64, 4096]");
   CSG_CHECK(F > 0 && (long long)F * n < (1LL << 31), CSG_E_SHAPE, "FFT: bad field count");
   FftBand bd, sp;
   if (band) {
-    CSG_CHECK(fa && !pro.n && !epi.n && band->src && band->dst && !support &&
+    CSG_CHECK(fa && !pro.n && !epi.n && band->src && band->dst && !band->split && !support &&
                   fft_band_supported(n, band->lo, band->n),
               CSG_E_ARG, "FFT: unsupported band-limited transform");
     bd = *band;
   }
+  CSG_CHECK(!split_out || (fa && !band), CSG_E_ARG,
+            "FFT: the split output needs a Fresnel pass over the whole field");
   if (support) {
-    CSG_CHECK(fa && !support->src && !support->dst &&
+    CSG_CHECK(fa && !support->src && !support->dst && !support->split &&
                   fft_band_supported(n, support->lo, support->n),
               CSG_E_ARG, "FFT: unsupported row support");
     sp = *support;
@@ -635,15 +656,17 @@ int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const F
   else if (support)
     total = (double)F * n * support->n * 16.0 * (gen ? 0.5 : 1.0) +
             (double)F * n * (n + support->n) * 8.0 + pass_bytes;
+  if (split_out) total += (double)F * n * n * 12.0;
   ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0, total);
+  __nv_bfloat16* so = split_out;
   switch (n) {
-    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
-    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
-    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
-    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
-    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
-    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
-    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp);
+    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
   }
 }
 

@@ -140,21 +140,8 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
 // 8); grid.y is the field; field f reads input field in_idx[f] (f when
 // in_idx is null). The input is the R x C window at (r0, c0) of fields whose
 // planes are RT x PT (the element ops see the field's own coordinates and
-// size). The parts come from paired bf16 conversions (two values per
-// instruction), bit-identical to split3.
-__device__ __forceinline__ void split3_pair(float x0, float x1, uint32_t& h0, uint32_t& h1,
-                                            uint32_t& h2) {
-  const __nv_bfloat162 a = __floats2bfloat162_rn(x0, x1);
-  const float2 fa = __bfloat1622float2(a);
-  const float r0 = x0 - fa.x, r1 = x1 - fa.y;
-  const __nv_bfloat162 b = __floats2bfloat162_rn(r0, r1);
-  const float2 fb = __bfloat1622float2(b);
-  const __nv_bfloat162 c = __floats2bfloat162_rn(r0 - fb.x, r1 - fb.y);
-  h0 = *reinterpret_cast<const uint32_t*>(&a);
-  h1 = *reinterpret_cast<const uint32_t*>(&b);
-  h2 = *reinterpret_cast<const uint32_t*>(&c);
-}
-
+// size). The parts come from paired bf16 conversions (split3_pair, two
+// values per instruction), bit-identical to split3.
 __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int R,
                               int C, int r0, int c0, int RT, int PT,
                               const float* __restrict__ mul,
@@ -528,7 +515,7 @@ size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
 int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
                          const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
                          const PixOps& pre, const FieldInfo& fi, const MftWindow* iw,
-                         const MftWindow* ow, const int* in_idx) {
+                         const MftWindow* ow, const int* in_idx, bool presplit) {
   CSG_CHECK(ctx && m && in && out && slot, CSG_E_ARG, "csg_mft_execute: null argument");
   CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_mft_execute: n_fields must be positive");
   CSG_CHECK(!in_mul || mul_idx, CSG_E_ARG, "csg_mft_execute: in_mul needs mul_idx");
@@ -549,7 +536,9 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
   auto* tt = static_cast<__nv_bfloat16*>(m->tt.ptr);
 
   const double F = n_fields;
-  {
+  CSG_CHECK(!presplit || (!in_mul && !pre.n && !iw && !in_idx), CSG_E_ARG,
+            "csg_mft_execute: a split input takes no input ops, window or index");
+  if (!presplit) {  // else the producer of the input wrote split_in
     ProfScope ps(ctx, "mft_split", 0, F * m->ny * m->nx * (8.0 + 12.0 + (in_mul ? 8.0 : 0.0)));
     CSG_CHECK(n_fields < 65536, CSG_E_SHAPE, "csg_mft_execute: too many fields in one call");
     dim3 grid(grid_for((long long)m->ny * m->nx / 8, 256, 1024), n_fields);
@@ -631,6 +620,17 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     if (rc) return rc;
   }
   return CSG_OK;
+}
+
+__nv_bfloat16* csg::mft_split_buffer(csg_mft* m, int n_fields) {
+  if (!m || n_fields <= 0) return nullptr;
+  if (m->split_in.ensure((size_t)n_fields * 12 * m->ny * m->nx)) return nullptr;
+  return static_cast<__nv_bfloat16*>(m->split_in.ptr);
+}
+
+void csg::mft_input_shape(const csg_mft* m, int* ny, int* nx) {
+  *ny = m->ny;
+  *nx = m->nx;
 }
 
 extern "C" int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float* out,

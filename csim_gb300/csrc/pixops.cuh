@@ -272,6 +272,9 @@ struct FftBand {
   int lo = 0, n = 0;
   const float* src = nullptr;
   float* dst = nullptr;
+  // inverse row pass only: also store the three-part bf16 split of the
+  // result, [F][3][2][N][N] (an MFT's operand layout), beside the fp32 field
+  __nv_bfloat16* split = nullptr;
 };
 
 // 2-D FFT (direction -1 / +1) or, with fa, Fresnel propagation of F square
@@ -280,9 +283,12 @@ struct FftBand {
 // rows [lo, lo + n) once pro is applied (a mask's support), so the first row
 // pass transforms only those rows and the column pass reads only them; the
 // other rows of the field are not read before they are overwritten.
+// split_out (with fa, without band): the last pass also writes the result's
+// three-part bf16 split in the layout of an N x N MFT's input (mft_split_buffer).
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi,
-                const FftBand* band = nullptr, const FftBand* support = nullptr);
+                const FftBand* band = nullptr, const FftBand* support = nullptr,
+                __nv_bfloat16* split_out = nullptr);
 // Whether fft2d_fused can run an N-point padded transform band-limited to
 // [lo, lo + n).
 bool fft_band_supported(int N, int lo, int n);
@@ -302,6 +308,13 @@ struct MftWindow {
 int mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
                     const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
                     const PixOps& pre, const FieldInfo& fi, const MftWindow* iw = nullptr,
-                    const MftWindow* ow = nullptr, const int* in_idx = nullptr);
+                    const MftWindow* ow = nullptr, const int* in_idx = nullptr,
+                    bool presplit = false);
+// The plan's input split buffer, [n_fields][3][2][ny][nx] bf16, grown to
+// n_fields (nullptr: allocation failed). A producer that writes it lets
+// mft_execute_ops run with presplit = true, which skips the split pass.
+__nv_bfloat16* mft_split_buffer(csg_mft* m, int n_fields);
+// Input rows and columns of a plan.
+void mft_input_shape(const csg_mft* m, int* ny, int* nx);
 
 }  // namespace csg

@@ -3,8 +3,10 @@ FP64 oracle, including the reference's own 2N-convolution fpmPupToLyot.
 
 Errors are peak-normalised to the calibration (FPM-free) image peak, the
 normalisation the dark-hole contrast uses (regionContrast.cpp:145-195).
-Bounds: field error <= 1e-6 of the calibration peak; contrast (mean
-normalised intensity over a 2-8 lambda/D annulus) within 1%.
+Bounds: field error < 1e-6 of the calibration peak (the fp32-storage floor
+of the full-size chain is 1.0e-7; this path measures 3.7e-7 to 5.0e-7, a
+plain complex64 evaluation 1.3e-6 to 1.9e-6); contrast (mean normalised
+intensity over a 2-8 lambda/D annulus) within 1%.
 """
 import math
 
@@ -69,9 +71,11 @@ def test_piaacmc_chain_matches_oracle(ctx, conv_form):
         refs.append(oc.piaacmc_field(*args, conv_form=conv_form))
         rcal.append(oc.piaacmc_field(*args, calibrating=True))
         peak = max(peak, np.abs(rcal[-1]).max())
-    for f in range(len(refs)):
-        assert np.abs(gcal[f] - rcal[f]).max() / peak < 1e-6
-        assert np.abs(got[f] - refs[f]).max() / peak < 1e-6
+    e_cal = max(np.abs(gcal[f] - rcal[f]).max() for f in range(len(refs))) / peak
+    e_img = max(np.abs(got[f] - refs[f]).max() for f in range(len(refs))) / peak
+    print(f"\npiaacmc n={spec.n} conv_form={conv_form}: calibration field {e_cal:.3e}, final "
+          f"field {e_img:.3e} (of the calibration peak)")
+    assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
     if conv_form:
         return
     # dark-hole contrast per candidate, 2-8 lambda/D
@@ -86,6 +90,88 @@ def test_piaacmc_chain_matches_oracle(ctx, conv_form):
         full = (np.abs(np.array(refs[c * per:(c + 1) * per])) ** 2).sum(0)
         ref_con = oe.region_contrast(full, np.full_like(full, rcmax), reg.mask)
         assert abs(con[c] - ref_con) / ref_con < 0.01, (con[c], ref_con)
+
+
+def test_piaacmc_full_size_field_and_contrast(ctx):
+    """The 1024^2 PIAACMC configuration itself (512^2 mask grid, 217 hexes,
+    64 x 64 sub-pixel tables, 256^2 image, the mask's support crop), three
+    candidates and an on-axis plus an off-axis source, against the FP64
+    oracle: final and calibration fields within 1e-6 of the calibration peak
+    (measured 3.7e-7 and 5.0e-7; storing the fields and tables in fp32 alone,
+    with exact arithmetic, already costs 1.0e-7), closer to the oracle than
+    the same chain evaluated plainly in complex64 (cuFFT, complex64 matmuls:
+    1.3e-6), and dark-hole contrast (2-8 lambda/D) within 1%."""
+    from baseline.fp64_gpu import Fp64Piaacmc
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import workloads as W
+    spec = W.PiaacmcSpec()
+    sources = [cg.PointSource(1.0, 0.0, 0.0), cg.PointSource(0.3, 0.015, -0.01)]
+    cor, inp = W.build_piaacmc(ctx, spec, sources)
+    n_cand = 3
+    sags = W.random_sags(np.random.default_rng(21), n_cand, spec.n_hex, spec.sag_range)
+    cor.sags(n_cand).copy_(torch.as_tensor(sags))
+    F = cor.batch_all(n_cand)
+    img = cor.execute(calibrating=False).clone()
+    cal = cor.execute(calibrating=True).clone()
+    ctx.sync()
+    got = img[:, 0].double().cpu().numpy() + 1j * img[:, 1].double().cpu().numpy()
+    gcal = cal[:, 0].double().cpu().numpy() + 1j * cal[:, 1].double().cpu().numpy()
+    li, amp, tip, tilt, cand = cor._batch
+    lam = inp["lam"]
+    refs, rcal = [], []
+    for f in range(F):
+        args = (inp, spec, lam[li[f]], amp[f], tip[f], tilt[f], sags[cand[f]])
+        refs.append(oc.piaacmc_field(*args))
+        rcal.append(oc.piaacmc_field(*args, calibrating=True))
+    peak = max(np.abs(r).max() for r in rcal)
+    e_cal = max(np.abs(gcal[f] - rcal[f]).max() for f in range(F)) / peak
+    e_img = max(np.abs(got[f] - refs[f]).max() for f in range(F)) / peak
+    reg = cg.RegionContrast(ctx, img.shape[-1], cor.out_pixel, inp["lod_image"], 2.0, 8.0)
+    per = F // n_cand
+    cmax = (np.abs(gcal[:per]) ** 2).sum(0).max()
+    con = reg.contrast(img, per, cmax).cpu().numpy()
+    rcmax = (np.abs(np.array(rcal[:per])) ** 2).sum(0).max()
+    e_con = 0.0
+    for c in range(n_cand):
+        full = (np.abs(np.array(refs[c * per:(c + 1) * per])) ** 2).sum(0)
+        ref_con = oe.region_contrast(full, np.full_like(full, rcmax), reg.mask)
+        e_con = max(e_con, abs(con[c] - ref_con) / ref_con)
+    # the plain complex64 path on the on-axis fields (source 0 of each candidate)
+    plain = Fp64Piaacmc(inp, spec, dtype=torch.complex64)
+    e_plain = e_ours = 0.0
+    for c in range(n_cand):
+        f = c * per
+        g = plain.field(int(li[f]), float(amp[f]), torch.as_tensor(sags[c], device="cuda"))
+        g = g.to(torch.complex128).cpu().numpy()
+        e_plain = max(e_plain, np.abs(g - refs[f]).max() / peak)
+        e_ours = max(e_ours, np.abs(got[f] - refs[f]).max() / peak)
+    print(f"\nfull-size piaacmc: calibration field {e_cal:.3e}, final field {e_img:.3e} "
+          f"(of the calibration peak; on-axis {e_ours:.3e}, plain complex64 path "
+          f"{e_plain:.3e}), contrast {e_con:.3e} relative")
+    assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
+    assert e_ours < e_plain, (e_ours, e_plain)
+    assert e_con < 0.01, e_con
+
+
+def test_fresnel_split_handoff_is_exact(ctx, monkeypatch):
+    """The Fresnel's last row pass writing the hex FPM's operand split (the
+    default) gives bit-identical images to the separate split pass
+    (CSG_FRESNEL_SPLIT=0): the parts come from the same fp32 values."""
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import workloads as W
+    spec = small_spec()
+    cor, inp = W.build_piaacmc(ctx, spec, [cg.PointSource(1.0, 0.0, 0.0),
+                                           cg.PointSource(0.5, 0.02, -0.01)])
+    cor.sags(3).copy_(torch.as_tensor(W.random_sags(np.random.default_rng(8), 3,
+                                                    inp["hex_x"].size, 5e-7)))
+    cor.batch_all(3)
+    outs = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("CSG_FRESNEL_SPLIT", flag)
+        outs.append(cor.execute(use_graph=False).clone())
+    ctx.sync()
+    assert torch.equal(outs[0], outs[1])
+    cor.close()
 
 
 def test_fpm_support_crop_is_exact(ctx):

@@ -45,9 +45,8 @@ def test_plain_lyot_matches_oracle(ctx, full, babinet):
         rcal.append(oc.plain_lyot_field(inp, spec, int(li[f]), amp[f], tip[f], tilt[f],
                                         calibrating=True))
     peak = max(np.abs(r).max() for r in rcal)
-    for f in range(F):
-        assert np.abs(cal[f] - rcal[f]).max() / peak < 1e-6
-        assert np.abs(img[f] - refs[f]).max() / peak < 1e-6
+    e_cal = max(np.abs(cal[f] - rcal[f]).max() for f in range(F)) / peak
+    e_img = max(np.abs(img[f] - refs[f]).max() for f in range(F)) / peak
     # contrast over 3-12 lambda/D (outside the 3 lambda/D occulter)
     n_out = img.shape[-1]
     reg = cg.RegionContrast(ctx, n_out, cor.out_pixel, inp["lod_image"], 3.0,
@@ -57,6 +56,10 @@ def test_plain_lyot_matches_oracle(ctx, full, babinet):
     rfull = (np.abs(np.array(refs)) ** 2).sum(0)
     rmax = (np.abs(np.array(rcal)) ** 2).sum(0).max()
     ref_con = oe.region_contrast(rfull, np.full_like(rfull, rmax), reg.mask)
+    print(f"\nplain Lyot n={spec.n} babinet={babinet}: calibration field {e_cal:.3e}, final "
+          f"field {e_img:.3e} (of the calibration peak), contrast "
+          f"{abs(con - ref_con) / ref_con:.3e} relative")
+    assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
     assert abs(con - ref_con) / ref_con < 0.01, (con, ref_con)
     assert ref_con < 1e-2  # the occulter and stop do suppress the star
     cor.close()
