@@ -612,11 +612,12 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
                                  (long long)n_fields * 2, outw.pitch, outw.rows)
                     ? 1
                     : 0;
+    const CUtensorMap* tmo = p.tma_out ? &to : nullptr;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->mo * m->no * m->ny);
-    rc = bn1 == 64    ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st, &to)
-         : bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st, &to)
-                      : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st, &to);
+    rc = bn1 == 64    ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo)
+         : bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo)
+                      : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo);
     if (rc) return rc;
   }
   return CSG_OK;

@@ -158,6 +158,7 @@ def test_fresnel_split_handoff_is_exact(ctx, monkeypatch):
     """The Fresnel's last row pass writing the hex FPM's operand split (the
     default) gives bit-identical images to the separate split pass
     (CSG_FRESNEL_SPLIT=0): the parts come from the same fp32 values."""
+    from csim_gb300 import _lib
     from csim_gb300 import coronagraph as cg
     from csim_gb300 import workloads as W
     spec = small_spec()
@@ -166,11 +167,15 @@ def test_fresnel_split_handoff_is_exact(ctx, monkeypatch):
     cor.sags(3).copy_(torch.as_tensor(W.random_sags(np.random.default_rng(8), 3,
                                                     inp["hex_x"].size, 5e-7)))
     cor.batch_all(3)
-    outs = []
+    cor.execute(use_graph=False)  # plans, buffers and tile tuning first
+    outs, launches = [], []
     for flag in ("1", "0"):
         monkeypatch.setenv("CSG_FRESNEL_SPLIT", flag)
+        n0 = _lib.api["csg_launch_count"]()
         outs.append(cor.execute(use_graph=False).clone())
+        launches.append(_lib.api["csg_launch_count"]() - n0)
     ctx.sync()
+    assert launches[1] - launches[0] == 1  # one split pass fewer
     assert torch.equal(outs[0], outs[1])
     cor.close()
 
