@@ -343,17 +343,30 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
     fim[s * TPT] = xi[s];
   }
   if constexpr (INV) {
-    if (band.split) {  // the next MFT's operand parts, straight from the registers
-      uint16_t* sp = reinterpret_cast<uint16_t*>(band.split) + (size_t)f * 6 * plane +
-                     (size_t)row * N + u;
+    if (band.split) {
+      // The next MFT's operand parts, straight from the registers. Lane pairs
+      // (u, u ^ 1) swap one value per two slots so that each lane holds two
+      // adjacent columns of one slot (the even lane of slot s, the odd lane
+      // of slot s + 1) and stores every part as one bf16x2 word. TPT is even
+      // and a warp holds whole rows, so the pair is in the same row.
+      const int odd = u & 1;
+      const size_t plane2 = plane / 2;
+      uint32_t* sp = reinterpret_cast<uint32_t*>(band.split) +
+                     ((size_t)f * 6 * plane + (size_t)row * N + (u - odd)) / 2;
 #pragma unroll
-      for (int s = 0; s < E; ++s) {
-        uint32_t h[3];
-        split3_pair(xr[s], xi[s], h[0], h[1], h[2]);  // low half re, high half im
+      for (int s = 0; s < E; s += 2) {
+        const float rr = __shfl_xor_sync(0xffffffffu, odd ? xr[s] : xr[s + 1], 1);
+        const float ri = __shfl_xor_sync(0xffffffffu, odd ? xi[s] : xi[s + 1], 1);
+        const float ar = odd ? rr : xr[s], br = odd ? xr[s + 1] : rr;  // columns c, c + 1
+        const float ai = odd ? ri : xi[s], bi = odd ? xi[s + 1] : ri;
+        uint32_t hr[3], hi[3];
+        split3_pair(ar, br, hr[0], hr[1], hr[2]);
+        split3_pair(ai, bi, hi[0], hi[1], hi[2]);
+        const size_t w = (size_t)(odd ? s + 1 : s) * (TPT / 2);
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-          sp[(size_t)(2 * p) * plane + s * TPT] = (uint16_t)(h[p] & 0xffffu);
-          sp[(size_t)(2 * p + 1) * plane + s * TPT] = (uint16_t)(h[p] >> 16);
+          sp[(size_t)(2 * p) * plane2 + w] = hr[p];
+          sp[(size_t)(2 * p + 1) * plane2 + w] = hi[p];
         }
       }
     }
