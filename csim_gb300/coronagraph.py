@@ -56,6 +56,23 @@ class ComplexMask:
 
 
 @dataclass
+class DoubleFraunhoferInterpFPM:
+    """doubleFraunhoferInterpFPM with its complexHexMaskFPM: zoom FFT of the
+    field to a padFactor N grid of pixel fpmScale (metres) at lambda f =
+    3.52 lambda, the hex mask (tables [3][S][S], candidate sags, phaseSign)
+    on the centred S x S block, zoom FFT back at -3.52 lambda."""
+    hex_id: np.ndarray
+    count: np.ndarray
+    n_sub: int
+    n_hex: int
+    fpmScale: float
+    padFactor: float = 2.0
+    phaseSign: float = 1.0
+    disableForCalibration: bool = True
+    lambdaFocalFactor: float = 3.52  # doubleFraunhoferInterpFPM.cpp:99
+
+
+@dataclass
 class FpmPupToLyotHex:
     """fpmPupToLyot + fpmIntHexCMCForPupToLyot + complexHexMaskFPM: hex tables
     [3][S][S] (ids, counts), nSubPix, hex count, mask pixel scale (metres),
@@ -162,6 +179,13 @@ class Coronagraph:
                  cnt.ctypes.data_as(C.c_void_p), ids.shape[-1], e.n_sub, e.n_hex, e.pixelScale,
                  e.focalRatio, self.ef.beamRadiusPhysical, e.fRatioSign, e.zoomFftSign,
                  e.phaseSign, int(e.disableForCalibration))
+            self.n_hex = e.n_hex
+        elif isinstance(e, DoubleFraunhoferInterpFPM):
+            ids = np.ascontiguousarray(e.hex_id, np.int16)
+            cnt = np.ascontiguousarray(e.count, np.uint16)
+            call("csg_chain_add_fpm_hex_double", self.h, ids.ctypes.data_as(C.c_void_p),
+                 cnt.ctypes.data_as(C.c_void_p), ids.shape[-1], e.n_sub, e.n_hex, e.fpmScale,
+                 e.padFactor, e.lambdaFocalFactor, e.phaseSign, int(e.disableForCalibration))
             self.n_hex = e.n_hex
         elif isinstance(e, PaddedFftFpm):
             L = len(self.ef.wavelengths)

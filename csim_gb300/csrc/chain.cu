@@ -43,7 +43,16 @@ int hex_mask_with_phasor_buffer(csg_ctx* ctx, const int16_t* hex_id, const uint1
                                 const int* cand, const double* lambda, double phase_sign, int flip,
                                 double subtract, int use_only_hex, float* out, float2* phasors);
 
-enum ElemKind { E_MASK, E_MIRROR, E_FRESNEL, E_CMASK, E_FPM_HEX, E_FRAUNHOFER, E_FFT_FPM };
+enum ElemKind {
+  E_MASK,
+  E_MIRROR,
+  E_FRESNEL,
+  E_CMASK,
+  E_FPM_HEX,
+  E_FRAUNHOFER,
+  E_FFT_FPM,
+  E_FPM_HEX_DOUBLE
+};
 
 template <typename T>
 static T* dev_copy(const T* h, size_t n, cudaStream_t st) {
@@ -83,6 +92,11 @@ struct Elem {
   double phase_sign = 1.0;
   csg_mft* mft1 = nullptr;
   csg_mft* mft2 = nullptr;
+  // double-Fraunhofer hex FPM: mft1 field -> zoom grid, mft2 zoom grid ->
+  // field, mft3 the mask block of the zoom grid -> field; nz x nz zoom grid
+  // with the S x S block at (zr0, zr0)
+  csg_mft* mft3 = nullptr;
+  int nz = 0, zr0 = 0;
   // fraunhofer
   csg_mft* mft = nullptr;
   int n_out = 0;
@@ -214,6 +228,7 @@ int csg_chain_destroy(csg_chain* c) {
     cudaFree(e.dmask);
     csg_mft_destroy(e.mft1);
     csg_mft_destroy(e.mft2);
+    csg_mft_destroy(e.mft3);
     csg_mft_destroy(e.mft);
   }
   for (void* p : {(void*)c->slot, (void*)c->lam_f, (void*)c->amp, (void*)c->tip, (void*)c->tilt,
@@ -422,6 +437,73 @@ int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* c
   e.lf = lf;
   e.pref = pref2;
   e.dm = dm;
+  c->elems.push_back(e);
+  c->planned = false;
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// doubleFraunhoferInterpFPM (doubleFraunhoferInterpFPM.cpp:24-65, geometry
+// :86-121) with its complexHexMaskFPM (complexHexMaskFPM.cpp:25-42): the
+// mask multiplies the centred S x S block of the zoom grid and leaves the
+// rest, so E_out = MFT_out[Z] + MFT_out restricted to the block[(M - 1) Z].
+int csg_chain_add_fpm_hex_double(csg_chain* c, const int16_t* hex_id, const uint16_t* count,
+                                 int S, int n_sub, int n_hex, double fpm_scale, double pad_factor,
+                                 double lf_factor, double phase_sign,
+                                 int disable_for_calibration) {
+  CSG_CHECK(c && hex_id && count, CSG_E_ARG, "csg_chain_add_fpm_hex_double: null argument");
+  const int n = c->n, L = c->n_lambda;
+  const int nz = (int)(pad_factor * n);  // int nRows = padFactor * nRowsE
+  CSG_CHECK(S >= 8 && S % 8 == 0 && n_sub > 0 && n_hex > 0 && nz % 8 == 0 && nz >= S &&
+                fpm_scale > 0.0 && lf_factor != 0.0,
+            CSG_E_SHAPE,
+            "csg_chain_add_fpm_hex_double: S and pad_factor N must be multiples of 8, "
+            "pad_factor N >= S");
+  DeviceGuard g(c->ctx->device);
+  cudaStream_t st = c->ctx->stream;
+  Elem e;
+  e.kind = E_FPM_HEX_DOUBLE;
+  e.S = S;
+  e.n_sub = n_sub;
+  e.n_hex = n_hex;
+  e.phase_sign = phase_sign;
+  e.disable_for_calibration = disable_for_calibration;
+  e.nz = nz;
+  e.zr0 = nz / 2 - S / 2;  // tcMat.n_rows / 2 - complexIntMask.n_rows / 2
+  e.r0 = e.c0 = 0;
+  e.RR = e.CC = S;
+  e.hex_id = dev_copy(hex_id, (size_t)3 * S * S, st);
+  e.count = dev_copy(count, (size_t)3 * S * S, st);
+  CSG_CHECK(e.hex_id && e.count, CSG_E_NOMEM, "csg_chain_add_fpm_hex_double: allocation failed");
+  // zoom grid (i - n/2) fpm_scale; field pixel centres
+  std::vector<double> xz(nz), xp = pixel_centres(n, c->dx);
+  for (int i = 0; i < nz; ++i) xz[i] = ((double)i - (double)nz / 2.0) * fpm_scale;
+  std::vector<double> lf_in(L), lf_out(L), pin(2 * L), pout(2 * L);
+  for (int l = 0; l < L; ++l) {
+    lf_in[l] = lf_factor * c->lambda[l];
+    lf_out[l] = -lf_in[l];
+    // zoomFft prefactor dx_in dy_in / (i lambda f) (csim_fft.cpp:794-801)
+    pin[2 * l] = 0.0;
+    pin[2 * l + 1] = -c->dx * c->dx / lf_in[l];
+    pout[2 * l] = 0.0;
+    pout[2 * l + 1] = -fpm_scale * fpm_scale / lf_out[l];
+  }
+  int rc = csg_mft_create(c->ctx, &e.mft1, n, n, nz, nz, xp.data(), xp.data(), xz.data(),
+                          xz.data(), L, lf_in.data(), pin.data(), -1.0, c->precision);
+  if (!rc)
+    rc = csg_mft_create(c->ctx, &e.mft2, nz, nz, n, n, xz.data(), xz.data(), xp.data(), xp.data(),
+                        L, lf_out.data(), pout.data(), -1.0, c->precision);
+  if (!rc)
+    rc = csg_mft_create(c->ctx, &e.mft3, S, S, n, n, xz.data() + e.zr0, xz.data() + e.zr0,
+                        xp.data(), xp.data(), L, lf_out.data(), pout.data(), -1.0, c->precision);
+  if (rc) {
+    csg_mft_destroy(e.mft1);
+    csg_mft_destroy(e.mft2);
+    csg_mft_destroy(e.mft3);
+    cudaFree(e.hex_id);
+    cudaFree(e.count);
+    return rc;
+  }
   c->elems.push_back(e);
   c->planned = false;
   drop_graph(c);
@@ -798,6 +880,14 @@ static int prepare(csg_chain* c) {
       int rc = csg_mft_reserve(e.mft1, c->n_fields);
       if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
       if (rc) return rc;
+    } else if (e.kind == E_FPM_HEX_DOUBLE) {
+      fpm_need = std::max(fpm_need, F * 2 * (size_t)e.S * e.S * sizeof(float));
+      ph_need = std::max(ph_need, F * (e.n_hex + 1) * sizeof(float2));
+      pad_need = std::max(pad_need, F * 2 * (size_t)e.nz * e.nz * sizeof(float));  // zoom grid
+      int rc = csg_mft_reserve(e.mft1, c->n_fields);
+      if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
+      if (!rc) rc = csg_mft_reserve(e.mft3, c->n_fields);
+      if (rc) return rc;
     } else if (e.kind == E_FFT_FPM && e.bab == 0) {
       pad_need = std::max(pad_need, F * 2 * (size_t)e.P * e.P * sizeof(float));
     } else if (e.kind == E_FRAUNHOFER) {
@@ -821,7 +911,7 @@ static int prepare(csg_chain* c) {
 // ops right after it in its last row pass, ops before the final MFT in its
 // operand split; only ops with no such neighbour get one standalone pass.
 struct Step {
-  enum Kind { PIX, FRESNEL, FPM, FINAL, FFT_FPM } kind;
+  enum Kind { PIX, FRESNEL, FPM, FINAL, FFT_FPM, FPM_DOUBLE } kind;
   PixOps pro, epi;
   const Elem* e = nullptr;
   int sup0 = 0, sup1 = 1 << 30;  // FRESNEL: rows that can be nonzero on input
@@ -903,6 +993,10 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
       pend = PixOps();
       prog.push_back(Step{Step::FPM, PixOps(), PixOps(), &e});
       epi_open = false;
+    } else if (e.kind == E_FPM_HEX_DOUBLE) {
+      prog.push_back(Step{Step::FPM_DOUBLE, pend, PixOps(), &e});  // ops ride in its split
+      pend = PixOps();
+      epi_open = false;
     } else if (e.kind == E_FFT_FPM) {
       prog.push_back(Step{Step::FFT_FPM, pend, PixOps(), &e});  // ops ride in the padding pass
       pend = PixOps();
@@ -976,6 +1070,28 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         rc = mft_execute_ops(ctx, s.e->mft, c->field, c->image, F, c->slot, 0, nullptr, nullptr,
                              s.pro, fi, &s.e->win, nullptr);
         break;
+      case Step::FPM_DOUBLE: {
+        const Elem& e = *s.e;
+        CSG_CHECK(c->sags && c->sag_hex == e.n_hex, CSG_E_STATE,
+                  "hex FPM: candidate sags not set (csg_chain_sags) or wrong hex count");
+        // M - 1 (no flip) for each field's (candidate, wavelength)
+        rc = hex_mask_region(ctx, e.hex_id, e.count, e.S, 0, 0, e.S, e.S, e.n_sub, c->sags,
+                             e.n_hex, F, c->cand, c->lam_f, e.phase_sign, 0, 1.0, c->fpm_mask,
+                             c->phasors);
+        // Z = zoom grid field (the element ops ride in the split)
+        if (!rc)
+          rc = mft_execute_ops(ctx, e.mft1, c->field, c->padbuf, F, c->slot, 0, nullptr, nullptr,
+                               s.pro, fi);
+        // E = MFT_out[Z] + MFT_out[(M - 1) Z] over the mask block
+        if (!rc)
+          rc = mft_execute_ops(ctx, e.mft2, c->padbuf, c->field, F, c->slot, 0, nullptr, nullptr,
+                               PixOps(), fi);
+        const MftWindow blk{e.zr0, e.zr0, e.nz, e.nz};
+        if (!rc)
+          rc = mft_execute_ops(ctx, e.mft3, c->padbuf, c->field, F, c->slot, 1, c->fpm_mask,
+                               c->ident, PixOps(), fi, &blk, nullptr);
+        break;
+      }
       case Step::FFT_FPM: {
         const Elem& e = *s.e;
         if (e.bab) {

@@ -252,6 +252,20 @@ int csg_chain_add_fresnel(csg_chain* chain, double z, double ap_rad);
 /* complexMask (complexMask.cpp:24-66): centred amp exp(-i ph), host fp32. */
 int csg_chain_add_complex_mask(csg_chain* chain, const float* amp, const float* ph, int mrows,
                                int mcols, int disable_for_calibration);
+/* doubleFraunhoferInterpFPM with complexHexMaskFPM
+ * (doubleFraunhoferInterpFPM.cpp:24-65, init_geom :86-121;
+ * complexHexMaskFPM.cpp:25-42): zoom FFT of the field to a zoom grid of
+ * pad_factor N pixels of size fpm_scale at coordinates (i - n/2) fpm_scale
+ * with lambda f = lf_factor lambda (3.52 in the reference), the S x S
+ * interpolated hex mask M (candidate sags, no flip) multiplied onto the
+ * centred block of that grid, and the zoom FFT back at -lf_factor lambda.
+ * Computed as Z = MFT_in[E]; E <- MFT_out[Z] + MFT_out,box[(M - 1) Z_box]:
+ * three split-bf16 transforms, the last accumulating. Tables as
+ * csg_hex_mask; S a multiple of 8, pad_factor N a multiple of 8 and >= S. */
+int csg_chain_add_fpm_hex_double(csg_chain* chain, const int16_t* hex_id, const uint16_t* count,
+                                 int S, int n_sub, int n_hex, double fpm_scale, double pad_factor,
+                                 double lf_factor, double phase_sign,
+                                 int disable_for_calibration);
 /* fpmPupToLyot + fpmIntHexCMCForPupToLyot + complexHexMaskFPM
  * (fpmPupToLyot.cpp:24-167, 419-455; complexHexMaskFPM.cpp:44-99) in
  * matrix-Fourier Babinet form, algebraically identical to the reference's

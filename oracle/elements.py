@@ -215,6 +215,31 @@ def complex_interpolated_mask(hexnum: np.ndarray, nsub: np.ndarray, sags: np.nda
     return (n * np.exp(phase_sign * 2 * math.pi * 1j * 2.0 * sag / lam)).sum(0) / float(n_sub_pix * n_sub_pix)
 
 
+def double_fraunhofer_interp_fpm(cube, lambdas, egeom: ArrayGeom, fpm_scale: float,
+                                 pad_factor: float, masks, lf_factor: float = 3.52):
+    """doubleFraunhoferInterpFPM::execute (doubleFraunhoferInterpFPM.cpp:24-65)
+    with its geometry (init_geom, :86-121) and complexHexMaskFPM::execute
+    (complexHexMaskFPM.cpp:25-42), per wavelength slice: zoomFft of E to an
+    nz x nz grid (nz = int(padFactor N), pixel centres (i - nz/2) fpmScale)
+    at lambda f = 3.52 lambda; the S x S mask multiplies the block starting at
+    (nz/2 - S/2, nz/2 - S/2), the rest of the grid is left as it is; zoomFft
+    back to E's geometry at -3.52 lambda. masks[sl] is the complex
+    interpolated mask of slice sl (complex_interpolated_mask, no flip)."""
+    cube = np.asarray(cube, dtype=np.complex128)
+    n = cube.shape[-1]
+    nz = int(pad_factor * n)
+    zg = ArrayGeom.set_xy_offset_m1(nz, nz, fpm_scale)
+    out = np.empty_like(cube)
+    for sl, lam in enumerate(lambdas):
+        lf_in = lf_factor * lam
+        z = ZoomFft(egeom, zg, [lf_in]).mft(cube[sl], 0)
+        m = np.asarray(masks[sl])
+        r0, c0 = nz // 2 - m.shape[0] // 2, nz // 2 - m.shape[1] // 2
+        z[r0:r0 + m.shape[0], c0:c0 + m.shape[1]] *= m
+        out[sl] = ZoomFft(zg, egeom, [-lf_in]).mft(z, 0)
+    return out
+
+
 def hex_mask_pixel_scale(beam_radius: float, pixel_scale: float, mask_size: int,
                          zoom_factor: float, lambda_ref: float, fpm_f_ratio: float) -> float:
     """complexHexMaskFPM.cpp:199-206 / :367-369 compute_fpmScale."""
