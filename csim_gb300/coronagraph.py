@@ -56,6 +56,22 @@ class ComplexMask:
 
 
 @dataclass
+class FpmPupToLyotMask:
+    """fpmPupToLyot with a fixed mask (fpmCMCForPupToLyot, fpmBinaryForPupToLyot):
+    complex mask [n_mask][rows][cols] (or 2-D) of pixel pixelScale (metres),
+    lambdaFocalLength per wavelength (with fRatioSign), doBabinet; calibMask
+    (None: ones) is what the calibration walk applies when disabled for it."""
+    mask: np.ndarray
+    pixelScale: float
+    lambdaFocalLength: np.ndarray
+    fRatioSign: float = -1.0
+    zoomFftSign: float = -1.0
+    doBabinet: bool = True
+    calibMask: np.ndarray | None = None
+    disableForCalibration: bool = True
+
+
+@dataclass
 class DoubleFraunhoferInterpFPM:
     """doubleFraunhoferInterpFPM with its complexHexMaskFPM: zoom FFT of the
     field to a padFactor N grid of pixel fpmScale (metres) at lambda f =
@@ -180,6 +196,21 @@ class Coronagraph:
                  e.focalRatio, self.ef.beamRadiusPhysical, e.fRatioSign, e.zoomFftSign,
                  e.phaseSign, int(e.disableForCalibration))
             self.n_hex = e.n_hex
+        elif isinstance(e, FpmPupToLyotMask):
+            m = np.asarray(e.mask)
+            m = m[None] if m.ndim == 2 else m
+            re, im = _f32(m.real), _f32(m.imag)
+            lf = np.ascontiguousarray(e.lambdaFocalLength, np.float64)
+            cre = cim = None
+            if e.calibMask is not None:
+                cm = np.asarray(e.calibMask)
+                cm = cm[None] if cm.ndim == 2 else cm
+                assert cm.shape == m.shape, "calibMask must have the mask's shape"
+                cre, cim = _f32(cm.real), _f32(cm.imag)
+            ptr = lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None  # noqa: E731
+            call("csg_chain_add_fpm_mask", self.h, ptr(re), ptr(im), m.shape[0], m.shape[1],
+                 m.shape[2], e.pixelScale, ptr(lf), e.fRatioSign, e.zoomFftSign,
+                 int(e.doBabinet), ptr(cre), ptr(cim), int(e.disableForCalibration))
         elif isinstance(e, DoubleFraunhoferInterpFPM):
             ids = np.ascontiguousarray(e.hex_id, np.int16)
             cnt = np.ascontiguousarray(e.count, np.uint16)

@@ -51,7 +51,8 @@ enum ElemKind {
   E_FPM_HEX,
   E_FRAUNHOFER,
   E_FFT_FPM,
-  E_FPM_HEX_DOUBLE
+  E_FPM_HEX_DOUBLE,
+  E_FPM_MASK
 };
 
 template <typename T>
@@ -110,6 +111,9 @@ struct Elem {
   int bab = 0;
   int br0 = 0, bc0 = 0, bR = 0, bC = 0;
   float* dmask = nullptr;  // [L][2][bR][bC] planar: 1 - M on the box
+  // fixed-mask fpmPupToLyot: cmask the calibration mask (M - 1 or M like
+  // dmask, [L][2][RR][CC]); null when calibration leaves the field as it is
+  float* cmask = nullptr;
   // per-wavelength tables (mirror phasors, Fresnel transfer function)
   float2* tab = nullptr;
   // mirror right after a real mask: the mask times the phasor table
@@ -226,6 +230,7 @@ int csg_chain_destroy(csg_chain* c) {
     cudaFree(e.tab);
     cudaFree(e.tab_m);
     cudaFree(e.dmask);
+    cudaFree(e.cmask);
     csg_mft_destroy(e.mft1);
     csg_mft_destroy(e.mft2);
     csg_mft_destroy(e.mft3);
@@ -437,6 +442,76 @@ int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* c
   e.lf = lf;
   e.pref = pref2;
   e.dm = dm;
+  c->elems.push_back(e);
+  c->planned = false;
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// fpmPupToLyot with a fixed mask (the CMC and binary adapters,
+// fpmPupToLyot.cpp:303-367, 521-557): the hex element's transform pair with
+// the mask uploaded once per wavelength instead of built from sags.
+int csg_chain_add_fpm_mask(csg_chain* c, const float* mask_re, const float* mask_im, int n_mask,
+                           int rows, int cols, double mask_pixel, const double* lf,
+                           double f_ratio_sign, double zoom_fft_sign, int babinet,
+                           const float* calib_re, const float* calib_im,
+                           int disable_for_calibration) {
+  CSG_CHECK(c && mask_re && lf, CSG_E_ARG, "csg_chain_add_fpm_mask: null argument");
+  const int n = c->n, L = c->n_lambda;
+  CSG_CHECK(rows >= 8 && cols >= 8 && rows % 8 == 0 && cols % 8 == 0 &&
+                (n_mask == 1 || n_mask == L) && mask_pixel > 0.0,
+            CSG_E_SHAPE,
+            "csg_chain_add_fpm_mask: rows and cols must be multiples of 8, n_mask 1 or n_lambda");
+  DeviceGuard g(c->ctx->device);
+  cudaStream_t st = c->ctx->stream;
+  Elem e;
+  e.kind = E_FPM_MASK;
+  e.disable_for_calibration = disable_for_calibration;
+  e.bab = babinet ? 1 : 0;
+  e.r0 = e.c0 = 0;
+  e.RR = rows;
+  e.CC = cols;
+  e.dm = mask_pixel;
+  // planar per-wavelength multipliers: M - 1 (Babinet) or M
+  const size_t plane = (size_t)rows * cols;
+  auto planes = [&](const float* re, const float* im, bool ones) {
+    std::vector<float> d((size_t)L * 2 * plane);
+    for (int l = 0; l < L; ++l) {
+      const size_t src = (size_t)(n_mask == 1 ? 0 : l) * plane;
+      for (size_t p = 0; p < plane; ++p) {
+        const float mr = ones ? 1.f : re[src + p], mi = ones || !im ? 0.f : im[src + p];
+        d[(size_t)l * 2 * plane + p] = e.bab ? mr - 1.f : mr;
+        d[(size_t)l * 2 * plane + plane + p] = mi;
+      }
+    }
+    return d;
+  };
+  std::vector<float> d = planes(mask_re, mask_im, false);
+  e.dmask = dev_copy(d.data(), d.size(), st);
+  CSG_CHECK(e.dmask, CSG_E_NOMEM, "csg_chain_add_fpm_mask: allocation failed");
+  // the calibration mask, unless it leaves the field as it is (ones with Babinet)
+  if (disable_for_calibration && (calib_re || !e.bab)) {
+    std::vector<float> cd = planes(calib_re, calib_im, calib_re == nullptr);
+    e.cmask = dev_copy(cd.data(), cd.size(), st);
+    CSG_CHECK(e.cmask, CSG_E_NOMEM, "csg_chain_add_fpm_mask: allocation failed");
+  }
+  std::vector<double> lfv(lf, lf + L), pref1(2 * L, 0.0), pref2(2 * L, 0.0);
+  for (int l = 0; l < L; ++l) {
+    pref1[2 * l] = 1.0;
+    pref2[2 * l] = zoom_fft_sign * mask_pixel * mask_pixel * c->dx * c->dx /
+                   (f_ratio_sign * lf[l] * lf[l]);
+  }
+  std::vector<double> xp = pixel_centres(n, c->dx), yr = pixel_centres(rows, mask_pixel),
+                      xc = pixel_centres(cols, mask_pixel);
+  int rc = csg_mft_create(c->ctx, &e.mft1, n, n, rows, cols, xp.data(), xp.data(), yr.data(),
+                          xc.data(), L, lfv.data(), pref1.data(), +1.0, c->precision);
+  if (rc) {
+    cudaFree(e.dmask);
+    cudaFree(e.cmask);
+    return rc;
+  }
+  e.lf = lfv;
+  e.pref = pref2;
   c->elems.push_back(e);
   c->planned = false;
   drop_graph(c);
@@ -730,6 +805,19 @@ static int build_plans(csg_chain* c) {
       e.win = MftWindow{w.r0, w.c0, n, n};  // output window of the n x n field
       e.win_rows = w.rows;
       e.win_cols = w.pitch;
+    } else if (e.kind == E_FPM_MASK) {
+      int j = i + 1;
+      while (j < ne && is_pointwise(c->elems[j].kind)) ++j;
+      MftWindow w = (j < ne && c->elems[j].kind == E_FRAUNHOFER) ? stop_window(c, i, j)
+                                                                 : MftWindow{0, 0, n, n};
+      std::vector<double> yr = pixel_centres(e.RR, e.dm), xc = pixel_centres(e.CC, e.dm);
+      csg_mft_destroy(e.mft2);
+      e.mft2 = nullptr;
+      int rc = csg_mft_create(c->ctx, &e.mft2, e.RR, e.CC, w.rows, w.pitch, yr.data(), xc.data(),
+                              xps.data() + w.r0, xps.data() + w.c0, L, e.lf.data(),
+                              e.pref.data(), -1.0, c->precision);
+      if (rc) return rc;
+      e.win = MftWindow{w.r0, w.c0, n, n};  // output window of the n x n field
     } else if (e.kind == E_FFT_FPM && e.bab == 1) {
       int j = i + 1;
       while (j < ne && is_pointwise(c->elems[j].kind)) ++j;
@@ -880,6 +968,11 @@ static int prepare(csg_chain* c) {
       int rc = csg_mft_reserve(e.mft1, c->n_fields);
       if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
       if (rc) return rc;
+    } else if (e.kind == E_FPM_MASK) {
+      fpm_need = std::max(fpm_need, F * 2 * (size_t)e.RR * e.CC * sizeof(float));
+      int rc = csg_mft_reserve(e.mft1, c->n_fields);
+      if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
+      if (rc) return rc;
     } else if (e.kind == E_FPM_HEX_DOUBLE) {
       fpm_need = std::max(fpm_need, F * 2 * (size_t)e.S * e.S * sizeof(float));
       ph_need = std::max(ph_need, F * (e.n_hex + 1) * sizeof(float2));
@@ -915,6 +1008,7 @@ struct Step {
   PixOps pro, epi;
   const Elem* e = nullptr;
   int sup0 = 0, sup1 = 1 << 30;  // FRESNEL: rows that can be nonzero on input
+  bool calib = false;            // FPM with a fixed mask: apply its calibration mask
   // FRESNEL followed by a hex FPM: the last row pass also writes the FPM's
   // forward-transform operand split (split_to), and the FPM skips its split
   csg_mft* split_to = nullptr;
@@ -945,7 +1039,9 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
   const size_t ne = c->elems.size();
   for (size_t ei = 0; ei < ne; ++ei) {
     const Elem& e = c->elems[ei];
-    if (calibrating && e.disable_for_calibration) continue;
+    // disabled for calibration: skipped, or a fixed-mask FPM's calibration mask
+    const bool calib_mask = calibrating && e.disable_for_calibration && e.kind == E_FPM_MASK;
+    if (calibrating && e.disable_for_calibration && !(calib_mask && e.cmask)) continue;
     int kind = 0;
     float param = 0.f;
     const float* a = e.a;
@@ -992,6 +1088,13 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
       if (pend.n) prog.push_back(Step{Step::PIX, pend, PixOps(), nullptr});
       pend = PixOps();
       prog.push_back(Step{Step::FPM, PixOps(), PixOps(), &e});
+      epi_open = false;
+    } else if (e.kind == E_FPM_MASK) {
+      if (pend.n) prog.push_back(Step{Step::PIX, pend, PixOps(), nullptr});
+      pend = PixOps();
+      Step s{Step::FPM, PixOps(), PixOps(), &e};
+      s.calib = calib_mask;
+      prog.push_back(s);
       epi_open = false;
     } else if (e.kind == E_FPM_HEX_DOUBLE) {
       prog.push_back(Step{Step::FPM_DOUBLE, pend, PixOps(), &e});  // ops ride in its split
@@ -1052,6 +1155,15 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
       }
       case Step::FPM: {
         const Elem& e = *s.e;
+        if (e.kind == E_FPM_MASK) {
+          rc = mft_execute_ops(ctx, e.mft1, c->field, c->fpm, F, c->slot, 0, nullptr, nullptr,
+                               PixOps(), fi, nullptr, nullptr, nullptr, s.presplit);
+          if (!rc)
+            rc = mft_execute_ops(ctx, e.mft2, c->fpm, c->field, F, c->slot, e.bab,
+                                 s.calib ? e.cmask : e.dmask, c->slot, PixOps(), fi, nullptr,
+                                 &e.win);
+          break;
+        }
         CSG_CHECK(c->sags && c->sag_hex == e.n_hex, CSG_E_STATE,
                   "hex FPM: candidate sags not set (csg_chain_sags) or wrong hex count");
         // (fliplr(M) - 1) for each field's (candidate, wavelength) on the box
@@ -1271,7 +1383,8 @@ int csg_chain_response(csg_chain* c, int fpm_index, const int* pix_idx, int n_pi
   std::vector<Step> prog = plan_walk(c, 0);
   int fi_step = -1, k = 0;
   for (size_t i = 0; i < prog.size(); ++i)
-    if (prog[i].kind == Step::FPM && k++ == fpm_index) fi_step = (int)i;
+    if (prog[i].kind == Step::FPM && prog[i].e->kind == E_FPM_HEX && k++ == fpm_index)
+      fi_step = (int)i;
   CSG_CHECK(fi_step >= 0, CSG_E_ARG, "csg_chain_response: no such hex FPM element");
   for (size_t i = fi_step + 1; i < prog.size(); ++i)
     CSG_CHECK(prog[i].kind == Step::PIX || prog[i].kind == Step::FINAL, CSG_E_STATE,

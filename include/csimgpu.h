@@ -252,6 +252,24 @@ int csg_chain_add_fresnel(csg_chain* chain, double z, double ap_rad);
 /* complexMask (complexMask.cpp:24-66): centred amp exp(-i ph), host fp32. */
 int csg_chain_add_complex_mask(csg_chain* chain, const float* amp, const float* ph, int mrows,
                                int mcols, int disable_for_calibration);
+/* fpmPupToLyot with a fixed focal-plane mask: the fpmCMCForPupToLyot
+ * (fpmPupToLyot.cpp:303-367) and fpmBinaryForPupToLyot (:521-557) adapters,
+ * in the same matrix-Fourier form as csg_chain_add_fpm_hex:
+ *   babinet != 0:  E <- E + c MFT2[(M - 1) MFT1[E]]   (CMC with doBabinet)
+ *   babinet == 0:  E <- c MFT2[M MFT1[E]]             (binary, CMC without)
+ * mask_re / mask_im (host, mask_im may be null): [n_mask][rows][cols] with
+ * n_mask 1 or n_lambda, pixel mask_pixel (maskGeom.set_xy(mask, pixel)),
+ * rows and cols multiples of 8; lf: the lambdaFocalLength of each wavelength
+ * (fRatioSign lambda focalRatio 2 beamRadius for the CMC, fRatioSign lambda
+ * primaryfLength for the binary mask); c = zoomFftSign mask_pixel^2 dx^2 /
+ * (fRatioSign lf^2). calib_re / calib_im (may be null: a mask of ones, the
+ * CMC's fpmMatAmpCalib): the mask the calibration walk applies when
+ * disable_for_calibration is set (the binary adapter's calibMat). */
+int csg_chain_add_fpm_mask(csg_chain* chain, const float* mask_re, const float* mask_im,
+                           int n_mask, int rows, int cols, double mask_pixel, const double* lf,
+                           double f_ratio_sign, double zoom_fft_sign, int babinet,
+                           const float* calib_re, const float* calib_im,
+                           int disable_for_calibration);
 /* doubleFraunhoferInterpFPM with complexHexMaskFPM
  * (doubleFraunhoferInterpFPM.cpp:24-65, init_geom :86-121;
  * complexHexMaskFPM.cpp:25-42): zoom FFT of the field to a zoom grid of

@@ -283,3 +283,71 @@ def test_double_fraunhofer_hex_fpm_matches_oracle(ctx):
           f"(of the calibration peak)")
     assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
     cor.close()
+
+
+@pytest.mark.parametrize("babinet", [True, False])
+def test_fixed_mask_fpm_matches_reference_algorithm(ctx, babinet):
+    """fpmPupToLyot with a fixed mask (the CMC adapter with doBabinet, the
+    binary adapter without, with its calibration mask) on a rectangular
+    mask grid, against the oracle running the reference's own 2N FFT
+    convolution: fields within 1e-6 of the calibration peak."""
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import workloads as W
+    from oracle import csim_fft as of
+    spec = small_spec(wavelengths=(640e-9, 660e-9))
+    sources = [cg.PointSource(1.0, 0.0, 0.0), cg.PointSource(0.5, 0.02, -0.01)]
+    a = W.piaacmc_arrays(spec, sources)
+    rows, cols, dm = 64, 48, a["dm"]
+    rng = np.random.default_rng(17)
+    yy, xx = np.mgrid[0:rows, 0:cols]
+    r = np.hypot(yy - rows / 2 + 0.5, xx - cols / 2 + 0.5)
+    if babinet:  # complex mask amp exp(-i ph)
+        mask = (0.6 + 0.4 * rng.random((rows, cols))) * np.exp(-1j * rng.uniform(-2, 2, (rows, cols)))
+        calib = None
+    else:  # binary occulter and its calibration mask
+        mask = (r > 8.0).astype(np.complex128)
+        calib = np.ones((rows, cols), np.complex128)
+    ef, tel = a["ef"], a["tel"]
+    lfl = np.array([-1.0 * lam * spec.fpm_focal_ratio * 2 * ef.beamRadiusPhysical
+                    for lam in a["lam"]])
+    elems = [cg.Mask(a["pupil"]), cg.Mirror(a["sag1"], 1.0),
+             cg.FpmPupToLyotMask(mask, dm, lfl, -1.0, -1.0, babinet, calib),
+             cg.Mask(a["lyot"]), cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov)]
+    cor = cg.Coronagraph(ctx, tel, ef, elems, 6, True)
+    F = cor.batch_all(1)
+    img = cor.execute(calibrating=False).clone()
+    cal = cor.execute(calibrating=True).clone()
+    ctx.sync()
+    got = img[:, 0].double().cpu().numpy() + 1j * img[:, 1].double().cpu().numpy()
+    gcal = cal[:, 0].double().cpu().numpy() + 1j * cal[:, 1].double().cpu().numpy()
+    li, amp, tip, tilt, _ = cor._batch
+    n, dx = spec.n, a["dx"]
+    geom = of.ArrayGeom.set_xy(n, n, dx)
+    mgeom = of.ArrayGeom.set_xy(cols, rows, dm)
+    n_out = int(np.ceil(spec.n_out_fov * spec.spl))
+    gout = of.ArrayGeom.set_xy(n_out, n_out, a["lod_image"] / spec.spl)
+    peak, e_img, e_cal = 0.0, 0.0, 0.0
+    for f in range(F):
+        lam = float(a["lam"][li[f]])
+        e = oe.point_source_field(geom, 1, amp[f] * amp[f], tip[f], tilt[f])
+        e = oe.mask_apply(e, a["pupil"])
+        e = oe.mirror_apply(e, a["sag1"].astype(np.float64), [lam], 1.0)
+        outs = []
+        for m in (mask, calib):
+            if m is None:
+                x = e
+            else:
+                mm = (m - 1.0) if babinet else m
+                x = oe.pup_to_lyot_conv(e, [lam], geom, mgeom, mm[None], lfl[li[f]:li[f] + 1],
+                                        -1.0, -1.0, babinet=babinet)
+            x = oe.mask_apply(x, a["lyot"])
+            outs.append(oe.fraunhofer_focal(x, geom, gout, [lam], ef.beamRadiusPhysical,
+                                            tel.primaryfRatio)[0])
+        peak = max(peak, np.abs(outs[1]).max())
+        e_img = max(e_img, np.abs(got[f] - outs[0]).max())
+        e_cal = max(e_cal, np.abs(gcal[f] - outs[1]).max())
+    e_img, e_cal = e_img / peak, e_cal / peak
+    print(f"\nfixed-mask fpmPupToLyot babinet={babinet}: calibration field {e_cal:.3e}, final "
+          f"field {e_img:.3e} (of the calibration peak)")
+    assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
+    cor.close()
