@@ -72,6 +72,19 @@ class FpmPupToLyotMask:
 
 
 @dataclass
+class DoubleFraunhoferFPM:
+    """doubleFraunhoferFPM: zoom FFT to a padFactor N grid whose pixel is
+    2 (beamRadius / (pixelScale N zoomFactor)) lambda 80 for each wavelength,
+    the fixed complex mask on its centred block, zoom FFT back (lambda f =
+    +-3.52 lambda)."""
+    mask: np.ndarray
+    zoomFactor: float
+    padFactor: float = 2.0
+    disableForCalibration: bool = True
+    lambdaFocalFactor: float = 3.52  # doubleFraunhoferFPM.cpp:44-45
+
+
+@dataclass
 class DoubleFraunhoferInterpFPM:
     """doubleFraunhoferInterpFPM with its complexHexMaskFPM: zoom FFT of the
     field to a padFactor N grid of pixel fpmScale (metres) at lambda f =
@@ -211,6 +224,17 @@ class Coronagraph:
             call("csg_chain_add_fpm_mask", self.h, ptr(re), ptr(im), m.shape[0], m.shape[1],
                  m.shape[2], e.pixelScale, ptr(lf), e.fRatioSign, e.zoomFftSign,
                  int(e.doBabinet), ptr(cre), ptr(cim), int(e.disableForCalibration))
+        elif isinstance(e, DoubleFraunhoferFPM):
+            m = np.asarray(e.mask)
+            re, im = _f32(m.real), _f32(m.imag)
+            ef = self.ef
+            zpx = np.ascontiguousarray(
+                [2 * (ef.beamRadiusPhysical / (ef.pixelScale * ef.n * e.zoomFactor)) * lam * 80
+                 for lam in ef.wavelengths], np.float64)
+            call("csg_chain_add_fpm_double_mask", self.h, re.ctypes.data_as(C.c_void_p),
+                 im.ctypes.data_as(C.c_void_p), m.shape[0], m.shape[1],
+                 zpx.ctypes.data_as(C.c_void_p), e.padFactor, e.lambdaFocalFactor,
+                 int(e.disableForCalibration))
         elif isinstance(e, DoubleFraunhoferInterpFPM):
             ids = np.ascontiguousarray(e.hex_id, np.int16)
             cnt = np.ascontiguousarray(e.count, np.uint16)

@@ -93,11 +93,12 @@ struct Elem {
   double phase_sign = 1.0;
   csg_mft* mft1 = nullptr;
   csg_mft* mft2 = nullptr;
-  // double-Fraunhofer hex FPM: mft1 field -> zoom grid, mft2 zoom grid ->
-  // field, mft3 the mask block of the zoom grid -> field; nz x nz zoom grid
-  // with the S x S block at (zr0, zr0)
+  // double-Fraunhofer FPM: mft1 field -> zoom grid, mft2 zoom grid -> field,
+  // mft3 the mask block of the zoom grid -> field; nz x nz zoom grid with the
+  // RR x CC block at (zr0, zc0); the mask is the hex mask (hex_id set) or
+  // the fixed dmask (M - 1 per wavelength slot)
   csg_mft* mft3 = nullptr;
-  int nz = 0, zr0 = 0;
+  int nz = 0, zr0 = 0, zc0 = 0;
   // fraunhofer
   csg_mft* mft = nullptr;
   int n_out = 0;
@@ -518,22 +519,68 @@ int csg_chain_add_fpm_mask(csg_chain* c, const float* mask_re, const float* mask
   return CSG_OK;
 }
 
-// doubleFraunhoferInterpFPM (doubleFraunhoferInterpFPM.cpp:24-65, geometry
-// :86-121) with its complexHexMaskFPM (complexHexMaskFPM.cpp:25-42): the
-// mask multiplies the centred S x S block of the zoom grid and leaves the
-// rest, so E_out = MFT_out[Z] + MFT_out restricted to the block[(M - 1) Z].
+// The double-Fraunhofer elements (doubleFraunhoferInterpFPM.cpp:24-65 with
+// geometry :86-121 and complexHexMaskFPM.cpp:25-42; doubleFraunhoferFPM.cpp:
+// 23-110): zoom FFT to an nz x nz grid of pixel zpx[l] at lambda f =
+// lf_factor lambda, a mask on the centred rows x cols block (the rest of the
+// grid left as it is), zoom FFT back at -lf_factor lambda. So E_out =
+// MFT_out[Z] + MFT_out restricted to the block[(M - 1) Z]. The zoom grid's
+// coordinates (i - nz/2) zpx[l] enter the phases as integers over
+// lambda f / zpx[l], so one plan serves every wavelength's pixel size.
+static int add_double_fraunhofer(csg_chain* c, Elem& e, int rows, int cols, const double* zpx,
+                                 double pad_factor, double lf_factor) {
+  const int n = c->n, L = c->n_lambda;
+  const int nz = (int)(pad_factor * n);  // int nRows = padFactor * nRowsE
+  CSG_CHECK(rows >= 8 && cols >= 8 && rows % 8 == 0 && cols % 8 == 0 && nz % 8 == 0 &&
+                nz >= rows && nz >= cols && lf_factor != 0.0,
+            CSG_E_SHAPE,
+            "double-Fraunhofer FPM: mask sides and pad_factor N must be multiples of 8, "
+            "pad_factor N at least the mask");
+  for (int l = 0; l < L; ++l)
+    CSG_CHECK(zpx[l] > 0.0, CSG_E_ARG, "double-Fraunhofer FPM: zoom pixel must be positive");
+  e.nz = nz;
+  e.zr0 = nz / 2 - rows / 2;  // tcMat.n_rows / 2 - mask.n_rows / 2
+  e.zc0 = nz / 2 - cols / 2;
+  e.r0 = e.c0 = 0;
+  e.RR = rows;
+  e.CC = cols;
+  std::vector<double> zi(nz), xp = pixel_centres(n, c->dx);
+  for (int i = 0; i < nz; ++i) zi[i] = (double)i - (double)nz / 2.0;
+  std::vector<double> lf_in(L), lf_out(L), pin(2 * L), pout(2 * L);
+  for (int l = 0; l < L; ++l) {
+    const double lf = lf_factor * c->lambda[l];
+    lf_in[l] = lf / zpx[l];
+    lf_out[l] = -lf / zpx[l];
+    // zoomFft prefactor dx_in dy_in / (i lambda f) (csim_fft.cpp:794-801)
+    pin[2 * l] = 0.0;
+    pin[2 * l + 1] = -c->dx * c->dx / lf;
+    pout[2 * l] = 0.0;
+    pout[2 * l + 1] = zpx[l] * zpx[l] / lf;
+  }
+  int rc = csg_mft_create(c->ctx, &e.mft1, n, n, nz, nz, xp.data(), xp.data(), zi.data(),
+                          zi.data(), L, lf_in.data(), pin.data(), -1.0, c->precision);
+  if (!rc)
+    rc = csg_mft_create(c->ctx, &e.mft2, nz, nz, n, n, zi.data(), zi.data(), xp.data(), xp.data(),
+                        L, lf_out.data(), pout.data(), -1.0, c->precision);
+  if (!rc)
+    rc = csg_mft_create(c->ctx, &e.mft3, rows, cols, n, n, zi.data() + e.zr0, zi.data() + e.zc0,
+                        xp.data(), xp.data(), L, lf_out.data(), pout.data(), -1.0, c->precision);
+  if (rc) {
+    csg_mft_destroy(e.mft1);
+    csg_mft_destroy(e.mft2);
+    csg_mft_destroy(e.mft3);
+    return rc;
+  }
+  return CSG_OK;
+}
+
 int csg_chain_add_fpm_hex_double(csg_chain* c, const int16_t* hex_id, const uint16_t* count,
                                  int S, int n_sub, int n_hex, double fpm_scale, double pad_factor,
                                  double lf_factor, double phase_sign,
                                  int disable_for_calibration) {
   CSG_CHECK(c && hex_id && count, CSG_E_ARG, "csg_chain_add_fpm_hex_double: null argument");
-  const int n = c->n, L = c->n_lambda;
-  const int nz = (int)(pad_factor * n);  // int nRows = padFactor * nRowsE
-  CSG_CHECK(S >= 8 && S % 8 == 0 && n_sub > 0 && n_hex > 0 && nz % 8 == 0 && nz >= S &&
-                fpm_scale > 0.0 && lf_factor != 0.0,
-            CSG_E_SHAPE,
-            "csg_chain_add_fpm_hex_double: S and pad_factor N must be multiples of 8, "
-            "pad_factor N >= S");
+  CSG_CHECK(S >= 8 && S % 8 == 0 && n_sub > 0 && n_hex > 0 && fpm_scale > 0.0, CSG_E_SHAPE,
+            "csg_chain_add_fpm_hex_double: bad mask size, sub-pixel count or scale");
   DeviceGuard g(c->ctx->device);
   cudaStream_t st = c->ctx->stream;
   Elem e;
@@ -543,41 +590,50 @@ int csg_chain_add_fpm_hex_double(csg_chain* c, const int16_t* hex_id, const uint
   e.n_hex = n_hex;
   e.phase_sign = phase_sign;
   e.disable_for_calibration = disable_for_calibration;
-  e.nz = nz;
-  e.zr0 = nz / 2 - S / 2;  // tcMat.n_rows / 2 - complexIntMask.n_rows / 2
-  e.r0 = e.c0 = 0;
-  e.RR = e.CC = S;
+  std::vector<double> zpx(c->n_lambda, fpm_scale);  // the hex mask's fpmScale
+  int rc = add_double_fraunhofer(c, e, S, S, zpx.data(), pad_factor, lf_factor);
+  if (rc) return rc;
   e.hex_id = dev_copy(hex_id, (size_t)3 * S * S, st);
   e.count = dev_copy(count, (size_t)3 * S * S, st);
-  CSG_CHECK(e.hex_id && e.count, CSG_E_NOMEM, "csg_chain_add_fpm_hex_double: allocation failed");
-  // zoom grid (i - n/2) fpm_scale; field pixel centres
-  std::vector<double> xz(nz), xp = pixel_centres(n, c->dx);
-  for (int i = 0; i < nz; ++i) xz[i] = ((double)i - (double)nz / 2.0) * fpm_scale;
-  std::vector<double> lf_in(L), lf_out(L), pin(2 * L), pout(2 * L);
-  for (int l = 0; l < L; ++l) {
-    lf_in[l] = lf_factor * c->lambda[l];
-    lf_out[l] = -lf_in[l];
-    // zoomFft prefactor dx_in dy_in / (i lambda f) (csim_fft.cpp:794-801)
-    pin[2 * l] = 0.0;
-    pin[2 * l + 1] = -c->dx * c->dx / lf_in[l];
-    pout[2 * l] = 0.0;
-    pout[2 * l + 1] = -fpm_scale * fpm_scale / lf_out[l];
-  }
-  int rc = csg_mft_create(c->ctx, &e.mft1, n, n, nz, nz, xp.data(), xp.data(), xz.data(),
-                          xz.data(), L, lf_in.data(), pin.data(), -1.0, c->precision);
-  if (!rc)
-    rc = csg_mft_create(c->ctx, &e.mft2, nz, nz, n, n, xz.data(), xz.data(), xp.data(), xp.data(),
-                        L, lf_out.data(), pout.data(), -1.0, c->precision);
-  if (!rc)
-    rc = csg_mft_create(c->ctx, &e.mft3, S, S, n, n, xz.data() + e.zr0, xz.data() + e.zr0,
-                        xp.data(), xp.data(), L, lf_out.data(), pout.data(), -1.0, c->precision);
-  if (rc) {
+  if (!e.hex_id || !e.count) {
+    cudaFree(e.hex_id);
+    cudaFree(e.count);
     csg_mft_destroy(e.mft1);
     csg_mft_destroy(e.mft2);
     csg_mft_destroy(e.mft3);
-    cudaFree(e.hex_id);
-    cudaFree(e.count);
-    return rc;
+    CSG_CHECK(false, CSG_E_NOMEM, "csg_chain_add_fpm_hex_double: allocation failed");
+  }
+  c->elems.push_back(e);
+  c->planned = false;
+  drop_graph(c);
+  return CSG_OK;
+}
+
+int csg_chain_add_fpm_double_mask(csg_chain* c, const float* mask_re, const float* mask_im,
+                                  int rows, int cols, const double* zoom_pixel, double pad_factor,
+                                  double lf_factor, int disable_for_calibration) {
+  CSG_CHECK(c && mask_re && zoom_pixel, CSG_E_ARG, "csg_chain_add_fpm_double_mask: null argument");
+  DeviceGuard g(c->ctx->device);
+  Elem e;
+  e.kind = E_FPM_HEX_DOUBLE;  // the same walk step, with a fixed mask
+  e.disable_for_calibration = disable_for_calibration;
+  int rc = add_double_fraunhofer(c, e, rows, cols, zoom_pixel, pad_factor, lf_factor);
+  if (rc) return rc;
+  // M - 1 per wavelength slot (one mask for every wavelength)
+  const int L = c->n_lambda;
+  const size_t plane = (size_t)rows * cols;
+  std::vector<float> d((size_t)L * 2 * plane);
+  for (int l = 0; l < L; ++l)
+    for (size_t p = 0; p < plane; ++p) {
+      d[(size_t)l * 2 * plane + p] = mask_re[p] - 1.f;
+      d[(size_t)l * 2 * plane + plane + p] = mask_im ? mask_im[p] : 0.f;
+    }
+  e.dmask = dev_copy(d.data(), d.size(), c->ctx->stream);
+  if (!e.dmask) {
+    csg_mft_destroy(e.mft1);
+    csg_mft_destroy(e.mft2);
+    csg_mft_destroy(e.mft3);
+    CSG_CHECK(false, CSG_E_NOMEM, "csg_chain_add_fpm_double_mask: allocation failed");
   }
   c->elems.push_back(e);
   c->planned = false;
@@ -974,7 +1030,7 @@ static int prepare(csg_chain* c) {
       if (!rc) rc = csg_mft_reserve(e.mft2, c->n_fields);
       if (rc) return rc;
     } else if (e.kind == E_FPM_HEX_DOUBLE) {
-      fpm_need = std::max(fpm_need, F * 2 * (size_t)e.S * e.S * sizeof(float));
+      fpm_need = std::max(fpm_need, F * 2 * (size_t)e.RR * e.CC * sizeof(float));
       ph_need = std::max(ph_need, F * (e.n_hex + 1) * sizeof(float2));
       pad_need = std::max(pad_need, F * 2 * (size_t)e.nz * e.nz * sizeof(float));  // zoom grid
       int rc = csg_mft_reserve(e.mft1, c->n_fields);
@@ -1184,12 +1240,15 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         break;
       case Step::FPM_DOUBLE: {
         const Elem& e = *s.e;
-        CSG_CHECK(c->sags && c->sag_hex == e.n_hex, CSG_E_STATE,
-                  "hex FPM: candidate sags not set (csg_chain_sags) or wrong hex count");
-        // M - 1 (no flip) for each field's (candidate, wavelength)
-        rc = hex_mask_region(ctx, e.hex_id, e.count, e.S, 0, 0, e.S, e.S, e.n_sub, c->sags,
-                             e.n_hex, F, c->cand, c->lam_f, e.phase_sign, 0, 1.0, c->fpm_mask,
-                             c->phasors);
+        const bool hex = e.hex_id != nullptr;
+        if (hex) {
+          CSG_CHECK(c->sags && c->sag_hex == e.n_hex, CSG_E_STATE,
+                    "hex FPM: candidate sags not set (csg_chain_sags) or wrong hex count");
+          // M - 1 (no flip) for each field's (candidate, wavelength)
+          rc = hex_mask_region(ctx, e.hex_id, e.count, e.S, 0, 0, e.S, e.S, e.n_sub, c->sags,
+                               e.n_hex, F, c->cand, c->lam_f, e.phase_sign, 0, 1.0, c->fpm_mask,
+                               c->phasors);
+        }
         // Z = zoom grid field (the element ops ride in the split)
         if (!rc)
           rc = mft_execute_ops(ctx, e.mft1, c->field, c->padbuf, F, c->slot, 0, nullptr, nullptr,
@@ -1198,10 +1257,11 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         if (!rc)
           rc = mft_execute_ops(ctx, e.mft2, c->padbuf, c->field, F, c->slot, 0, nullptr, nullptr,
                                PixOps(), fi);
-        const MftWindow blk{e.zr0, e.zr0, e.nz, e.nz};
+        const MftWindow blk{e.zr0, e.zc0, e.nz, e.nz};
         if (!rc)
-          rc = mft_execute_ops(ctx, e.mft3, c->padbuf, c->field, F, c->slot, 1, c->fpm_mask,
-                               c->ident, PixOps(), fi, &blk, nullptr);
+          rc = mft_execute_ops(ctx, e.mft3, c->padbuf, c->field, F, c->slot, 1,
+                               hex ? c->fpm_mask : e.dmask, hex ? c->ident : c->slot, PixOps(),
+                               fi, &blk, nullptr);
         break;
       }
       case Step::FFT_FPM: {

@@ -252,6 +252,15 @@ int csg_chain_add_fresnel(csg_chain* chain, double z, double ap_rad);
 /* complexMask (complexMask.cpp:24-66): centred amp exp(-i ph), host fp32. */
 int csg_chain_add_complex_mask(csg_chain* chain, const float* amp, const float* ph, int mrows,
                                int mcols, int disable_for_calibration);
+/* doubleFraunhoferFPM (doubleFraunhoferFPM.cpp:23-110): as
+ * csg_chain_add_fpm_hex_double with a fixed complex mask (host fp32,
+ * rows x cols, multiples of 8; mask_im may be null) on the centred block and
+ * a zoom-grid pixel per wavelength, zoom_pixel[l] (the reference's dxprime =
+ * 2 (beamRadius / (pixelScale N zoomFactor)) lambda 80). */
+int csg_chain_add_fpm_double_mask(csg_chain* chain, const float* mask_re, const float* mask_im,
+                                  int rows, int cols, const double* zoom_pixel,
+                                  double pad_factor, double lf_factor,
+                                  int disable_for_calibration);
 /* fpmPupToLyot with a fixed focal-plane mask: the fpmCMCForPupToLyot
  * (fpmPupToLyot.cpp:303-367) and fpmBinaryForPupToLyot (:521-557) adapters,
  * in the same matrix-Fourier form as csg_chain_add_fpm_hex:

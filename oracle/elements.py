@@ -224,13 +224,15 @@ def double_fraunhofer_interp_fpm(cube, lambdas, egeom: ArrayGeom, fpm_scale: flo
     at lambda f = 3.52 lambda; the S x S mask multiplies the block starting at
     (nz/2 - S/2, nz/2 - S/2), the rest of the grid is left as it is; zoomFft
     back to E's geometry at -3.52 lambda. masks[sl] is the complex
-    interpolated mask of slice sl (complex_interpolated_mask, no flip)."""
+    interpolated mask of slice sl (complex_interpolated_mask, no flip);
+    fpm_scale is one zoom pixel or one per slice."""
     cube = np.asarray(cube, dtype=np.complex128)
     n = cube.shape[-1]
     nz = int(pad_factor * n)
-    zg = ArrayGeom.set_xy_offset_m1(nz, nz, fpm_scale)
+    scales = np.broadcast_to(np.asarray(fpm_scale, dtype=np.float64), (len(lambdas),))
     out = np.empty_like(cube)
     for sl, lam in enumerate(lambdas):
+        zg = ArrayGeom.set_xy_offset_m1(nz, nz, float(scales[sl]))
         lf_in = lf_factor * lam
         z = ZoomFft(egeom, zg, [lf_in]).mft(cube[sl], 0)
         m = np.asarray(masks[sl])
@@ -238,6 +240,18 @@ def double_fraunhofer_interp_fpm(cube, lambdas, egeom: ArrayGeom, fpm_scale: flo
         z[r0:r0 + m.shape[0], c0:c0 + m.shape[1]] *= m
         out[sl] = ZoomFft(zg, egeom, [-lf_in]).mft(z, 0)
     return out
+
+
+def double_fraunhofer_fpm(cube, lambdas, egeom: ArrayGeom, beam_radius: float,
+                          pixel_scale: float, zoom_factor: float, pad_factor: float, mask):
+    """doubleFraunhoferFPM::execute (doubleFraunhoferFPM.cpp:23-110): the
+    same walk as doubleFraunhoferInterpFPM with the zoom pixel
+    dxprime = 2 (beamRadius / (pixelScale N zoomFactor)) lambda 80 of each
+    slice and one fixed complex mask (slice maskIndex) on every slice."""
+    n = np.asarray(cube).shape[-2]
+    scales = [2 * (beam_radius / (pixel_scale * n * zoom_factor)) * lam * 80 for lam in lambdas]
+    return double_fraunhofer_interp_fpm(cube, lambdas, egeom, scales, pad_factor,
+                                        [mask] * len(lambdas))
 
 
 def hex_mask_pixel_scale(beam_radius: float, pixel_scale: float, mask_size: int,

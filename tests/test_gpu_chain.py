@@ -351,3 +351,55 @@ def test_fixed_mask_fpm_matches_reference_algorithm(ctx, babinet):
           f"field {e_img:.3e} (of the calibration peak)")
     assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
     cor.close()
+
+
+def test_double_fraunhofer_fixed_mask_matches_oracle(ctx):
+    """doubleFraunhoferFPM: a fixed rectangular complex mask on the centred
+    block of a zoom grid whose pixel scales with each wavelength, two
+    wavelengths, against the oracle: fields within 1e-6 of the calibration
+    peak."""
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import workloads as W
+    from oracle import csim_fft as of
+    spec = small_spec(wavelengths=(620e-9, 680e-9))
+    a = W.piaacmc_arrays(spec, [cg.PointSource(1.0, 0.0, 0.0), cg.PointSource(0.5, 0.02, 0.0)])
+    ef, tel = a["ef"], a["tel"]
+    n, dx = spec.n, a["dx"]
+    rows, cols = 64, 48
+    rng = np.random.default_rng(19)
+    mask = (0.5 + 0.5 * rng.random((rows, cols))) * np.exp(1j * rng.uniform(-2, 2, (rows, cols)))
+    # zoom pixel about half the FFT sampling at 650 nm
+    zf = 2 * ef.beamRadiusPhysical / (ef.pixelScale * n) * 80 * n * dx / (3.52 * 0.5)
+    elems = [cg.Mask(a["pupil"]), cg.Mirror(a["sag1"], 1.0), cg.DoubleFraunhoferFPM(mask, zf, 2.0),
+             cg.Mask(a["lyot"]), cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov)]
+    cor = cg.Coronagraph(ctx, tel, ef, elems, 6, True)
+    F = cor.batch_all(1)
+    img = cor.execute(calibrating=False).clone()
+    cal = cor.execute(calibrating=True).clone()
+    ctx.sync()
+    got = img[:, 0].double().cpu().numpy() + 1j * img[:, 1].double().cpu().numpy()
+    gcal = cal[:, 0].double().cpu().numpy() + 1j * cal[:, 1].double().cpu().numpy()
+    li, amp, tip, tilt, _ = cor._batch
+    geom = of.ArrayGeom.set_xy(n, n, dx)
+    n_out = int(np.ceil(spec.n_out_fov * spec.spl))
+    gout = of.ArrayGeom.set_xy(n_out, n_out, a["lod_image"] / spec.spl)
+    peak, e_img, e_cal = 0.0, 0.0, 0.0
+    for f in range(F):
+        lam = float(a["lam"][li[f]])
+        e = oe.point_source_field(geom, 1, amp[f] * amp[f], tip[f], tilt[f])
+        e = oe.mask_apply(e, a["pupil"])
+        e = oe.mirror_apply(e, a["sag1"].astype(np.float64), [lam], 1.0)
+        outs = []
+        for x in (oe.double_fraunhofer_fpm(e, [lam], geom, ef.beamRadiusPhysical, ef.pixelScale,
+                                           zf, 2.0, mask), e):
+            x = oe.mask_apply(x, a["lyot"])
+            outs.append(oe.fraunhofer_focal(x, geom, gout, [lam], ef.beamRadiusPhysical,
+                                            tel.primaryfRatio)[0])
+        peak = max(peak, np.abs(outs[1]).max())
+        e_img = max(e_img, np.abs(got[f] - outs[0]).max())
+        e_cal = max(e_cal, np.abs(gcal[f] - outs[1]).max())
+    e_img, e_cal = e_img / peak, e_cal / peak
+    print(f"\ndoubleFraunhoferFPM fixed mask: calibration field {e_cal:.3e}, final field "
+          f"{e_img:.3e} (of the calibration peak)")
+    assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
+    cor.close()
