@@ -24,6 +24,7 @@ CSG_LAYOUT_COLMAJOR = 0
 CSG_LAYOUT_ROWMAJOR = 1
 CSG_PREC_BF16X6 = 6
 CSG_PREC_BF16X3 = 3
+CSG_PREC_HIGH = 16
 
 STATUS = {0: "CSG_OK", -1: "CSG_E_ARG", -2: "CSG_E_SHAPE", -3: "CSG_E_CUDA", -4: "CSG_E_TIMEOUT",
           -5: "CSG_E_NOMEM", -6: "CSG_E_NAN", -7: "CSG_E_STATE"}
@@ -63,9 +64,12 @@ SIGNATURES = {
     "csg_complex_mask": ([P, P, I, I, I, P, P, I, I], None),
     "csg_fft2d": ([P, P, I, I, I], None),
     "csg_fresnel": ([P, P, I, I, P, D, D], None),
+    "csg_fresnel_prec": ([P, P, I, I, P, D, D, I], None),
+    "csg_fft2d_prec": ([P, P, I, I, I, I], None),
     "csg_mft_create": ([P, C.POINTER(P), I, I, I, I, P, P, P, P, I, P, P, D, I], None),
     "csg_mft_destroy": ([P], None),
     "csg_mft_execute": ([P, P, P, P, I, P, I, P, P], None),
+    "csg_mft_execute_lo": ([P, P, P, P, P, I, P], None),
     "csg_mft_workspace_bytes": ([P, I], SZ),
     "csg_hex_mask": ([P, P, P, I, I, P, I, I, P, P, D, I, D, I, P], None),
     "csg_hex_mask_noalloc": ([P, P, P, I, I, P, I, I, P, P, D, I, D, I, P], None),

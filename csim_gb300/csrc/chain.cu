@@ -1176,7 +1176,7 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
       if (prog[i].kind == Step::FRESNEL && prog[i + 1].kind == Step::FPM) {
         int ny = 0, nx = 0;
         mft_input_shape(prog[i + 1].e->mft1, &ny, &nx);
-        if (ny == c->n && nx == c->n) {
+        if (ny == c->n && nx == c->n && !mft_is_high(prog[i + 1].e->mft1)) {
           prog[i].split_to = prog[i + 1].e->mft1;
           prog[i + 1].presplit = true;
         }

@@ -74,6 +74,69 @@ __device__ __forceinline__ void split3_pair(float x0, float x1, uint32_t& h0, ui
   h2 = *reinterpret_cast<const uint32_t*>(&c);
 }
 
+// Exponent-aligned three-way split (CSG_PREC_HIGH). All values of one
+// 64-wide K group of an operand row share the grid g = 2^(e - 8), where
+// 2^e bounds the group's largest magnitude: hi = rint(v / g) g is an integer
+// multiple of g with |hi / g| <= 256 (exact in bf16), and mid, lo are the
+// ordinary bf16 rounding of what is left (v - hi is exact in fp32). Every
+// hi x hi product of one K group then lies on the grid g_a g_b and a group's
+// sum (at most 64 * 2^16 grid units) is an integer below 2^24 units, so the
+// tensor core accumulates it without any rounding.
+struct Grid {
+  float g, inv;
+};
+// Grid of a group whose largest |value| has the fp32 bit pattern maxbits
+// (non-negative). Groups below 2^-100 use the grid of 2^-100.
+__device__ __forceinline__ Grid grid_of(uint32_t maxbits) {
+  int e = (int)(maxbits >> 23);  // biased exponent: max < 2^(e - 126)
+  e = e < 27 ? 27 : e;
+  Grid r;
+  r.g = __int_as_float((e - 7) << 23);     // 2^(e - 134)
+  r.inv = __int_as_float((261 - e) << 23);  // 2^(134 - e)
+  return r;
+}
+__device__ __forceinline__ uint32_t absbits(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+
+__device__ __forceinline__ void split3_aligned(float v, const Grid& gr, __nv_bfloat16& a,
+                                               __nv_bfloat16& b, __nv_bfloat16& c) {
+  const float h = rintf(v * gr.inv) * gr.g;
+  a = __float2bfloat16_rn(h);
+  const float r = v - h;
+  b = __float2bfloat16_rn(r);
+  c = __float2bfloat16_rn(r - __bfloat162float(b));
+}
+// The same for a two-float value v + w (|w| below half an ulp of v): the
+// low word joins the remainder.
+__device__ __forceinline__ void split3_aligned2(float v, float w, const Grid& gr,
+                                                __nv_bfloat16& a, __nv_bfloat16& b,
+                                                __nv_bfloat16& c) {
+  const float h = rintf(v * gr.inv) * gr.g;
+  a = __float2bfloat16_rn(h);
+  const float r = (v - h) + w;
+  b = __float2bfloat16_rn(r);
+  c = __float2bfloat16_rn(r - __bfloat162float(b));
+}
+// Two values on one grid, packed as split3_pair packs them.
+__device__ __forceinline__ void split3_aligned_pair(float x0, float x1, const Grid& gr,
+                                                    uint32_t& h0, uint32_t& h1, uint32_t& h2) {
+  const float a0 = rintf(x0 * gr.inv) * gr.g, a1 = rintf(x1 * gr.inv) * gr.g;
+  const __nv_bfloat162 a = __floats2bfloat162_rn(a0, a1);
+  const float r0 = x0 - a0, r1 = x1 - a1;
+  const __nv_bfloat162 b = __floats2bfloat162_rn(r0, r1);
+  const float2 fb = __bfloat1622float2(b);
+  const __nv_bfloat162 c = __floats2bfloat162_rn(r0 - fb.x, r1 - fb.y);
+  h0 = *reinterpret_cast<const uint32_t*>(&a);
+  h1 = *reinterpret_cast<const uint32_t*>(&b);
+  h2 = *reinterpret_cast<const uint32_t*>(&c);
+}
+
+// Error-free sum: s + e = a + b exactly (Knuth's TwoSum, no ordering needed).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
 inline int grid_for(long long n, int block, int cap = 152 * 32) {
   long long g = (n + block - 1) / block;
   if (g > cap) g = cap;

@@ -21,8 +21,11 @@
 // generated in-kernel from the integer frequency index.
 #include <map>
 #include <mutex>
+#include <type_traits>
+#include <vector>
 
 #include "ctx.hpp"
+#include "dfloat.cuh"
 #include "pixops.cuh"
 
 namespace csg {
@@ -34,6 +37,34 @@ __global__ void k_twiddles(float2* tw, int n) {
     sincospi(2.0 * (double)m / (double)n, &s, &c);
     tw[m] = make_float2((float)c, (float)s);
   }
+}
+
+// Two-float twiddles: (cos hi, cos lo, sin hi, sin lo).
+__global__ void k_twiddles_df(float4* tw, int n) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)m / (double)n, &s, &c);
+    const float2 a = split_f64(c), b = split_f64(s);
+    tw[m] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+static const float4* twiddles_df(int device, int n, cudaStream_t st) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, float4*> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(device, n);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  float4* p = nullptr;
+  if (cudaMalloc(&p, sizeof(float4) * n) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  k_twiddles_df<<<(n + 255) / 256, 256, 0, st>>>(p, n);
+  cudaStreamSynchronize(st);
+  cache[key] = p;
+  return p;
 }
 
 // One immutable table per (device, N); kept for the life of the process.
@@ -70,6 +101,92 @@ __device__ __forceinline__ float w32c(int m) {
   return c[m];
 }
 __device__ __forceinline__ float w32s(int m) { return w32c((m + 24) & 31); }  // sin = cos(. - pi/2)
+// The same as two-float constants (fp32 rounding of cos(pi m / 16) and of
+// the rest), symmetric by construction.
+__device__ __forceinline__ dfl w32c_df(int m) {
+  constexpr float h[32] = {
+      1.0f, 0.9807852506637573f, 0.9238795042037964f, 0.8314695954322815f, 0.7071067690849304f,
+      0.5555702447891235f, 0.3826834261417389f, 0.19509032368659973f, 0.0f,
+      -0.19509032368659973f, -0.3826834261417389f, -0.5555702447891235f, -0.7071067690849304f,
+      -0.8314695954322815f, -0.9238795042037964f, -0.9807852506637573f, -1.0f,
+      -0.9807852506637573f, -0.9238795042037964f, -0.8314695954322815f, -0.7071067690849304f,
+      -0.5555702447891235f, -0.3826834261417389f, -0.19509032368659973f, 0.0f,
+      0.19509032368659973f, 0.3826834261417389f, 0.5555702447891235f, 0.7071067690849304f,
+      0.8314695954322815f, 0.9238795042037964f, 0.9807852506637573f};
+  constexpr float l[32] = {
+      0.0f, 2.9739473106360492e-08f, 2.830748968563057e-08f, 1.687026340846387e-08f,
+      1.2101617485882343e-08f, -1.1769521357507529e-08f, 6.2233507236442165e-09f,
+      -1.670471427850373e-09f, 0.0f, 1.670471427850373e-09f, -6.2233507236442165e-09f,
+      1.1769521357507529e-08f, -1.2101617485882343e-08f, -1.687026340846387e-08f,
+      -2.830748968563057e-08f, -2.9739473106360492e-08f, 0.0f, -2.9739473106360492e-08f,
+      -2.830748968563057e-08f, -1.687026340846387e-08f, -1.2101617485882343e-08f,
+      1.1769521357507529e-08f, -6.2233507236442165e-09f, 1.670471427850373e-09f, 0.0f,
+      -1.670471427850373e-09f, 6.2233507236442165e-09f, -1.1769521357507529e-08f,
+      1.2101617485882343e-08f, 1.687026340846387e-08f, 2.830748968563057e-08f,
+      2.9739473106360492e-08f};
+  return dfl{h[m], l[m]};
+}
+__device__ __forceinline__ dfl w32s_df(int m) { return w32c_df((m + 24) & 31); }
+
+// Arithmetic of the transforms: fp32, or two-float (CSG_PREC_HIGH).
+__device__ __forceinline__ float vadd(float a, float b) { return a + b; }
+__device__ __forceinline__ float vsub(float a, float b) { return a - b; }
+__device__ __forceinline__ float vneg(float a) { return -a; }
+__device__ __forceinline__ dfl vadd(dfl a, dfl b) { return df_add(a, b); }
+__device__ __forceinline__ dfl vsub(dfl a, dfl b) { return df_sub(a, b); }
+__device__ __forceinline__ dfl vneg(dfl a) { return df_neg(a); }
+
+// (dr + i di) times W_32^m (forward e^-i, inverse e^+i) for m != 0, 8.
+template <bool INV>
+__device__ __forceinline__ void mul_w32(float dr, float di, int m, float& orr, float& oi) {
+  const float c = w32c(m), s = INV ? w32s(m) : -w32s(m);
+  orr = dr * c - di * s;
+  oi = dr * s + di * c;
+}
+template <bool INV>
+__device__ __forceinline__ void mul_w32(dfl dr, dfl di, int m, dfl& orr, dfl& oi) {
+  const dfl c = w32c_df(m), s = INV ? w32s_df(m) : df_neg(w32s_df(m));
+  df_cmul(dr, di, c, s, orr, oi);
+}
+
+// Twiddle tables: cos, sin of 2 pi m / N as float2 (fp32) or float4
+// (two-float: cos hi, cos lo, sin hi, sin lo), both generated in FP64.
+template <class T> struct TwOf;
+template <> struct TwOf<float> { using type = float2; };
+template <> struct TwOf<dfl> { using type = float4; };
+
+template <bool INV>
+__device__ __forceinline__ void mul_tw(const float2* tw, int idx, float& a, float& b) {
+  const float2 w = __ldg(&tw[idx]);
+  const float ws = INV ? w.y : -w.y;
+  const float tr = a * w.x - b * ws;
+  b = a * ws + b * w.x;
+  a = tr;
+}
+template <bool INV>
+__device__ __forceinline__ void mul_tw(const float4* tw, int idx, dfl& a, dfl& b) {
+  const float4 w = __ldg(&tw[idx]);
+  const dfl c{w.x, w.y};
+  const dfl s = INV ? dfl{w.z, w.w} : dfl{-w.z, -w.w};
+  dfl ra, rb;
+  df_cmul(a, b, c, s, ra, rb);
+  a = ra;
+  b = rb;
+}
+
+// Shared-memory words of one value: fp32 values take one word; two-float
+// values keep their low words LO words further on (their own planes).
+template <int LO>
+__device__ __forceinline__ void sld(const float* p, int i, float& v) { v = p[i]; }
+template <int LO>
+__device__ __forceinline__ void sld(const float* p, int i, dfl& v) { v = dfl{p[i], p[i + LO]}; }
+template <int LO>
+__device__ __forceinline__ void sst(float* p, int i, float v) { p[i] = v; }
+template <int LO>
+__device__ __forceinline__ void sst(float* p, int i, dfl v) {
+  p[i] = v.h;
+  p[i + LO] = v.l;
+}
 
 constexpr int bitrev(int q, int bits) {
   int r = 0;
@@ -80,44 +197,42 @@ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 // Radix-2 decimation-in-frequency network on R register values (natural
 // order in, bit-reversed order out). sg = -1 forward, +1 inverse.
-template <int R, int HALF, bool INV>
-__device__ __forceinline__ void dif_stage(float* xr, float* xi) {
+template <int R, int HALF, bool INV, class T>
+__device__ __forceinline__ void dif_stage(T* xr, T* xi) {
   if constexpr (HALF >= 1) {
 #pragma unroll
     for (int base = 0; base < R; base += 2 * HALF) {
 #pragma unroll
       for (int k = 0; k < HALF; ++k) {
-        const float ar = xr[base + k], ai = xi[base + k];
-        const float br = xr[base + k + HALF], bi = xi[base + k + HALF];
-        xr[base + k] = ar + br;
-        xi[base + k] = ai + bi;
-        const float dr = ar - br, di = ai - bi;
+        const T ar = xr[base + k], ai = xi[base + k];
+        const T br = xr[base + k + HALF], bi = xi[base + k + HALF];
+        xr[base + k] = vadd(ar, br);
+        xi[base + k] = vadd(ai, bi);
+        const T dr = vsub(ar, br), di = vsub(ai, bi);
         constexpr int step = 32 / (2 * HALF);  // twiddle W_{2 HALF}^k = W_32^(k step)
         const int m = k * step;
         if (m == 0) {
           xr[base + k + HALF] = dr;
           xi[base + k + HALF] = di;
         } else if (m == 8) {  // times -i (forward) or +i (inverse)
-          xr[base + k + HALF] = INV ? -di : di;
-          xi[base + k + HALF] = INV ? dr : -dr;
+          xr[base + k + HALF] = INV ? vneg(di) : di;
+          xi[base + k + HALF] = INV ? dr : vneg(dr);
         } else {
-          const float c = w32c(m), s = INV ? w32s(m) : -w32s(m);
-          xr[base + k + HALF] = dr * c - di * s;
-          xi[base + k + HALF] = dr * s + di * c;
+          mul_w32<INV>(dr, di, m, xr[base + k + HALF], xi[base + k + HALF]);
         }
       }
     }
-    dif_stage<R, HALF / 2, INV>(xr, xi);
+    dif_stage<R, HALF / 2, INV, T>(xr, xi);
   }
 }
 
 // Shared-memory swizzle for E elements per thread: word address s is stored
-// at s ^ ((s >> log2 E) & 31). It permutes words within each aligned
-// 32-word row, and it makes every shared-memory access of these transforms
-// (the stride-E stores of the first stage, the (g, k) gathers and scatters
-// of the later stages, for rows of any N and for column tiles of 4, 8 or 16
-// columns) hit 32 distinct banks; checked exhaustively for N = 64..4096,
-// E = 16 and 32.
+// at s ^ ((s >> log2 E) & 31), a bijection that permutes words within each
+// aligned 32-word row. It makes every shared-memory access of these
+// transforms (the stride-E stores of the first stage, the (g, k) gathers and
+// scatters of the later stages, for rows of any N and for column tiles of 4,
+// 8 or 16 columns) hit 32 distinct banks; checked exhaustively for
+// N = 64..4096, E = 16 and 32.
 template <int E>
 __device__ __forceinline__ int swz(int s) {
   return s ^ ((s >> ilog2c(E)) & 31);
@@ -138,11 +253,12 @@ struct ColAddr {
 // Stockham stages of radix R at sub-length L. Each thread owns E / R
 // butterflies j = u + i N / E of one transform (index t of the tile).
 // stage_read gathers a stage's inputs (with the inter-stage twiddles) into
-// registers, stage_write scatters its outputs.
-template <int N, int E, int R, int L, bool INV, class A>
+// registers, stage_write scatters its outputs. LO: offset of the low-word
+// planes (two-float values).
+template <int N, int E, int R, int L, bool INV, class A, int LO, class T, class TW>
 __device__ __forceinline__ void stage_read(const float* __restrict__ re,
                                            const float* __restrict__ im, int t, int u,
-                                           const float2* __restrict__ tw, float* xr, float* xi) {
+                                           const TW* __restrict__ tw, T* xr, T* xi) {
   constexpr int TPT = N / E, BPT = E / R, STRIDE = N / R, TWSTEP = N / (L * R);
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
@@ -151,29 +267,25 @@ __device__ __forceinline__ void stage_read(const float* __restrict__ re,
 #pragma unroll
     for (int q = 0; q < R; ++q) {
       const int m = g * L + k + q * STRIDE;
-      float a = re[A::at(t, m)], b = im[A::at(t, m)];
-      if (L > 1 && q > 0) {
-        const float2 w = __ldg(&tw[k * q * TWSTEP]);
-        const float ws = INV ? w.y : -w.y;
-        const float tr = a * w.x - b * ws;
-        b = a * ws + b * w.x;
-        a = tr;
-      }
+      T a, b;
+      sld<LO>(re, A::at(t, m), a);
+      sld<LO>(im, A::at(t, m), b);
+      if (L > 1 && q > 0) mul_tw<INV>(tw, k * q * TWSTEP, a, b);
       xr[i * R + q] = a;
       xi[i * R + q] = b;
     }
   }
 }
 
-template <int E, int R, bool INV>
-__device__ __forceinline__ void stage_butterflies(float* xr, float* xi) {
+template <int E, int R, bool INV, class T>
+__device__ __forceinline__ void stage_butterflies(T* xr, T* xi) {
 #pragma unroll
-  for (int i = 0; i < E / R; ++i) dif_stage<R, R / 2, INV>(&xr[i * R], &xi[i * R]);
+  for (int i = 0; i < E / R; ++i) dif_stage<R, R / 2, INV, T>(&xr[i * R], &xi[i * R]);
 }
 
-template <int N, int E, int R, int L, class A>
+template <int N, int E, int R, int L, class A, int LO, class T>
 __device__ __forceinline__ void stage_write(float* __restrict__ re, float* __restrict__ im, int t,
-                                            int u, const float* xr, const float* xi) {
+                                            int u, const T* xr, const T* xi) {
   constexpr int TPT = N / E, BPT = E / R, bits = ilog2c(R);
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
@@ -182,8 +294,8 @@ __device__ __forceinline__ void stage_write(float* __restrict__ re, float* __res
 #pragma unroll
     for (int q = 0; q < R; ++q) {
       const int m = g * L * R + k + q * L;
-      re[A::at(t, m)] = xr[i * R + bitrev(q, bits)];
-      im[A::at(t, m)] = xi[i * R + bitrev(q, bits)];
+      sst<LO>(re, A::at(t, m), xr[i * R + bitrev(q, bits)]);
+      sst<LO>(im, A::at(t, m), xi[i * R + bitrev(q, bits)]);
     }
   }
 }
@@ -191,20 +303,20 @@ __device__ __forceinline__ void stage_write(float* __restrict__ re, float* __res
 // Stages from sub-length L on: shared memory holds the output of the stages
 // before L. Radix E while E L < N, then one final stage of radix N / L
 // whose outputs stay in registers in natural order.
-template <int N, int E, int L, bool INV, class A>
-__device__ __forceinline__ void fft_tail(float* xr, float* xi, float* re, float* im, int t, int u,
-                                         const float2* tw) {
+template <int N, int E, int L, bool INV, class A, int LO, class T, class TW>
+__device__ __forceinline__ void fft_tail(T* xr, T* xi, float* re, float* im, int t, int u,
+                                         const TW* tw) {
   if constexpr (L * E < N) {
-    stage_read<N, E, E, L, INV, A>(re, im, t, u, tw, xr, xi);
+    stage_read<N, E, E, L, INV, A, LO>(re, im, t, u, tw, xr, xi);
     __syncthreads();
     stage_butterflies<E, E, INV>(xr, xi);
-    stage_write<N, E, E, L, A>(re, im, t, u, xr, xi);
+    stage_write<N, E, E, L, A, LO>(re, im, t, u, xr, xi);
     __syncthreads();
-    fft_tail<N, E, L * E, INV, A>(xr, xi, re, im, t, u, tw);
+    fft_tail<N, E, L * E, INV, A, LO>(xr, xi, re, im, t, u, tw);
   } else {
     constexpr int R = N / L, BPT = E / R, bits = ilog2c(R);
-    float yr[E], yi[E];
-    stage_read<N, E, R, L, INV, A>(re, im, t, u, tw, yr, yi);
+    T yr[E], yi[E];
+    stage_read<N, E, R, L, INV, A, LO>(re, im, t, u, tw, yr, yi);
     stage_butterflies<E, R, INV>(yr, yi);
     // the last stage writes element k + q L with k = j = u + i N/E and
     // L = BPT N/E: element u + (i + q BPT) N/E
@@ -224,55 +336,86 @@ __device__ __forceinline__ void fft_tail(float* xr, float* xi, float* re, float*
 // loads straight from global memory and stores the result straight back;
 // shared memory carries only the exchanges between stages. The caller
 // synchronises before shared memory is reused by another transform.
-template <int N, int E, bool INV, class A>
-__device__ __forceinline__ void fft_regs(float* xr, float* xi, float* re, float* im, int t, int u,
-                                         const float2* tw) {
+template <int N, int E, bool INV, class A, int LO, class T, class TW>
+__device__ __forceinline__ void fft_regs(T* xr, T* xi, float* re, float* im, int t, int u,
+                                         const TW* tw) {
   stage_butterflies<E, E, INV>(xr, xi);
-  stage_write<N, E, E, 1, A>(re, im, t, u, xr, xi);
+  stage_write<N, E, E, 1, A, LO>(re, im, t, u, xr, xi);
   __syncthreads();
-  fft_tail<N, E, E, INV, A>(xr, xi, re, im, t, u, tw);
+  fft_tail<N, E, E, INV, A, LO>(xr, xi, re, im, t, u, tw);
 }
 
 // Elements per thread: 32 (radix-32 stages, one shared-memory exchange at
-// N = 1024, 128 registers) from N = 512 up, 16 below.
+// N = 1024, 128 registers) from N = 512 up, 16 below; two-float transforms
+// always 16 (64 registers of values).
 constexpr int default_e(int n) { return n >= 512 ? 32 : 16; }
+template <class T>
+constexpr int elems_for(int n) {
+  return std::is_same<T, dfl>::value ? 16 : default_e(n);
+}
 // CTAs per SM the register budget is sized for: 128 registers per thread at
-// E = 32, 64-85 at E = 16.
+// E = 32, 64-85 at E = 16; two-float row passes 128 at 256 threads.
 constexpr int min_blocks(int e, int threads) {
   return e == 32 ? (threads >= 512 ? 1 : 512 / threads)
                  : (threads >= 1024 ? 1 : (threads >= 512 ? 2 : 3));
 }
+template <class T>
+constexpr int min_blocks_t(int e, int threads) {
+  return std::is_same<T, dfl>::value ? (threads >= 512 ? 1 : (threads >= 256 ? 2 : 4))
+                                     : min_blocks(e, threads);
+}
+// Words per value in shared memory.
+template <class T>
+constexpr int words_of() {
+  return std::is_same<T, dfl>::value ? 2 : 1;
+}
 
-template <int N, int E>
+template <int N, int E, class T = float>
 struct RowCfg {
   static constexpr int TPT = N / E;
   static constexpr int ROWS = 256 / TPT > 0 ? 256 / TPT : 1;  // 256 threads per CTA
   static constexpr int THREADS = ROWS * TPT;
-  static constexpr int MIN_BLOCKS = min_blocks(E, THREADS);
-  static constexpr size_t SMEM = (size_t)ROWS * N * 8;
+  static constexpr int MIN_BLOCKS = min_blocks_t<T>(E, THREADS);
+  static constexpr int PLANE = ROWS * N;  // words of one component plane
+  static constexpr size_t SMEM = (size_t)ROWS * N * 8 * words_of<T>();
 };
-// Column tile width: 8 columns (32-byte row segments) at N = 1024.
+// Column tile width: 8 columns (32-byte row segments) at N = 1024. Two-float
+// tiles hold 256 threads (one CTA per SM with up to 255 registers: the
+// transfer-function product and the inverse transform need them; 64 KB of
+// shared memory), 4 columns at N = 1024.
 constexpr int default_cols(int n) { return n <= 512 ? 16 : (n == 1024 ? 8 : 4); }
-template <int N, int E, int COLS>
+template <class T>
+constexpr int cols_for(int n) {
+  return std::is_same<T, dfl>::value ? (256 / (n / 16) > 0 ? 256 / (n / 16) : 1)
+                                     : default_cols(n);
+}
+template <int N, int E, int COLS, class T = float>
 struct ColCfg {
   static constexpr int TPT = N / E;
   static constexpr int THREADS = COLS * TPT;
-  static constexpr int MIN_BLOCKS = min_blocks(E, THREADS);
-  static constexpr size_t SMEM = (size_t)COLS * N * 8;
+  static constexpr int MIN_BLOCKS =
+      std::is_same<T, dfl>::value ? 1 : min_blocks_t<T>(E, THREADS);
+  static constexpr int PLANE = COLS * N;
+  static constexpr size_t SMEM = (size_t)COLS * N * 8 * words_of<T>();
 };
 
-// Row pass with fused element prologue / epilogue.
-template <int N, int E, bool INV>
-__global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCKS)
-    k_fft_rows(float* __restrict__ field, float scale, const float2* __restrict__ tw,
+// Row pass with fused element prologue / epilogue. Two-float passes (T =
+// dfl) apply the element ops in fp32 on the pupil-plane values as loaded and
+// as rounded for the store; the transform itself runs in two-float.
+template <int N, int E, bool INV, class T>
+__global__ void __launch_bounds__(RowCfg<N, E, T>::THREADS, RowCfg<N, E, T>::MIN_BLOCKS)
+    k_fft_rows(float* __restrict__ field, float scale,
+               const typename TwOf<T>::type* __restrict__ tw,
                const __grid_constant__ PixOps pro, const __grid_constant__ PixOps epi,
                const __grid_constant__ FieldInfo fi, const FftBand band) {
-  using CF = RowCfg<N, E>;
+  using CF = RowCfg<N, E, T>;
   using A = RowAddr<N, E>;
+  constexpr int LO = 2 * CF::PLANE;
+  constexpr bool DF = std::is_same<T, dfl>::value;
   extern __shared__ float sm[];
   __shared__ PixConsts shk[2];
   float* re = sm;
-  float* im = sm + CF::ROWS * N;
+  float* im = sm + CF::PLANE;
   constexpr int TPT = CF::TPT;
   const int cpf = band.n ? band.n / CF::ROWS : N / CF::ROWS;  // CTAs per field
   const int f = blockIdx.x / cpf;
@@ -318,9 +461,24 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
     for (int h = 0; h < E; h += G)
       pix_apply_n<G>(pro, kp, row, u + h * TPT, 0, TPT, N, N, xr + h, xi + h);
   }
-  fft_regs<N, E, INV, A>(xr, xi, re, im, t, u, tw);
+  if constexpr (DF) {
+    dfl yr[E], yi[E];
 #pragma unroll
-  for (int s = 0; s < E; ++s) xr[s] *= scale, xi[s] *= scale;
+    for (int s = 0; s < E; ++s) {
+      yr[s] = df_from(xr[s]);
+      yi[s] = df_from(xi[s]);
+    }
+    fft_regs<N, E, INV, A, LO>(yr, yi, re, im, t, u, tw);
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+      xr[s] = df_round(df_scale(yr[s], scale));  // scale: a power of two
+      xi[s] = df_round(df_scale(yi[s], scale));
+    }
+  } else {
+    fft_regs<N, E, INV, A, LO>(xr, xi, re, im, t, u, tw);
+#pragma unroll
+    for (int s = 0; s < E; ++s) xr[s] *= scale, xi[s] *= scale;
+  }
   if (epi.n) {
 #pragma unroll
     for (int h = 0; h < E; h += 8)
@@ -342,7 +500,7 @@ __global__ void __launch_bounds__(RowCfg<N, E>::THREADS, RowCfg<N, E>::MIN_BLOCK
     fre[s * TPT] = xr[s];
     fim[s * TPT] = xi[s];
   }
-  if constexpr (INV) {
+  if constexpr (INV && !DF) {
     if (band.split) {
       // The next MFT's operand parts, straight from the registers. Lane pairs
       // (u, u ^ 1) swap one value per two slots so that each lane holds two
@@ -419,10 +577,58 @@ __global__ void k_fresnel_table(int N, const double* lam, double z, double ap_ra
     out[(size_t)s * plane + i] = fresnel_h(N, i / N, i % N, fc);
 }
 
+// The transfer function of the two-float Fresnel (CSG_PREC_HIGH), evaluated
+// in FP64: turns = t0 - (z / lambda) eps / (1 + sqrt(1 - eps)) with
+// t0 = z / lambda reduced first, so the phase is exact to ~1e-13 turns;
+// stored as (cos hi, cos lo, sin hi, sin lo).
+__global__ void k_fresnel_table_df(int N, const double* lam, double z, double ap_rad,
+                                   float4* __restrict__ out) {
+  const int s = blockIdx.y;
+  const double zl = z / lam[s];
+  const double t0 = zl - rint(zl);
+  const double ce = 0.25 * (lam[s] / ap_rad) * (lam[s] / ap_rad);
+  const int plane = N * N;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x) {
+    const int r = i / N, c = i % N;
+    const int fr = r < N / 2 ? r : r - N;
+    const int fc = c < N / 2 ? c : c - N;
+    const double eps = ce * (double)(fr * fr + fc * fc);
+    double t = t0 - zl * eps / (1.0 + sqrt(1.0 - eps));
+    t -= rint(t);
+    double sn, cs;
+    sincospi(2.0 * t, &sn, &cs);
+    const float2 a = split_f64(cs), b = split_f64(sn);
+    out[(size_t)s * plane + i] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
 int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, double z,
                         double ap_rad, float2* out) {
   dim3 grid(grid_for((long long)N * N, 256, 1024), n_slot);
   k_fresnel_table<<<grid, 256, 0, st>>>(N, lam, z, ap_rad, out);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
+int build_fresnel_table_df(cudaStream_t st, int N, const double* lam, int n_slot, double z,
+                           double ap_rad, float4* out) {
+  dim3 grid(grid_for((long long)N * N, 256, 1024), n_slot);
+  k_fresnel_table_df<<<grid, 256, 0, st>>>(N, lam, z, ap_rad, out);
+  CSG_LAUNCH_CHECK();
+  return CSG_OK;
+}
+
+// A two-float table from an fp32 one (masks used as transfer functions).
+__global__ void k_table_to_df(const float2* __restrict__ in, float4* __restrict__ out,
+                              long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 v = in[i];
+    out[i] = make_float4(v.x, 0.f, v.y, 0.f);
+  }
+}
+int table_to_df(cudaStream_t st, const float2* in, float4* out, long long n) {
+  k_table_to_df<<<grid_for(n, 256, 1024), 256, 0, st>>>(in, out, n);
   CSG_LAUNCH_CHECK();
   return CSG_OK;
 }
@@ -433,17 +639,20 @@ int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, d
 // consecutive floats. In MODE 2 the forward transform leaves each thread
 // holding exactly the elements the inverse transform's first stage needs,
 // so H is applied in registers and the inverse starts without a
-// shared-memory exchange.
-template <int N, int E, int MODE, int COLS>
-__global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS>::MIN_BLOCKS)
-    k_fft_cols(float* __restrict__ field, const float2* __restrict__ tw,
+// shared-memory exchange. Two-float passes read the two-float table H4.
+template <int N, int E, int MODE, int COLS, class T>
+__global__ void __launch_bounds__(ColCfg<N, E, COLS, T>::THREADS,
+                                  ColCfg<N, E, COLS, T>::MIN_BLOCKS)
+    k_fft_cols(float* __restrict__ field, const typename TwOf<T>::type* __restrict__ tw,
                const __grid_constant__ FresnelArgs fa, int band_lo, int band_n, int store_all) {
-  using CF = ColCfg<N, E, COLS>;
+  using CF = ColCfg<N, E, COLS, T>;
   using A = ColAddr<COLS, E>;
+  constexpr int LO = 2 * CF::PLANE;
+  constexpr bool DF = std::is_same<T, dfl>::value;
   constexpr int TPT = CF::TPT;
   extern __shared__ float sm[];
   float* re = sm;
-  float* im = sm + A::PITCH * N;
+  float* im = sm + CF::PLANE;
   constexpr int CPF = N / COLS;
   const int f = blockIdx.x / CPF;
   const int c0 = (blockIdx.x % CPF) * COLS;
@@ -451,7 +660,7 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS
   const size_t plane = (size_t)N * N;
   float* fre = field + (size_t)f * 2 * plane + (size_t)u * N + c0 + t;
   float* fim = fre + plane;
-  float xr[E], xi[E];
+  T xr[E], xi[E];
   // band: rows u + s N/E outside [band_lo, band_lo + band_n) are zero on
   // input and, unless store_all, not stored (band_n = 0: every row)
   const int s0 = band_n ? band_lo / TPT : 0, s1 = band_n ? (band_lo + band_n) / TPT : E;
@@ -459,12 +668,34 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS
 #pragma unroll
   for (int s = 0; s < E; ++s) {
     const bool in = s >= s0 && s < s1;
-    xr[s] = in ? fre[(size_t)s * TPT * N] : 0.f;
-    xi[s] = in ? fim[(size_t)s * TPT * N] : 0.f;
+    const float a = in ? fre[(size_t)s * TPT * N] : 0.f;
+    const float b = in ? fim[(size_t)s * TPT * N] : 0.f;
+    if constexpr (DF) {
+      xr[s] = df_from(a);
+      xi[s] = df_from(b);
+    } else {
+      xr[s] = a;
+      xi[s] = b;
+    }
   }
-  fft_regs<N, E, MODE == 1, A>(xr, xi, re, im, t, u, tw);
+  fft_regs<N, E, MODE == 1, A, LO>(xr, xi, re, im, t, u, tw);
   if (MODE == 2) {
-    if (fa.H) {  // per-wavelength table (L2-resident, shared by the batch)
+    if constexpr (DF) {
+      const float4* Hs = fa.H4 + (size_t)fa.slot[f] * plane + (size_t)u * N + c0 + t;
+#pragma unroll
+      for (int h = 0; h < E; h += 4) {
+        float4 w[4];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) w[s] = __ldg(&Hs[(size_t)(h + s) * TPT * N]);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          dfl orr, oi;
+          df_cmul(xr[h + s], xi[h + s], dfl{w[s].x, w[s].y}, dfl{w[s].z, w[s].w}, orr, oi);
+          xr[h + s] = orr;
+          xi[h + s] = oi;
+        }
+      }
+    } else if (fa.H) {  // per-wavelength table (L2-resident, shared by the batch)
       const float2* Hs = fa.H + (size_t)fa.slot[f] * plane + (size_t)u * N + c0 + t;
 #pragma unroll
       for (int h = 0; h < E; h += 8) {  // in groups of 8 (bounds the live table values)
@@ -492,13 +723,18 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS>::THREADS, ColCfg<N, E, COLS
       }
     }
     __syncthreads();  // the forward transform's last reads precede the inverse's writes
-    fft_regs<N, E, true, A>(xr, xi, re, im, t, u, tw);
+    fft_regs<N, E, true, A, LO>(xr, xi, re, im, t, u, tw);
   }
 #pragma unroll
   for (int s = 0; s < E; ++s)
     if (s >= w0 && s < w1) {
-      fre[(size_t)s * TPT * N] = xr[s];
-      fim[(size_t)s * TPT * N] = xi[s];
+      if constexpr (DF) {
+        fre[(size_t)s * TPT * N] = df_round(xr[s]);
+        fim[(size_t)s * TPT * N] = df_round(xi[s]);
+      } else {
+        fre[(size_t)s * TPT * N] = xr[s];
+        fim[(size_t)s * TPT * N] = xi[s];
+      }
     }
 }
 
@@ -511,42 +747,45 @@ static int prep_smem(K kern, size_t bytes) {
   return CSG_OK;
 }
 
-template <int N, int E, int COLS>
-static int launch_cols(cudaStream_t st, float* field, int F, int mode, const float2* tw,
-                       const FresnelArgs* fa, const FftBand& band, int store_all) {
-  using CC = ColCfg<N, E, COLS>;
+template <int N, int E, int COLS, class T>
+static int launch_cols(cudaStream_t st, float* field, int F, int mode,
+                       const typename TwOf<T>::type* tw, const FresnelArgs* fa,
+                       const FftBand& band, int store_all) {
+  using CC = ColCfg<N, E, COLS, T>;
   const int grid = F * (N / COLS);
   int rc;
   if (mode == 2) {
-    if ((rc = prep_smem(k_fft_cols<N, E, 2, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, E, 2, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa, band.lo,
-                                                                   band.n, store_all);
+    if ((rc = prep_smem(k_fft_cols<N, E, 2, COLS, T>, CC::SMEM))) return rc;
+    k_fft_cols<N, E, 2, COLS, T><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa, band.lo,
+                                                                      band.n, store_all);
   } else if (mode == 1) {
-    if ((rc = prep_smem(k_fft_cols<N, E, 1, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, E, 1, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{}, 0,
-                                                                   0, 0);
+    if ((rc = prep_smem(k_fft_cols<N, E, 1, COLS, T>, CC::SMEM))) return rc;
+    k_fft_cols<N, E, 1, COLS, T><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{},
+                                                                      0, 0, 0);
   } else {
-    if ((rc = prep_smem(k_fft_cols<N, E, 0, COLS>, CC::SMEM))) return rc;
-    k_fft_cols<N, E, 0, COLS><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{}, 0,
-                                                                   0, 0);
+    if ((rc = prep_smem(k_fft_cols<N, E, 0, COLS, T>, CC::SMEM))) return rc;
+    k_fft_cols<N, E, 0, COLS, T><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, FresnelArgs{},
+                                                                      0, 0, 0);
   }
   CSG_LAUNCH_CHECK();
   return CSG_OK;
 }
 
-template <int N, int E>
+template <int N, int E, class T>
 static int launch_rows(cudaStream_t st, float* field, int F, bool inv, float scale,
-                       const float2* tw, const PixOps& p, const PixOps& e, const FieldInfo& fi,
-                       const FftBand& band) {
-  using RC = RowCfg<N, E>;
+                       const typename TwOf<T>::type* tw, const PixOps& p, const PixOps& e,
+                       const FieldInfo& fi, const FftBand& band) {
+  using RC = RowCfg<N, E, T>;
   const int grid = F * ((band.n ? band.n : N) / RC::ROWS);
   int rc;
   if (inv) {
-    if ((rc = prep_smem(k_fft_rows<N, E, true>, RC::SMEM))) return rc;
-    k_fft_rows<N, E, true><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi, band);
+    if ((rc = prep_smem(k_fft_rows<N, E, true, T>, RC::SMEM))) return rc;
+    k_fft_rows<N, E, true, T><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi,
+                                                                   band);
   } else {
-    if ((rc = prep_smem(k_fft_rows<N, E, false>, RC::SMEM))) return rc;
-    k_fft_rows<N, E, false><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi, band);
+    if ((rc = prep_smem(k_fft_rows<N, E, false, T>, RC::SMEM))) return rc;
+    k_fft_rows<N, E, false, T><<<grid, RC::THREADS, RC::SMEM, st>>>(field, scale, tw, p, e, fi,
+                                                                    band);
   }
   CSG_LAUNCH_CHECK();
   return CSG_OK;
@@ -562,18 +801,21 @@ static int env_choice(const char* name, std::initializer_list<int> allowed) {
   return 0;
 }
 
-template <int N>
+template <int N, class T>
 static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const FresnelArgs* fa,
-                   const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const float2* tw,
-                   const FftBand& band, const FftBand& sup, __nv_bfloat16* split_out) {
+                   const PixOps& pro, const PixOps& epi, const FieldInfo& fi,
+                   const typename TwOf<T>::type* tw, const FftBand& band, const FftBand& sup,
+                   __nv_bfloat16* split_out) {
+  constexpr bool DF = std::is_same<T, dfl>::value;
   cudaStream_t st = ctx->stream;
   const float inv_scale = 1.f / ((float)N * (float)N);
   // a band-limited pass moves n rows of N (the first and last touch n x n)
   const double pass_bytes = (double)F * N * (band.n ? band.n : N) * 16.0;
   const double edge_bytes = band.n ? (double)F * band.n * (N + band.n) * 8.0 : pass_bytes;
   const PixOps none;
-  const bool e16 = (N == 1024) && !band.n && !sup.n && env_choice("CSG_FFT_E", {16}) == 16;
-  const int c_over = env_choice("CSG_FFT_COLS", {4, 16});
+  const bool e16 =
+      !DF && (N == 1024) && !band.n && !sup.n && env_choice("CSG_FFT_E", {16}) == 16;
+  const int c_over = DF ? 0 : env_choice("CSG_FFT_COLS", {4, 16});
   int rc;
   auto rows = [&](bool inv, float scale, const PixOps& p, const PixOps& e,
                   const FftBand& bd) -> int {
@@ -582,20 +824,21 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
                              (gen ? 0.5 : 1.0) +
                          (bd.split ? (double)F * N * N * 12.0 : 0.0);
     ProfScope ps(ctx, inv ? "fft_rows_inv" : "fft_rows_fwd", 0, bytes);
-    if constexpr (N == 1024)
-      if (e16) return launch_rows<N, 16>(st, field, F, inv, scale, tw, p, e, fi, bd);
-    return launch_rows<N, default_e(N)>(st, field, F, inv, scale, tw, p, e, fi, bd);
+    if constexpr (N == 1024 && !DF)
+      if (e16) return launch_rows<N, 16, T>(st, field, F, inv, scale, tw, p, e, fi, bd);
+    return launch_rows<N, elems_for<T>(N), T>(st, field, F, inv, scale, tw, p, e, fi, bd);
   };
   auto cols = [&](int mode, const FftBand& bd, int store_all) -> int {
     const double bytes = store_all ? (double)F * N * (N + bd.n) * 8.0 : pass_bytes;
     ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, bytes);
-    if constexpr (N == 1024) {
-      if (e16) return launch_cols<N, 16, 8>(st, field, F, mode, tw, fa, bd, store_all);
-      if (c_over == 4) return launch_cols<N, 32, 4>(st, field, F, mode, tw, fa, bd, store_all);
-      if (c_over == 16) return launch_cols<N, 32, 16>(st, field, F, mode, tw, fa, bd, store_all);
+    if constexpr (N == 1024 && !DF) {
+      if (e16) return launch_cols<N, 16, 8, T>(st, field, F, mode, tw, fa, bd, store_all);
+      if (c_over == 4) return launch_cols<N, 32, 4, T>(st, field, F, mode, tw, fa, bd, store_all);
+      if (c_over == 16)
+        return launch_cols<N, 32, 16, T>(st, field, F, mode, tw, fa, bd, store_all);
     }
-    return launch_cols<N, default_e(N), default_cols(N)>(st, field, F, mode, tw, fa, bd,
-                                                         store_all);
+    return launch_cols<N, elems_for<T>(N), cols_for<T>(N), T>(st, field, F, mode, tw, fa, bd,
+                                                               store_all);
   };
   FftBand whole, last = band;
   whole.split = last.split = split_out;  // the last pass also writes the split
@@ -622,45 +865,67 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
   return CSG_OK;
 }
 
-bool fft_band_supported(int N, int lo, int n) {
-  const int E = default_e(N), TPT = N / E, rows = 256 / TPT > 0 ? 256 / TPT : 1;
+// Threads per transform of the row and column passes (fp32 or two-float).
+static int fft_tpt(int N, bool high) { return N / (high ? 16 : default_e(N)); }
+
+bool fft_band_supported(int N, int lo, int n, bool high) {
+  const int TPT = fft_tpt(N, high), rows = 256 / TPT > 0 ? 256 / TPT : 1;
   return n > 0 && lo >= 0 && lo + n <= N && lo % TPT == 0 && n % TPT == 0 && n % rows == 0;
 }
 
-bool fft_row_support(int N, int r0, int r1, int* lo, int* n) {
-  const int TPT = N / default_e(N);
+bool fft_row_support(int N, int r0, int r1, int* lo, int* n, bool high) {
+  const int TPT = fft_tpt(N, high);
   if (r0 < 0 || r1 > N || r0 >= r1) return false;
   *lo = r0 / TPT * TPT;
   *n = (r1 + TPT - 1) / TPT * TPT - *lo;
-  return fft_band_supported(N, *lo, *n);
+  return fft_band_supported(N, *lo, *n, high);
+}
+
+template <class T>
+static int run_fft_n(csg_ctx* ctx, float* field, int F, int n, int direction,
+                     const FresnelArgs* fa, const PixOps& pro, const PixOps& epi,
+                     const FieldInfo& fi, const typename TwOf<T>::type* tw, const FftBand& bd,
+                     const FftBand& sp, __nv_bfloat16* so) {
+  switch (n) {
+    case 64: return run_fft<64, T>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 128: return run_fft<128, T>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 256: return run_fft<256, T>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 512: return run_fft<512, T>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 1024:
+      return run_fft<1024, T>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    case 2048:
+      return run_fft<2048, T>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+    default:
+      return run_fft<4096, T>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+  }
 }
 
 // 2-D FFT or Fresnel propagation of F square N x N fields with fused element
-// ops (pro before the transform, epi after it).
+// ops (pro before the transform, epi after it); high: two-float arithmetic.
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const FftBand* band,
-                const FftBand* support, __nv_bfloat16* split_out) {
+                const FftBand* support, __nv_bfloat16* split_out, bool high) {
   CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
             "FFT size must be a power of two in [64, 4096]");
   CSG_CHECK(F > 0 && (long long)F * n < (1LL << 31), CSG_E_SHAPE, "FFT: bad field count");
   FftBand bd, sp;
   if (band) {
     CSG_CHECK(fa && !pro.n && !epi.n && band->src && band->dst && !band->split && !support &&
-                  fft_band_supported(n, band->lo, band->n),
+                  fft_band_supported(n, band->lo, band->n, high),
               CSG_E_ARG, "FFT: unsupported band-limited transform");
     bd = *band;
   }
-  CSG_CHECK(!split_out || (fa && !band), CSG_E_ARG,
-            "FFT: the split output needs a Fresnel pass over the whole field");
+  CSG_CHECK(!split_out || (fa && !band && !high), CSG_E_ARG,
+            "FFT: the split output needs an fp32 Fresnel pass over the whole field");
+  CSG_CHECK(!high || !fa || fa->H4, CSG_E_ARG,
+            "FFT: a two-float Fresnel pass needs the two-float transfer-function table");
   if (support) {
     CSG_CHECK(fa && !support->src && !support->dst && !support->split &&
-                  fft_band_supported(n, support->lo, support->n),
+                  fft_band_supported(n, support->lo, support->n, high),
               CSG_E_ARG, "FFT: unsupported row support");
     sp = *support;
   }
   cudaStream_t st = ctx->stream;
-  const float2* tw = twiddles(ctx->device, n, st);
-  CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
   const double pass_bytes = (double)F * n * n * 16.0;
   const bool gen = pro.n && pro.kind[0] == OP_SOURCE;  // the first pass only writes
   double total = pass_bytes * ((fa ? 3.0 : 2.0) - (gen ? 0.5 : 0.0));
@@ -670,17 +935,15 @@ int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const F
     total = (double)F * n * support->n * 16.0 * (gen ? 0.5 : 1.0) +
             (double)F * n * (n + support->n) * 8.0 + pass_bytes;
   if (split_out) total += (double)F * n * n * 12.0;
-  ProfScope ps(ctx, fa ? "fresnel_3pass" : "fft2d_2pass", 0, total);
-  __nv_bfloat16* so = split_out;
-  switch (n) {
-    case 64: return run_fft<64>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
-    case 128: return run_fft<128>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
-    case 256: return run_fft<256>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
-    case 512: return run_fft<512>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
-    case 1024: return run_fft<1024>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
-    case 2048: return run_fft<2048>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
-    default: return run_fft<4096>(ctx, field, F, direction, fa, pro, epi, fi, tw, bd, sp, so);
+  ProfScope ps(ctx, fa ? (high ? "fresnel_3pass_df" : "fresnel_3pass") : "fft2d_2pass", 0, total);
+  if (high) {
+    const float4* tw = twiddles_df(ctx->device, n, st);
+    CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
+    return run_fft_n<dfl>(ctx, field, F, n, direction, fa, pro, epi, fi, tw, bd, sp, nullptr);
   }
+  const float2* tw = twiddles(ctx->device, n, st);
+  CSG_CHECK(tw != nullptr, CSG_E_NOMEM, "twiddle table allocation failed");
+  return run_fft_n<float>(ctx, field, F, n, direction, fa, pro, epi, fi, tw, bd, sp, split_out);
 }
 
 }  // namespace csg
@@ -696,6 +959,19 @@ int csg_fft2d(csg_ctx* ctx, float* field, int n_fields, int n, int direction) {
   return fft2d_fused(ctx, field, n_fields, n, direction, nullptr, PixOps(), PixOps(), FieldInfo());
 }
 
+int csg_fft2d_prec(csg_ctx* ctx, float* field, int n_fields, int n, int direction,
+                   int precision) {
+  CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3 ||
+                precision == CSG_PREC_HIGH,
+            CSG_E_ARG, "csg_fft2d_prec: bad precision");
+  CSG_CHECK(ctx && field, CSG_E_ARG, "csg_fft2d_prec: null argument");
+  CSG_CHECK(direction == -1 || direction == 1, CSG_E_ARG,
+            "csg_fft2d_prec: direction must be -1 or +1");
+  DeviceGuard g(ctx->device);
+  return fft2d_fused(ctx, field, n_fields, n, direction, nullptr, PixOps(), PixOps(), FieldInfo(),
+                     nullptr, nullptr, nullptr, precision == CSG_PREC_HIGH);
+}
+
 int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
                 double ap_rad, double z) {
   CSG_CHECK(ctx && field && lambda, CSG_E_ARG, "csg_fresnel: null argument");
@@ -703,6 +979,51 @@ int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* l
   DeviceGuard g(ctx->device);
   FresnelArgs fa{lambda, z, ap_rad};
   return fft2d_fused(ctx, field, n_fields, n, -1, &fa, PixOps(), PixOps(), FieldInfo());
+}
+
+int csg_fresnel_prec(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
+                     double ap_rad, double z, int precision) {
+  CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3 ||
+                precision == CSG_PREC_HIGH,
+            CSG_E_ARG, "csg_fresnel_prec: bad precision");
+  if (precision != CSG_PREC_HIGH) return csg_fresnel(ctx, field, n_fields, n, lambda, ap_rad, z);
+  CSG_CHECK(ctx && field && lambda, CSG_E_ARG, "csg_fresnel_prec: null argument");
+  CSG_CHECK(ap_rad > 0, CSG_E_ARG, "csg_fresnel_prec: apRad must be positive");
+  CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
+            "FFT size must be a power of two in [64, 4096]");
+  CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_fresnel_prec: n_fields must be positive");
+  DeviceGuard g(ctx->device);
+  cudaStream_t st = ctx->stream;
+  // one two-float transfer function per field (its own wavelength), built in
+  // FP64 for this call: the fields' slot is their own index
+  const size_t plane = (size_t)n * n;
+  float4* H4 = nullptr;
+  int* slot = nullptr;
+  if (cudaMallocAsync(&H4, plane * n_fields * sizeof(float4), st) != cudaSuccess ||
+      cudaMallocAsync(&slot, n_fields * sizeof(int), st) != cudaSuccess) {
+    cudaGetLastError();
+    if (H4) cudaFreeAsync(H4, st);
+    set_error("csg_fresnel_prec: allocation failed");
+    return CSG_E_NOMEM;
+  }
+  std::vector<int> idx(n_fields);
+  for (int i = 0; i < n_fields; ++i) idx[i] = i;
+  int rc = CSG_OK;
+  if (cudaMemcpyAsync(slot, idx.data(), n_fields * sizeof(int), cudaMemcpyHostToDevice, st) !=
+      cudaSuccess) {
+    set_error("csg_fresnel_prec: copy failed");
+    rc = CSG_E_CUDA;
+  }
+  if (!rc) rc = build_fresnel_table_df(st, n, lambda, n_fields, z, ap_rad, H4);
+  if (!rc) {
+    FresnelArgs fa{lambda, z, ap_rad, nullptr, slot, H4};
+    rc = fft2d_fused(ctx, field, n_fields, n, -1, &fa, PixOps(), PixOps(), FieldInfo(), nullptr,
+                     nullptr, nullptr, true);
+  }
+  cudaStreamSynchronize(st);  // the host index vector and the tables
+  cudaFreeAsync(H4, st);
+  cudaFreeAsync(slot, st);
+  return rc;
 }
 
 }  // extern "C"

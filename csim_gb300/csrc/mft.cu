@@ -134,6 +134,66 @@ __global__ void k_build_operator(__nv_bfloat16* __restrict__ op, const double* _
   }
 }
 
+// The operator of CSG_PREC_HIGH: the same values, split on one grid per
+// 64-wide K group of each row and plane (split3_aligned). One warp per
+// (slot, row, group); lane l computes elements 64 g + l and 64 g + 32 + l.
+__global__ void k_build_operator_aligned(__nv_bfloat16* __restrict__ op,
+                                         const double* __restrict__ cout,
+                                         const double* __restrict__ cin, int rows, int K,
+                                         int n_slots, const double* __restrict__ lf,
+                                         const double* __restrict__ pref, double sgn, int cstride,
+                                         const int* __restrict__ valid) {
+  const int groups = (K + 63) / 64;
+  const long long nw = (long long)n_slots * rows * groups;
+  const long long plane = (long long)rows * K;
+  const int lane = threadIdx.x & 31;
+  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw;
+       w += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const int gi = (int)(w % groups);
+    const long long t = w / groups;
+    const int r = (int)(t % rows);
+    const int s = (int)(t / rows);
+    float vre[2], vim[2];
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const int k = gi * 64 + hh * 32 + lane;
+      vre[hh] = vim[hh] = 0.f;
+      if (k < K) {
+        double turns = cout[(long long)s * cstride + r] * cin[k] / lf[s];
+        turns -= rint(turns);
+        double sn, cs;
+        sincospi(2.0 * sgn * turns, &sn, &cs);
+        double pr = 1.0, pi = 0.0;
+        if (pref) {
+          pr = pref[2 * s];
+          pi = pref[2 * s + 1];
+        }
+        if (valid && r >= valid[s]) pr = pi = 0.0;
+        vre[hh] = (float)(pr * cs - pi * sn);
+        vim[hh] = (float)(pr * sn + pi * cs);
+      }
+    }
+    const Grid gre = grid_of(__reduce_max_sync(0xffffffffu, max(absbits(vre[0]), absbits(vre[1]))));
+    const Grid gim = grid_of(__reduce_max_sync(0xffffffffu, max(absbits(vim[0]), absbits(vim[1]))));
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const int k = gi * 64 + hh * 32 + lane;
+      if (k >= K) continue;
+      __nv_bfloat16 pre[3], pim[3];
+      split3_aligned(vre[hh], gre, pre[0], pre[1], pre[2]);
+      split3_aligned(vim[hh], gim, pim[0], pim[1], pim[2]);
+      const long long off = (long long)r * K + k;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        __nv_bfloat16* base = op + ((long long)(s * 3 + q) * 3) * plane + off;
+        base[0] = pre[q];
+        base[plane] = pim[q];
+        base[2 * plane] = __hneg(pim[q]);
+      }
+    }
+  }
+}
+
 // Data split: planar fp32 [F][2][R][C] -> (element ops `pre`) -> (times a
 // complex multiplier [n_mul][2][R][C] chosen by mul_idx[f]) -> bf16
 // [F][3][2][R][C]. Eight pixels of one row per thread (C is a multiple of
@@ -206,17 +266,101 @@ __global__ void k_split_field(const float* __restrict__ in, __nv_bfloat16* __res
   }
 }
 
+// The data split of CSG_PREC_HIGH: as k_split_field, with every 64-column
+// group of a row split on one grid (split3_aligned). One warp per (row,
+// 256-column chunk): lane l holds columns 8 l .. 8 l + 7 of the chunk, so
+// the eight lanes 8 m .. 8 m + 7 hold one group and exchange their maxima.
+__global__ void k_split_field_aligned(const float* __restrict__ in,
+                                      __nv_bfloat16* __restrict__ out, int R, int C, int r0,
+                                      int c0, int RT, int PT, const float* __restrict__ mul,
+                                      const int* __restrict__ mul_idx,
+                                      const __grid_constant__ PixOps pre,
+                                      const __grid_constant__ FieldInfo fi,
+                                      const int* __restrict__ in_idx) {
+  __shared__ PixConsts shk;
+  const int f = blockIdx.y;
+  const int plane = R * C;
+  const size_t fplane = (size_t)RT * PT;
+  PixConsts k;
+  if (pre.n) pix_consts_cta(pre, fi, f, RT, PT, k, &shk);
+  const float* ire = in + (size_t)(in_idx ? in_idx[f] : f) * 2 * fplane;
+  const float* iim = ire + fplane;
+  const float* mre = mul ? mul + (size_t)mul_idx[f] * 2 * plane : nullptr;
+  const int chunks = (C + 255) / 256;
+  const int nw = R * chunks;
+  const int lane = threadIdx.x & 31;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw;
+       w += (gridDim.x * blockDim.x) >> 5) {
+    const int r = w / chunks, c = (w - r * chunks) * 256 + lane * 8;
+    const bool act = c < C;  // C is a multiple of 8
+    float xr[8], xi[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) xr[q] = xi[q] = 0.f;
+    const size_t g = (size_t)(r0 + r) * PT + c0 + c;
+    const int e0 = r * C + c;
+    if (act) {
+      const float4 a0 = *reinterpret_cast<const float4*>(ire + g);
+      const float4 a1 = *reinterpret_cast<const float4*>(ire + g + 4);
+      const float4 b0 = *reinterpret_cast<const float4*>(iim + g);
+      const float4 b1 = *reinterpret_cast<const float4*>(iim + g + 4);
+      xr[0] = a0.x, xr[1] = a0.y, xr[2] = a0.z, xr[3] = a0.w;
+      xr[4] = a1.x, xr[5] = a1.y, xr[6] = a1.z, xr[7] = a1.w;
+      xi[0] = b0.x, xi[1] = b0.y, xi[2] = b0.z, xi[3] = b0.w;
+      xi[4] = b1.x, xi[5] = b1.y, xi[6] = b1.z, xi[7] = b1.w;
+      if (pre.n) pix_apply_n<8>(pre, k, r0 + r, c0 + c, 0, 1, RT, PT, xr, xi);
+      if (mre) {
+        const float4* m4 = reinterpret_cast<const float4*>(mre + e0);
+        const float4* n4 = reinterpret_cast<const float4*>(mre + plane + e0);
+        const float4 m0 = m4[0], m1 = m4[1], q0 = n4[0], q1 = n4[1];
+        const float mr[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+        const float mi[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float tr = xr[q] * mr[q] - xi[q] * mi[q];
+          xi[q] = xr[q] * mi[q] + xi[q] * mr[q];
+          xr[q] = tr;
+        }
+      }
+    }
+    uint32_t br = 0, bi = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      br = max(br, absbits(xr[q]));
+      bi = max(bi, absbits(xi[q]));
+    }
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      br = max(br, __shfl_xor_sync(0xffffffffu, br, o));
+      bi = max(bi, __shfl_xor_sync(0xffffffffu, bi, o));
+    }
+    if (!act) continue;
+    const Grid gre = grid_of(br), gim = grid_of(bi);
+    uint32_t hr[3][4], hi[3][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      split3_aligned_pair(xr[2 * q], xr[2 * q + 1], gre, hr[0][q], hr[1][q], hr[2][q]);
+      split3_aligned_pair(xi[2 * q], xi[2 * q + 1], gim, hi[0][q], hi[1][q], hi[2][q]);
+    }
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+      __nv_bfloat16* o = out + ((size_t)(f * 3 + p) * 2) * plane + e0;
+      *reinterpret_cast<uint4*>(o) = make_uint4(hr[p][0], hr[p][1], hr[p][2], hr[p][3]);
+      *reinterpret_cast<uint4*>(o + plane) = make_uint4(hi[p][0], hi[p][1], hi[p][2], hi[p][3]);
+    }
+  }
+}
+
 // The GEMM issues a prefix of its fixed product order (tc::term_a, tc::term_b):
 // all six products for bf16x6, the three largest for bf16x3.
 void terms_for(int precision, tc::Params& p) {
   p.n_terms = precision == CSG_PREC_BF16X3 ? 3 : 6;
 }
 
-template <int BN, bool OP_IS_A, int EPI>
+template <int BN, bool OP_IS_A, int EPI, bool HP = false>
 static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Params& p,
                        int grid, cudaStream_t st, const CUtensorMap* o = nullptr) {
-  auto kern = tc::k_split_gemm<BN, OP_IS_A, EPI>;
-  constexpr size_t smem = tc::smem_bytes<BN, EPI>();
+  auto kern = tc::k_split_gemm<BN, OP_IS_A, EPI, HP>;
+  constexpr size_t smem = tc::smem_bytes<BN, EPI, HP>();
   static bool attr_set = false;  // per template instance
   if (!attr_set) {
     CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -301,7 +445,7 @@ int autotune(csg_mft* m, int F) {
   const bool prof = m->ctx->prof;
   m->ctx->prof = false;
   // 256-wide tiles only where the output is at least that wide per component
-  const int n_cand = m->no >= 256 ? 3 : 2;
+  const int n_cand = m->no >= 256 && m->precision != CSG_PREC_HIGH ? 3 : 2;
   m->tuned_ms[2] = 0;
   for (int i = 0; i < n_cand && !rc; ++i) {
     m->bn = cand[i];
@@ -362,8 +506,10 @@ static int create_plan(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int
             "csg_mft_create: non-positive size");
   CSG_CHECK(n_in_x % 8 == 0 && n_in_y % 8 == 0, CSG_E_SHAPE,
             "csg_mft_create: input sizes must be multiples of 8");
-  CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3, CSG_E_ARG,
-            "csg_mft_create: precision must be CSG_PREC_BF16X6 or CSG_PREC_BF16X3");
+  CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3 ||
+                precision == CSG_PREC_HIGH,
+            CSG_E_ARG,
+            "csg_mft_create: precision must be CSG_PREC_BF16X6, CSG_PREC_BF16X3 or CSG_PREC_HIGH");
   for (int s = 0; s < n_slots; ++s)
     CSG_CHECK(lf[s] != 0.0, CSG_E_ARG, "csg_mft_create: zero lambda*f");
   DeviceGuard g(ctx->device);
@@ -409,16 +555,29 @@ static int create_plan(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int
   const int* valid = n_out ? reinterpret_cast<const int*>(dvec + o_valid) : nullptr;
   cudaStream_t st = ctx->stream;
   CSG_CUDA(cudaMemcpyAsync(dvec, h.data(), nvec * sizeof(double), cudaMemcpyHostToDevice, st));
-  // stage-1 operator: rows u (xout), K = x (xin), no prefactor
-  k_build_operator<<<grid_for((long long)n_slots * n_out_x * n_in_x, 256), 256, 0, st>>>(
-      m->op1, dvec + o_xout, dvec + o_xin, n_out_x, n_in_x, n_slots, dvec + o_lf, nullptr, sgn,
-      n_out ? n_out_x : 0, valid);
-  CSG_LAUNCH_CHECK();
+  // stage-1 operator: rows u (xout), K = x (xin), no prefactor;
   // stage-2 operator: rows v (yout), K = y (yin), carries the prefactor
-  k_build_operator<<<grid_for((long long)n_slots * n_out_y * n_in_y, 256), 256, 0, st>>>(
-      m->op2, dvec + o_yout, dvec + o_yin, n_out_y, n_in_y, n_slots, dvec + o_lf,
-      dvec + o_pref, sgn, n_out ? n_out_y : 0, valid);
-  CSG_LAUNCH_CHECK();
+  if (precision == CSG_PREC_HIGH) {
+    k_build_operator_aligned<<<grid_for((long long)n_slots * n_out_x * ((n_in_x + 63) / 64), 8),
+                               256, 0, st>>>(m->op1, dvec + o_xout, dvec + o_xin, n_out_x,
+                                             n_in_x, n_slots, dvec + o_lf, nullptr, sgn,
+                                             n_out ? n_out_x : 0, valid);
+    CSG_LAUNCH_CHECK();
+    k_build_operator_aligned<<<grid_for((long long)n_slots * n_out_y * ((n_in_y + 63) / 64), 8),
+                               256, 0, st>>>(m->op2, dvec + o_yout, dvec + o_yin, n_out_y,
+                                             n_in_y, n_slots, dvec + o_lf, dvec + o_pref, sgn,
+                                             n_out ? n_out_y : 0, valid);
+    CSG_LAUNCH_CHECK();
+  } else {
+    k_build_operator<<<grid_for((long long)n_slots * n_out_x * n_in_x, 256), 256, 0, st>>>(
+        m->op1, dvec + o_xout, dvec + o_xin, n_out_x, n_in_x, n_slots, dvec + o_lf, nullptr, sgn,
+        n_out ? n_out_x : 0, valid);
+    CSG_LAUNCH_CHECK();
+    k_build_operator<<<grid_for((long long)n_slots * n_out_y * n_in_y, 256), 256, 0, st>>>(
+        m->op2, dvec + o_yout, dvec + o_yin, n_out_y, n_in_y, n_slots, dvec + o_lf,
+        dvec + o_pref, sgn, n_out ? n_out_y : 0, valid);
+    CSG_LAUNCH_CHECK();
+  }
   CSG_CUDA(cudaStreamSynchronize(st));
   cudaFree(dvec);
   if (n_out) {  // per-slot output extents, for skipping the all-zero tiles
@@ -488,6 +647,8 @@ int csg_mft_set_tile(csg_mft* m, int bn) {
             "csg_mft_set_tile: width must be 0, 64, 128 or 256");
   CSG_CHECK(bn != 256 || m->no >= 256, CSG_E_ARG,
             "csg_mft_set_tile: 256-wide tiles need at least 256 output columns");
+  CSG_CHECK(bn != 256 || m->precision != CSG_PREC_HIGH, CSG_E_ARG,
+            "csg_mft_set_tile: CSG_PREC_HIGH runs 64- or 128-wide tiles");
   m->bn = bn;
   m->tuned_fields = bn ? -1 : 0;  // -1: fixed by the caller, never retuned
   return CSG_OK;
@@ -515,7 +676,8 @@ size_t csg_mft_workspace_bytes(csg_mft* m, int n_fields) {
 int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n_fields,
                          const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
                          const PixOps& pre, const FieldInfo& fi, const MftWindow* iw,
-                         const MftWindow* ow, const int* in_idx, bool presplit) {
+                         const MftWindow* ow, const int* in_idx, bool presplit,
+                         float* out_lo) {
   CSG_CHECK(ctx && m && in && out && slot, CSG_E_ARG, "csg_mft_execute: null argument");
   CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_mft_execute: n_fields must be positive");
   CSG_CHECK(!in_mul || mul_idx, CSG_E_ARG, "csg_mft_execute: in_mul needs mul_idx");
@@ -538,16 +700,27 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
   const double F = n_fields;
   CSG_CHECK(!presplit || (!in_mul && !pre.n && !iw && !in_idx), CSG_E_ARG,
             "csg_mft_execute: a split input takes no input ops, window or index");
+  const bool hp = m->precision == CSG_PREC_HIGH;
+  CSG_CHECK(!out_lo || (hp && !accumulate), CSG_E_ARG,
+            "csg_mft_execute: a low-order output plane needs CSG_PREC_HIGH and no accumulation");
   if (!presplit) {  // else the producer of the input wrote split_in
     ProfScope ps(ctx, "mft_split", 0, F * m->ny * m->nx * (8.0 + 12.0 + (in_mul ? 8.0 : 0.0)));
     CSG_CHECK(n_fields < 65536, CSG_E_SHAPE, "csg_mft_execute: too many fields in one call");
-    dim3 grid(grid_for((long long)m->ny * m->nx / 8, 256, 1024), n_fields);
-    k_split_field<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, inw.r0, inw.c0, inw.rows,
-                                        inw.pitch, in_mul, mul_idx, pre, fi, in_idx);
+    if (hp) {
+      const long long warps = (long long)m->ny * ((m->nx + 255) / 256);
+      dim3 grid(grid_for(warps, 8, 1024), n_fields);
+      k_split_field_aligned<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, inw.r0, inw.c0,
+                                                  inw.rows, inw.pitch, in_mul, mul_idx, pre, fi,
+                                                  in_idx);
+    } else {
+      dim3 grid(grid_for((long long)m->ny * m->nx / 8, 256, 1024), n_fields);
+      k_split_field<<<grid, 256, 0, st>>>(in, sin, m->ny, m->nx, inw.r0, inw.c0, inw.rows,
+                                          inw.pitch, in_mul, mul_idx, pre, fi, in_idx);
+    }
     CSG_LAUNCH_CHECK();
   }
 
-  const int bn1 = m->bn ? m->bn : 128;
+  const int bn1 = m->bn && !(hp && m->bn == 256) ? m->bn : 128;
   const int kb = bn1 == 256 ? 32 : tc::BK;  // K block of the tile width
   // ---- stage 1: T^T = split(in . B_x^T)^T
   {
@@ -575,9 +748,13 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     // algorithmic work: 8 flops per complex multiply-add of the contraction
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->ny * m->no * m->nx);
-    rc = bn1 == 64    ? launch_gemm<64, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
-         : bn1 == 256 ? launch_gemm<256, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
-                      : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
+    if (hp)
+      rc = bn1 == 64 ? launch_gemm<64, false, tc::EPI_T_SPLIT, true>(ta, tb, p, grid, st)
+                     : launch_gemm<128, false, tc::EPI_T_SPLIT, true>(ta, tb, p, grid, st);
+    else
+      rc = bn1 == 64    ? launch_gemm<64, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
+           : bn1 == 256 ? launch_gemm<256, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st)
+                        : launch_gemm<128, false, tc::EPI_T_SPLIT>(ta, tb, p, grid, st);
     if (rc) return rc;
   }
   // ---- stage 2: out = (pref A_y) . T
@@ -607,6 +784,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.accumulate = accumulate;
     p.status = ctx->status;
     p.valid = m->valid;
+    p.out_lo = out_lo;
     CUtensorMap to;
     p.tma_out = make_map_f32_out(&to, out + (size_t)outw.r0 * outw.pitch + outw.c0, m->no, m->mo,
                                  (long long)n_fields * 2, outw.pitch, outw.rows)
@@ -615,9 +793,13 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     const CUtensorMap* tmo = p.tma_out ? &to : nullptr;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->mo * m->no * m->ny);
-    rc = bn1 == 64    ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo)
-         : bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo)
-                      : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo);
+    if (hp)
+      rc = bn1 == 64 ? launch_gemm<64, true, tc::EPI_F32, true>(ta, tb, p, grid, st, tmo)
+                     : launch_gemm<128, true, tc::EPI_F32, true>(ta, tb, p, grid, st, tmo);
+    else
+      rc = bn1 == 64    ? launch_gemm<64, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo)
+           : bn1 == 256 ? launch_gemm<256, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo)
+                        : launch_gemm<128, true, tc::EPI_F32>(ta, tb, p, grid, st, tmo);
     if (rc) return rc;
   }
   return CSG_OK;
@@ -629,6 +811,8 @@ __nv_bfloat16* csg::mft_split_buffer(csg_mft* m, int n_fields) {
   return static_cast<__nv_bfloat16*>(m->split_in.ptr);
 }
 
+bool csg::mft_is_high(const csg_mft* m) { return m && m->precision == CSG_PREC_HIGH; }
+
 void csg::mft_input_shape(const csg_mft* m, int* ny, int* nx) {
   *ny = m->ny;
   *nx = m->nx;
@@ -639,4 +823,11 @@ extern "C" int csg_mft_execute(csg_ctx* ctx, csg_mft* m, const float* in, float*
                                const int* mul_idx) {
   return mft_execute_ops(ctx, m, in, out, n_fields, slot, accumulate, in_mul, mul_idx, PixOps(),
                          FieldInfo());
+}
+
+extern "C" int csg_mft_execute_lo(csg_ctx* ctx, csg_mft* m, const float* in, float* out,
+                                  float* out_lo, int n_fields, const int* slot) {
+  CSG_CHECK(out_lo, CSG_E_ARG, "csg_mft_execute_lo: null low-order output");
+  return mft_execute_ops(ctx, m, in, out, n_fields, slot, 0, nullptr, nullptr, PixOps(),
+                         FieldInfo(), nullptr, nullptr, nullptr, false, out_lo);
 }

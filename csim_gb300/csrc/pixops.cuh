@@ -249,7 +249,10 @@ struct FresnelArgs {
   double z;
   double ap_rad;
   const float2* H = nullptr;      // optional transfer-function table [slot][N][N]
-  const int* slot = nullptr;      // per field, with H
+  const int* slot = nullptr;      // per field, with H or H4
+  // two-float transfer-function table [slot][N][N] (cos hi, cos lo, sin hi,
+  // sin lo): required by the two-float (CSG_PREC_HIGH) passes
+  const float4* H4 = nullptr;
 };
 
 // Per-wavelength tables, built once per chain in FP64-reduced phases:
@@ -259,6 +262,11 @@ int build_phasor_table(cudaStream_t st, const float* sag, int R, int C, const do
                        int n_slot, double sign, float2* out);
 int build_fresnel_table(cudaStream_t st, int N, const double* lam, int n_slot, double z,
                         double ap_rad, float2* out);
+// The same in FP64, stored two-float (the CSG_PREC_HIGH Fresnel).
+int build_fresnel_table_df(cudaStream_t st, int N, const double* lam, int n_slot, double z,
+                           double ap_rad, float4* out);
+// Two-float copy (low words zero) of an fp32 complex table of n values.
+int table_to_df(cudaStream_t st, const float2* in, float4* out, long long n);
 
 // Band-limited padded transform (with fa only): the n x n field src sits at
 // rows and columns [lo, lo + n) of zero-padded N x N fields. The first row
@@ -285,16 +293,18 @@ struct FftBand {
 // other rows of the field are not read before they are overwritten.
 // split_out (with fa, without band): the last pass also writes the result's
 // three-part bf16 split in the layout of an N x N MFT's input (mft_split_buffer).
+// high: the transforms run in two-float arithmetic (CSG_PREC_HIGH; a Fresnel
+// then reads fa->H4 and split_out is not available).
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi,
                 const FftBand* band = nullptr, const FftBand* support = nullptr,
-                __nv_bfloat16* split_out = nullptr);
+                __nv_bfloat16* split_out = nullptr, bool high = false);
 // Whether fft2d_fused can run an N-point padded transform band-limited to
-// [lo, lo + n).
-bool fft_band_supported(int N, int lo, int n);
+// [lo, lo + n) (fp32 or two-float passes).
+bool fft_band_supported(int N, int lo, int n, bool high = false);
 // Rows [r0, r1) widened to a band fft2d_fused accepts as a row support
 // (false: none).
-bool fft_row_support(int N, int r0, int r1, int* lo, int* n);
+bool fft_row_support(int N, int r0, int r1, int* lo, int* n, bool high = false);
 
 // A window of a field: rows x cols of the transform start at (r0, c0) of
 // planes that are `rows` x `pitch`.
@@ -309,7 +319,10 @@ int mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, int n
                     const int* slot, int accumulate, const float* in_mul, const int* mul_idx,
                     const PixOps& pre, const FieldInfo& fi, const MftWindow* iw = nullptr,
                     const MftWindow* ow = nullptr, const int* in_idx = nullptr,
-                    bool presplit = false);
+                    bool presplit = false, float* out_lo = nullptr);
+// Whether a plan runs at CSG_PREC_HIGH (its input split is exponent-aligned,
+// so a producer must not hand it a plain split).
+bool mft_is_high(const csg_mft* m);
 // The plan's input split buffer, [n_fields][3][2][ny][nx] bf16, grown to
 // n_fields (nullptr: allocation failed). A producer that writes it lets
 // mft_execute_ops run with presplit = true, which skips the split pass.

@@ -55,6 +55,9 @@ struct Params {
   // computed (stage 2 writes their zeros); nullptr: every tile
   const int* valid;
   int* status;
+  // high precision, EPI_F32: the low words of the two-float results, stored
+  // per thread beside `out` (same window and pitch); null: not written
+  float* out_lo;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -246,14 +249,18 @@ constexpr int MAX_PARTS = 3;
 // room for two or three stages, and tensor memory holds one 256-column
 // rotating hi x hi slot beside the small products' slot: hi x hi is
 // committed first, so its drain overlaps the rest of the block.
-template <int BN, int EPI>
+template <int BN, int EPI, bool HP = false>
 struct Cfg {
   static_assert(BN == 64 || BN == 128 || BN == 256, "N tile must be 64, 128 or 256");
+  static_assert(!HP || BN <= 128, "high precision: N tile 64 or 128");
   static constexpr int KB = BN == 256 ? 32 : BK;  // K elements per pipeline stage
   static constexpr uint32_t A_BYTES = BM * KB * 2;
   static constexpr uint32_t B_BYTES = BN * KB * 2;
   static constexpr uint32_t STAGE_BYTES = MAX_PARTS * (A_BYTES + B_BYTES);
-  static constexpr uint32_t STAGING_BYTES = EPI == 1 ? DRAIN_WARPS * 4096 : 0;
+  // fp32 epilogue: 4 KB box per drain warp; high-precision split epilogue:
+  // the per-column group maxima of each warp, double-buffered by tile
+  static constexpr uint32_t STAGING_BYTES =
+      EPI == 1 ? DRAIN_WARPS * 4096 : (HP ? 2 * DRAIN_WARPS * (BN / 2) * 4 : 0);
   // 192 KB (+ 32 KB staging) at N = 128; 216 KB or 144 KB (+ 32 KB) at 64
   // and at 256
   static constexpr int STAGES = BN == 128 ? 2 : (EPI == 1 ? 2 : 3);
@@ -265,9 +272,9 @@ struct Cfg {
   static_assert(SMEM <= 232448, "shared memory per CTA");
 };
 
-template <int BN, int EPI>
+template <int BN, int EPI, bool HP = false>
 constexpr size_t smem_bytes() {
-  return Cfg<BN, EPI>::SMEM;
+  return Cfg<BN, EPI, HP>::SMEM;
 }
 
 // Drain one lane quadrant's CPW columns at taddr into acc (+=).
@@ -282,6 +289,53 @@ __device__ __forceinline__ void drain_add(uint32_t taddr, float* acc) {
 #pragma unroll
     for (int j = 0; j < 64; ++j)
       if (cb + j < CPW) acc[cb + j] += __uint_as_float(r[j]);
+  }
+}
+
+// High precision: each K block's exact hi x hi sum joins a two-float
+// register accumulator (acc, lo) through an error-free TwoSum. The low word
+// only gathers rounding errors of the fp32 word (each below half its ulp),
+// so it is kept in bf16 pairs: its own 2^-9 relative rounding is 2^-33 of
+// the result, and both words of 64 columns fit the drain warps' registers.
+template <int CPW>
+__device__ __forceinline__ void drain_add2(uint32_t taddr, float* acc, __nv_bfloat162* lo) {
+#pragma unroll
+  for (int cb = 0; cb < CPW; cb += 32) {
+    uint32_t r[32];
+    tmem_ld32_nowait(taddr + cb, r);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 32; j += 2) {
+      float s0, e0, s1, e1;
+      two_sum(acc[cb + j], __uint_as_float(r[j]), s0, e0);
+      two_sum(acc[cb + j + 1], __uint_as_float(r[j + 1]), s1, e1);
+      acc[cb + j] = s0;
+      acc[cb + j + 1] = s1;
+      lo[(cb + j) / 2] = __hadd2(lo[(cb + j) / 2], __floats2bfloat162_rn(e0, e1));
+    }
+  }
+}
+
+// The end of a high-precision tile: the smaller products' slot (fp32) and
+// the low words join, and (acc, lo) become the renormalised pair: acc the
+// fp32 rounding of the result, lo the rest.
+template <int CPW>
+__device__ __forceinline__ void drain_final2(uint32_t taddr, float* acc, __nv_bfloat162* lo) {
+#pragma unroll
+  for (int cb = 0; cb < CPW; cb += 32) {
+    uint32_t r[32];
+    tmem_ld32_nowait(taddr + cb, r);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 32; j += 2) {
+      const float2 l = __bfloat1622float2(lo[(cb + j) / 2]);
+      float s0, e0, s1, e1;
+      two_sum(acc[cb + j], __uint_as_float(r[j]) + l.x, s0, e0);
+      two_sum(acc[cb + j + 1], __uint_as_float(r[j + 1]) + l.y, s1, e1);
+      acc[cb + j] = s0;
+      acc[cb + j + 1] = s1;
+      lo[(cb + j) / 2] = __floats2bfloat162_rn(e0, e1);
+    }
   }
 }
 
@@ -358,11 +412,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int BN, bool OP_IS_A, int EPI>
+template <int BN, bool OP_IS_A, int EPI, bool HP = false>
 __global__ void __launch_bounds__(THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const __grid_constant__ CUtensorMap tmO, const Params p) {
-  using CF = Cfg<BN, EPI>;
+  using CF = Cfg<BN, EPI, HP>;
   constexpr int STAGES = CF::STAGES;
   constexpr int NSLOT = CF::NSLOT;  // rotating group-0 slots
   constexpr int CPW = CF::COLS_PER_WARP;
@@ -378,7 +432,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint64_t* gdone = tempty + NSLOT;   // a tile's products all complete (per tile)
   uint64_t* gfree = gdone + 1;        // a tile's persistent slot read (per tile)
   uint64_t* quiesce = gfree + 1;      // abort path: in-flight products done
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(quiesce + 1);
+  uint64_t* pairbar = quiesce + 1;    // HP split epilogue: warp pairs' maxima written (4)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(pairbar + DRAIN_WARPS / 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
@@ -399,6 +454,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     mbar_init(gdone, 1);
     mbar_init(gfree, DRAIN_WARPS);
     mbar_init(quiesce, 1);
+    for (int q = 0; q < DRAIN_WARPS / 2; ++q) mbar_init(&pairbar[q], 64);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -515,13 +571,18 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint8_t* stage_w = staging + warp * 4096;  // this warp's fp32 box
     long long g = 0;
     int j = 0;
+    int xt = 0;  // HP split epilogue: exchanges of group maxima done by this warp
     bool ok = true;
     for (int t = blockIdx.x; t < n_tiles_total && ok; t += gridDim.x) {
       const TileCoord tc = tile_coord<BN, OP_IS_A>(p, t);
       const int field = tc.field, d = tc.d, row_a0 = tc.row_a0, row_b0 = tc.row_b0;
       float acc[CPW];
+      // HP: low words of the two-float accumulators, in pairs (unused otherwise)
+      __nv_bfloat162 lo[HP ? CPW / 2 : 1];
 #pragma unroll
       for (int jj = 0; jj < CPW; ++jj) acc[jj] = 0.f;
+#pragma unroll
+      for (int jj = 0; jj < (HP ? CPW / 2 : 1); ++jj) lo[jj] = __floats2bfloat162_rn(0.f, 0.f);
       // a ragged tile beyond its slot: nothing computed; stage 2 stores zeros
       const bool beyond = tile_beyond<OP_IS_A>(p, tc);
       if (beyond && EPI == EPI_T_SPLIT) continue;
@@ -532,7 +593,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         ok = __all_sync(0xffffffffu, ok && !*abort_flag);
         if (!ok) break;
         tc_fence_after();
-        drain_add<CPW>(t_rot + (uint32_t)(ts * BN) + lane_off, acc);
+        if constexpr (HP)
+          drain_add2<CPW>(t_rot + (uint32_t)(ts * BN) + lane_off, acc, lo);
+        else
+          drain_add<CPW>(t_rot + (uint32_t)(ts * BN) + lane_off, acc);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&tempty[ts]);
@@ -550,13 +614,85 @@ __global__ void __launch_bounds__(THREADS, 1)
         // add the persistent slot of the smaller products, then hand it to
         // the next tile
         tc_fence_after();
-        drain_add<CPW>(t_gs + lane_off, acc);
+        if constexpr (HP)
+          drain_final2<CPW>(t_gs + lane_off, acc, lo);
+        else
+          drain_add<CPW>(t_gs + lane_off, acc);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(gfree);
         ++j;
       }
-      if (EPI == EPI_T_SPLIT) {
+      if (EPI == EPI_T_SPLIT && HP) {
+        // C[y][u] -> T^T parts [field][part][d][u][y] (bf16), split on the
+        // grid of each column's 64-row group (quadrant pair q, q ^ 1): this
+        // warp's per-column maxima go to shared memory, the pair meets at a
+        // bounded barrier, and both take the larger of the two.
+        uint32_t* xown =
+            reinterpret_cast<uint32_t*>(staging) + ((xt & 1) * DRAIN_WARPS + warp) * CPW;
+        const uint32_t* xpar = reinterpret_cast<const uint32_t*>(staging) +
+                               ((xt & 1) * DRAIN_WARPS + (warp ^ 1)) * CPW;
+#pragma unroll
+        for (int jj = 0; jj < CPW; ++jj) {
+          const uint32_t m = __reduce_max_sync(0xffffffffu, absbits(acc[jj]));
+          if (lane == (jj & 31)) xown[jj] = m;
+        }
+        mbar_arrive(&pairbar[warp >> 1]);  // every lane of both warps (release)
+        ok = mbar_wait(&pairbar[warp >> 1], (uint32_t)(xt & 1));
+        ok = __all_sync(0xffffffffu, ok && !*abort_flag);
+        ++xt;
+        if (!ok) {
+          atomicExch(p.status, 4);
+          *abort_flag = 1;
+          break;
+        }
+        const int y = row_a0 + row;
+        if ((p.out_cols & 1) == 0) {
+          __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(p.out);
+          const size_t plane2 = (size_t)p.out_rows * p.out_cols / 2;
+          const int odd = lane & 1;
+          const int ye = y - odd;
+          const int u0 = row_b0 + h * CPW + odd;
+#pragma unroll
+          for (int jj = 0; jj < CPW; jj += 2) {
+            const float recv = __shfl_xor_sync(0xffffffffu, odd ? acc[jj] : acc[jj + 1], 1);
+            const float2 l = __bfloat1622float2(lo[jj / 2]);
+            const float recvl = __shfl_xor_sync(0xffffffffu, odd ? l.x : l.y, 1);
+            const float v0 = odd ? recv : acc[jj], w0 = odd ? recvl : l.x;
+            const float v1 = odd ? acc[jj + 1] : recv, w1 = odd ? l.y : recvl;
+            const int col = jj + odd;
+            const Grid gr = grid_of(max(xown[col], xpar[col]));
+            const int u = u0 + jj;
+            if (ye < p.out_cols && u < p.cols_valid) {
+              __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+              split3_aligned2(v0, w0, gr, a0, a1, a2);
+              split3_aligned2(v1, w1, gr, b0, b1, b2);
+              const size_t off = ((size_t)u * p.out_cols + ye) / 2;
+              out[((size_t)(field * 3 + 0) * 2 + d) * plane2 + off] = __halves2bfloat162(a0, b0);
+              out[((size_t)(field * 3 + 1) * 2 + d) * plane2 + off] = __halves2bfloat162(a1, b1);
+              out[((size_t)(field * 3 + 2) * 2 + d) * plane2 + off] = __halves2bfloat162(a2, b2);
+            }
+          }
+        } else if (y < p.out_cols) {
+          __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+          const size_t plane = (size_t)p.out_rows * p.out_cols;
+          const int u0 = row_b0 + h * CPW;
+#pragma unroll
+          for (int jj = 0; jj < CPW; ++jj) {
+            const int u = u0 + jj;
+            if (u < p.cols_valid) {
+              const Grid gr = grid_of(max(xown[jj], xpar[jj]));
+              const float2 l = __bfloat1622float2(lo[jj / 2]);
+              __nv_bfloat16 h0, h1, h2;
+              split3_aligned2(acc[jj], (jj & 1) ? l.y : l.x, gr, h0, h1, h2);
+              const size_t off = (size_t)u * p.out_cols + y;
+              out[((size_t)(field * 3 + 0) * 2 + d) * plane + off] = h0;
+              out[((size_t)(field * 3 + 1) * 2 + d) * plane + off] = h1;
+              out[((size_t)(field * 3 + 2) * 2 + d) * plane + off] = h2;
+            }
+          }
+        }
+      } else if (EPI == EPI_T_SPLIT) {
         // C[y][u] -> T^T parts [field][part][d][u][y] (bf16)
         const int y = row_a0 + row;
         if ((p.out_cols & 1) == 0) {
@@ -604,6 +740,24 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
           }
         }
+      }
+      if (EPI == EPI_F32 && HP && p.out_lo) {
+        // low words of the two-float results, per thread, beside `out`
+        const int v = row_a0 + row;
+        if (v < p.rows_valid) {
+          float* out = p.out_lo +
+                       ((size_t)(field * 2 + d) * p.out_plane_rows + p.out_r0 + v) * p.out_pitch +
+                       p.out_c0;
+          const int u0 = row_b0 + h * CPW;
+#pragma unroll
+          for (int jj = 0; jj < CPW; jj += 2) {
+            const float2 l = __bfloat1622float2(lo[jj / 2]);
+            if (u0 + jj < p.cols_valid) out[u0 + jj] = l.x;
+            if (u0 + jj + 1 < p.cols_valid) out[u0 + jj + 1] = l.y;
+          }
+        }
+      }
+      if (EPI == EPI_T_SPLIT) {
       } else if (p.tma_out) {
         // Each warp stages its 32 x CPW block one 32 x 32 fp32 box at a time
         // in its own 4 KB of the staging region, in the TMA 128B-swizzled

@@ -90,15 +90,22 @@ class Context:
         call("csg_complex_mask", self.h, ptr(field), F, R, Cc, ptr(amp), ptr(ph), amp.shape[0],
              amp.shape[1])
 
-    def fft2d(self, field, direction=-1):
+    def fft2d(self, field, direction=-1, precision=None):
         F, _, R, Cc = field.shape
         if R != Cc:
             raise ValueError("square fields only")
-        call("csg_fft2d", self.h, ptr(field), F, R, direction)
+        if precision is None:
+            call("csg_fft2d", self.h, ptr(field), F, R, direction)
+        else:
+            call("csg_fft2d_prec", self.h, ptr(field), F, R, direction, int(precision))
 
-    def fresnel(self, field, lam, ap_rad, z):
+    def fresnel(self, field, lam, ap_rad, z, precision=None):
         F, _, R, Cc = field.shape
-        call("csg_fresnel", self.h, ptr(field), F, R, ptr(lam), float(ap_rad), float(z))
+        if precision is None:
+            call("csg_fresnel", self.h, ptr(field), F, R, ptr(lam), float(ap_rad), float(z))
+        else:
+            call("csg_fresnel_prec", self.h, ptr(field), F, R, ptr(lam), float(ap_rad), float(z),
+                 int(precision))
 
     def hex_mask(self, hex_id, count, n_sub, sags, cand, lam, phase_sign=1.0, flip=True,
                  subtract=1.0, use_only_hex=-1, out=None):
@@ -161,6 +168,15 @@ class Mft:
         call("csg_mft_execute", self.ctx.h, self.h, ptr(field_in), ptr(out), F, ptr(slot),
              int(accumulate), ptr(in_mul), ptr(mul_idx))
         return out
+
+    def execute_lo(self, field_in, slot):
+        """CSG_PREC_HIGH plans: (out, out_lo), the two-float transform."""
+        F = field_in.shape[0]
+        out = torch.empty((F, 2) + self.shape_out, dtype=torch.float32, device=field_in.device)
+        lo = torch.empty_like(out)
+        call("csg_mft_execute_lo", self.ctx.h, self.h, ptr(field_in), ptr(out), ptr(lo), F,
+             ptr(slot))
+        return out, lo
 
     def close(self):
         if self.h:

@@ -48,6 +48,14 @@ extern "C" {
  * x1y1 + x1y2 + x2y1 (about 2^-16 relative error per product). */
 #define CSG_PREC_BF16X6 6
 #define CSG_PREC_BF16X3 3
+/* High precision: the six products of an exponent-aligned split (all values
+ * of a 64-wide K group of an operand row share one power-of-two grid, so
+ * every tensor-core sum of the leading products is exact) with compensated
+ * two-float accumulation across K groups; in a chain, the Fresnel and
+ * padded-FFT passes also run in double-float arithmetic, and the final
+ * image carries a low-order plane (csg_chain_image_lo). Peak-normalised
+ * field errors against FP64 at the 1e-8 level instead of the 1e-7 level. */
+#define CSG_PREC_HIGH 16
 
 typedef struct csg_ctx csg_ctx;
 typedef struct csg_mft csg_mft;
@@ -140,12 +148,22 @@ int csg_complex_mask(csg_ctx* ctx, float* field, int n_fields, int rows, int col
  * :127, :192-193): forward exp(-i), inverse exp(+i) divided by N^2.
  * N is a power of two, 64 <= N <= 4096. direction: -1 forward, +1 inverse. */
 int csg_fft2d(csg_ctx* ctx, float* field, int n_fields, int n, int direction);
+/* csg_fft2d with a precision: CSG_PREC_HIGH runs the passes in two-float
+ * arithmetic (about 48-bit intermediates; fields stay fp32 in memory). */
+int csg_fft2d_prec(csg_ctx* ctx, float* field, int n_fields, int n, int direction,
+                   int precision);
 /* fresnelPropagateAS::execute (csim_fft.cpp:371-392): per field
  * E <- IFFT(FFT(E) exp(i 2 pi / lambda_f z sqrt(1 - (lambda_f/apRad)^2 H / 4))),
  * H = fftshifted integer frequency index squared. One fused pipeline:
  * row FFT, column FFT x transfer x column IFFT, row IFFT. */
 int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
                 double ap_rad, double z);
+/* csg_fresnel with a precision: CSG_PREC_HIGH evaluates the transfer function
+ * in FP64 and runs the three passes in two-float arithmetic (fields stay fp32
+ * in memory); it allocates a per-call table of n_fields * n^2 * 16 bytes and
+ * returns after the work is done. Other precisions are csg_fresnel. */
+int csg_fresnel_prec(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
+                     double ap_rad, double z, int precision);
 
 /* ------------------------------------------------------------------ MFT */
 /* Matrix Fourier transform plan: the reference's zoomFft (csim_fft.cpp:
@@ -181,6 +199,12 @@ int csg_mft_destroy(csg_mft* plan);
  * fpmPupToLyot). */
 int csg_mft_execute(csg_ctx* ctx, csg_mft* plan, const float* in, float* out, int n_fields,
                     const int* slot, int accumulate, const float* in_mul, const int* mul_idx);
+/* csg_mft_execute of a CSG_PREC_HIGH plan that also stores the low-order
+ * words of its two-float results: the transform is out + out_lo (both
+ * [F][2][n_out_y][n_out_x] fp32), about 2^-24 closer to exact than out
+ * alone. No accumulation or input multiplier. */
+int csg_mft_execute_lo(csg_ctx* ctx, csg_mft* plan, const float* in, float* out, float* out_lo,
+                       int n_fields, const int* slot);
 /* Bytes of device scratch the plan uses for n_fields (informational). */
 size_t csg_mft_workspace_bytes(csg_mft* plan, int n_fields);
 
