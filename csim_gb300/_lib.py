@@ -108,6 +108,7 @@ SIGNATURES = {
     "csg_chain_sags": ([P, I, I, C.POINTER(P)], None),
     "csg_chain_execute": ([P, I, I], None),
     "csg_chain_image": ([P, C.POINTER(P), C.POINTER(I)], None),
+    "csg_chain_image_lo": ([P, C.POINTER(P)], None),
     "csg_chain_field": ([P, C.POINTER(P)], None),
     "csg_mft_reserve": ([P, I], None),
     "csg_mft_set_tile": ([P, I], None),

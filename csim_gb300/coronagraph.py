@@ -335,6 +335,17 @@ class Coronagraph:
         call("csg_chain_image", self.h, C.byref(p), C.byref(n))
         return _tensor_from_ptr(p.value, (self.n_fields, 2, n.value, n.value), torch.float32)
 
+    def image_lo(self):
+        """CSG_PREC_HIGH chains: the low-order words of the last image (the
+        image is execute() + image_lo()); None at other precisions."""
+        p = C.c_void_p()
+        n = C.c_int()
+        call("csg_chain_image", self.h, C.byref(C.c_void_p()), C.byref(n))
+        call("csg_chain_image_lo", self.h, C.byref(p))
+        if not p.value:
+            return None
+        return _tensor_from_ptr(p.value, (self.n_fields, 2, n.value, n.value), torch.float32)
+
     def close(self):
         if self.h:
             call("csg_chain_destroy", self.h)

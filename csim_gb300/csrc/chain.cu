@@ -117,6 +117,8 @@ struct Elem {
   float* cmask = nullptr;
   // per-wavelength tables (mirror phasors, Fresnel transfer function)
   float2* tab = nullptr;
+  // CSG_PREC_HIGH: the transfer function (Fresnel, padded-FFT mask) two-float
+  float4* tab4 = nullptr;
   // mirror right after a real mask: the mask times the phasor table
   float2* tab_m = nullptr;
   // real mask: bounding box [sr0, sr1) x [sc0, sc1) of its nonzero pixels
@@ -159,10 +161,11 @@ struct csg_chain {
   float* fpm_mask = nullptr;    // [F][2][S][S]
   float2* phasors = nullptr;    // [F][n_hex+1]
   float* image = nullptr;       // [F][2][n_out][n_out]
+  float* image_lo = nullptr;    // CSG_PREC_HIGH: low-order words of the image
   float* padbuf = nullptr;      // [F][2][P][P] (padded-FFT focal-plane masks)
   double* sags = nullptr;       // [n_cand][n_hex]
   int n_cand = 0, sag_hex = 0;
-  size_t fpm_cap = 0, img_cap = 0, ph_cap = 0, pad_cap = 0;
+  size_t fpm_cap = 0, img_cap = 0, ph_cap = 0, pad_cap = 0, img_lo_cap = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_calib = -1;
@@ -198,6 +201,9 @@ int csg_chain_create(csg_ctx* ctx, csg_chain** out, int n, double pixel_scale, i
   CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
             "csg_chain_create: the field must be N x N with N a power of two in [64, 4096]");
   CSG_CHECK(n_lambda > 0 && pixel_scale > 0, CSG_E_ARG, "csg_chain_create: bad parameters");
+  CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3 ||
+                precision == CSG_PREC_HIGH,
+            CSG_E_ARG, "csg_chain_create: precision must be a CSG_PREC_* value");
   csg_chain* c = new csg_chain();
   c->ctx = ctx;
   c->n = n;
@@ -229,6 +235,7 @@ int csg_chain_destroy(csg_chain* c) {
     cudaFree(e.hex_id);
     cudaFree(e.count);
     cudaFree(e.tab);
+    cudaFree(e.tab4);
     cudaFree(e.tab_m);
     cudaFree(e.dmask);
     cudaFree(e.cmask);
@@ -239,7 +246,8 @@ int csg_chain_destroy(csg_chain* c) {
   }
   for (void* p : {(void*)c->slot, (void*)c->lam_f, (void*)c->amp, (void*)c->tip, (void*)c->tilt,
                   (void*)c->cand, (void*)c->ident, (void*)c->field, (void*)c->fpm,
-                  (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->sags,
+                  (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->image_lo,
+                  (void*)c->sags,
                   (void*)c->lam_slots, (void*)c->padbuf})
     cudaFree(p);
   delete c;
@@ -332,7 +340,21 @@ int csg_chain_add_fresnel(csg_chain* c, double z, double ap_rad) {
   e.tab = dev_copy<float2>(nullptr, (size_t)c->n * c->n * c->n_lambda, c->ctx->stream);
   CSG_CHECK(e.tab, CSG_E_NOMEM, "csg_chain_add_fresnel: allocation failed");
   int rc = build_fresnel_table(c->ctx->stream, c->n, c->lam_slots, c->n_lambda, z, ap_rad, e.tab);
-  if (rc) return rc;
+  if (!rc && c->precision == CSG_PREC_HIGH) {
+    e.tab4 = dev_copy<float4>(nullptr, (size_t)c->n * c->n * c->n_lambda, c->ctx->stream);
+    if (!e.tab4) {
+      cudaFree(e.tab);
+      set_error("csg_chain_add_fresnel: allocation failed");
+      return CSG_E_NOMEM;
+    }
+    rc = build_fresnel_table_df(c->ctx->stream, c->n, c->lam_slots, c->n_lambda, z, ap_rad,
+                                e.tab4);
+  }
+  if (rc) {
+    cudaFree(e.tab);
+    cudaFree(e.tab4);
+    return rc;
+  }
   c->elems.push_back(e);
   c->planned = false;
   drop_graph(c);
@@ -672,6 +694,20 @@ int csg_chain_add_fft_fpm(csg_chain* c, int pad, const float* mask_re, const flo
       }
   e.tab = dev_copy(h.data(), h.size(), c->ctx->stream);
   CSG_CHECK(e.tab, CSG_E_NOMEM, "csg_chain_add_fft_fpm: allocation failed");
+  if (c->precision == CSG_PREC_HIGH) {  // the two-float passes read a two-float table
+    e.tab4 = dev_copy<float4>(nullptr, h.size(), c->ctx->stream);
+    if (!e.tab4) {
+      cudaFree(e.tab);
+      set_error("csg_chain_add_fft_fpm: allocation failed");
+      return CSG_E_NOMEM;
+    }
+    const int rc4 = table_to_df(c->ctx->stream, e.tab, e.tab4, (long long)h.size());
+    if (rc4) {
+      cudaFree(e.tab);
+      cudaFree(e.tab4);
+      return rc4;
+    }
+  }
   if (c->fft_fpm_babinet) {
     // Babinet form: E - crop(ifft((1 - M) fft(embed(E)))). Where 1 - M has a
     // small support only those frequencies enter, and both transforms are
@@ -1050,6 +1086,7 @@ static int prepare(csg_chain* c) {
   if (!rc) rc = ensure_buf(&c->fpm_mask, mask_cap, fpm_need);
   if (!rc) rc = ensure_buf(reinterpret_cast<float**>(&c->phasors), c->ph_cap, ph_need);
   if (!rc) rc = ensure_buf(&c->image, c->img_cap, img_need);
+  if (!rc && c->precision == CSG_PREC_HIGH) rc = ensure_buf(&c->image_lo, c->img_lo_cap, img_need);
   if (!rc) rc = ensure_buf(&c->padbuf, c->pad_cap, pad_need);
   return rc;
 }
@@ -1195,18 +1232,20 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
         rc = pixops_pass(ctx->stream, c->field, F, n, n, s.pro, fi);
         break;
       case Step::FRESNEL: {
-        FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad, s.e->tab, c->slot};
+        const bool high = c->precision == CSG_PREC_HIGH;
+        FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad, s.e->tab, c->slot, s.e->tab4};
         FftBand sup;  // rows a mask left nonzero, widened to the transform's row groups
         __nv_bfloat16* split = nullptr;
         if (s.split_to) {
           split = mft_split_buffer(s.split_to, F);
           CSG_CHECK(split, CSG_E_NOMEM, "Fresnel: FPM operand buffer allocation failed");
         }
-        if (fft_row_support(n, s.sup0, std::min(s.sup1, n), &sup.lo, &sup.n) && sup.n < n)
-          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, &sup, split);
+        if (fft_row_support(n, s.sup0, std::min(s.sup1, n), &sup.lo, &sup.n, high) && sup.n < n)
+          rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, &sup, split,
+                           high);
         else
           rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, nullptr,
-                           split);
+                           split, high);
         break;
       }
       case Step::FPM: {
@@ -1236,7 +1275,8 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
       }
       case Step::FINAL:
         rc = mft_execute_ops(ctx, s.e->mft, c->field, c->image, F, c->slot, 0, nullptr, nullptr,
-                             s.pro, fi, &s.e->win, nullptr);
+                             s.pro, fi, &s.e->win, nullptr, nullptr, false,
+                             c->precision == CSG_PREC_HIGH ? c->image_lo : nullptr);
         break;
       case Step::FPM_DOUBLE: {
         const Elem& e = *s.e;
@@ -1276,9 +1316,10 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
                                  PixOps(), fi, nullptr, &e.win);
           break;
         }
-        FresnelArgs fa{c->lam_f, 0.0, 1.0, e.tab, c->slot};  // H = the mask table
+        const bool high = c->precision == CSG_PREC_HIGH;
+        FresnelArgs fa{c->lam_f, 0.0, 1.0, e.tab, c->slot, e.tab4};  // H = the mask table
         const int lo = (e.P - n) / 2;
-        if (fft_band_supported(e.P, lo, n)) {
+        if (fft_band_supported(e.P, lo, n, high)) {
           // only the n rows that hold the field are transformed; the padding
           // is generated in registers and the crop is the last pass's store
           rc = pixops_pass(ctx->stream, c->field, F, n, n, s.pro, fi);
@@ -1288,10 +1329,13 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
           band.src = c->field;
           band.dst = c->field;
           if (!rc)
-            rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi, &band);
+            rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi, &band,
+                             nullptr, nullptr, high);
         } else {
           rc = pad_center_pass(ctx->stream, c->field, c->padbuf, F, n, e.P, s.pro, fi);
-          if (!rc) rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi);
+          if (!rc)
+            rc = fft2d_fused(ctx, c->padbuf, F, e.P, -1, &fa, PixOps(), PixOps(), fi, nullptr,
+                             nullptr, nullptr, high);
           if (!rc) rc = crop_center_pass(ctx->stream, c->padbuf, c->field, F, n, e.P);
         }
         break;
@@ -1578,6 +1622,14 @@ int csg_chain_image(csg_chain* c, float** dev_image, int* n_out) {
   *n_out = 0;
   for (auto& e : c->elems)
     if (e.kind == E_FRAUNHOFER) *n_out = e.n_out;
+  return CSG_OK;
+}
+
+// CSG_PREC_HIGH chains: the low-order words of the final image (the image
+// is image + image_lo); null at other precisions.
+int csg_chain_image_lo(csg_chain* c, float** dev_image_lo) {
+  CSG_CHECK(c && dev_image_lo, CSG_E_ARG, "csg_chain_image_lo: null argument");
+  *dev_image_lo = c->precision == CSG_PREC_HIGH ? c->image_lo : nullptr;
   return CSG_OK;
 }
 

@@ -11,7 +11,7 @@ import ctypes as C
 import numpy as np
 import torch
 
-from ._lib import CSG_PREC_BF16X6, CsgError, call  # noqa: F401
+from ._lib import CSG_PREC_BF16X6, CSG_PREC_HIGH, CsgError, call  # noqa: F401
 
 
 def ptr(t: torch.Tensor | None) -> int | None:

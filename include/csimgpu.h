@@ -391,6 +391,10 @@ int csg_chain_response(csg_chain* chain, int fpm_index, const int* pix_idx, int 
 /* Device pointers to the final image fields [F][2][n_out][n_out] and to the
  * working pupil-plane fields [F][2][N][N]. */
 int csg_chain_image(csg_chain* chain, float** dev_image, int* n_out);
+/* CSG_PREC_HIGH chains: the low-order words of the final image, same layout
+ * (the image is image + image_lo to ~2^-33 of its values); NULL at other
+ * precisions. */
+int csg_chain_image_lo(csg_chain* chain, float** dev_image_lo);
 int csg_chain_field(csg_chain* chain, float** dev_field);
 /* Pre-size an MFT plan's scratch for n_fields (so graph capture allocates
  * nothing) and autotune its tensor-core tile width (128 or 64 output

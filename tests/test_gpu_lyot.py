@@ -18,11 +18,14 @@ def _cplx(t):
     return t[:, 0].double().cpu().numpy() + 1j * t[:, 1].double().cpu().numpy()
 
 
-@pytest.mark.parametrize("full,babinet", [(False, True), (False, False), (True, True),
-                                          (True, False)])
-def test_plain_lyot_matches_oracle(ctx, full, babinet):
+@pytest.mark.parametrize("full,babinet,precision",
+                         [(False, True, 6), (False, False, 6), (True, True, 6), (True, False, 6),
+                          (False, False, 16), (True, True, 16), (True, False, 16)])
+def test_plain_lyot_matches_oracle(ctx, full, babinet, precision):
     """Both forms of the occulter: the Babinet pair of MFTs over the support
-    of 1 - M (the default for a compact occulter) and the padded FFT."""
+    of 1 - M (the default for a compact occulter) and the padded FFT.
+    precision 16 (CSG_PREC_HIGH, image + its low-order plane): fields within
+    1e-7 of the calibration peak."""
     from csim_gb300 import coronagraph as cg
     from csim_gb300 import workloads as W
     if full:
@@ -32,11 +35,18 @@ def test_plain_lyot_matches_oracle(ctx, full, babinet):
         spec = W.PlainLyotSpec(n=128, pad=512, radius_px=50.0, wavelengths=(530e-9, 570e-9),
                                n_out_fov=16.0)
         sources = [cg.PointSource(1.0, 0.0, 0.0), cg.PointSource(0.5, 0.3, -0.2)]
-    cor, inp = W.build_plain_lyot(ctx, spec, sources, fft_fpm_babinet=babinet)
+    cor, inp = W.build_plain_lyot(ctx, spec, sources, precision=precision,
+                                  fft_fpm_babinet=babinet)
     F = cor.batch_all(1)
-    img_t = cor.execute(calibrating=False).clone()
-    img = _cplx(img_t)
-    cal = _cplx(cor.execute(calibrating=True).clone())
+    high = precision == 16
+
+    def run(calibrating):
+        t = cor.execute(calibrating=calibrating).clone()
+        full = t.double() + (cor.image_lo().double() if high else 0.0)
+        return t, full[:, 0].cpu().numpy() + 1j * full[:, 1].cpu().numpy()
+
+    img_t, img = run(False)
+    _, cal = run(True)
     ctx.sync()
     li, amp, tip, tilt, _ = cor._batch
     refs, rcal = [], []
@@ -56,10 +66,11 @@ def test_plain_lyot_matches_oracle(ctx, full, babinet):
     rfull = (np.abs(np.array(refs)) ** 2).sum(0)
     rmax = (np.abs(np.array(rcal)) ** 2).sum(0).max()
     ref_con = oe.region_contrast(rfull, np.full_like(rfull, rmax), reg.mask)
-    print(f"\nplain Lyot n={spec.n} babinet={babinet}: calibration field {e_cal:.3e}, final "
-          f"field {e_img:.3e} (of the calibration peak), contrast "
+    print(f"\nplain Lyot n={spec.n} babinet={babinet} precision {precision}: calibration field "
+          f"{e_cal:.3e}, final field {e_img:.3e} (of the calibration peak), contrast "
           f"{abs(con - ref_con) / ref_con:.3e} relative")
-    assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
+    bound = 1e-7 if high else 1e-6
+    assert e_cal < bound and e_img < bound, (e_cal, e_img)
     assert abs(con - ref_con) / ref_con < 0.01, (con, ref_con)
     assert ref_con < 1e-2  # the occulter and stop do suppress the star
     cor.close()
