@@ -48,9 +48,10 @@ def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
             p = json.load(fh)
-        return float(p["hbm_gbs"]), float(p["bf16_tflops_sustained"]), "measured"
+        # the dominant GEMM is timed within a ~5 ms step: the burst figure applies
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
     except Exception:
-        return 6800.0, 1700.0, "fallback"
+        return 6800.0, 1900.0, "fallback"
 
 
 class ClockSampler:
@@ -501,11 +502,11 @@ def main():
         gemm_tflops = g["flops"] / (g["ms"] / 1e3) / 1e12
         roofline = {"bound": "tensor", "kernel": "k_split_gemm (tcgen05 split-bf16 MFT)",
                     "achieved": gemm_tflops, "peak": tc_peak, "unit": "TFLOP/s",
-                    "frac": gemm_tflops / tc_peak, "peak_kind": f"{peak_kind} bf16 sustained",
+                    "frac": gemm_tflops / tc_peak, "peak_kind": f"{peak_kind} bf16 burst",
                     "traffic": TRAFFIC_PER_FIELD * B if args.workload == "piaacmc" else None,
                     "algorithmic_flops_per_launch": g["flops"] / g["count"],
                     "avg_launch_ms": g["ms"] / g["count"],
-                    "executed_bf16_tflops": gemm_tflops * args.precision,
+                    "executed_bf16_tflops": gemm_tflops * (3 if args.precision == 3 else 6),
                     "share_of_step": g["ms"] / total_ms if total_ms else None}
     else:  # the padded-FFT occulter passes dominate
         fz = prof.get("fresnel_3pass", {"count": 1, "ms": float("nan"), "bytes": 0.0})
@@ -542,7 +543,7 @@ def main():
     line = {"metric": "field propagations/s", "value": value, "unit": "fields/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 fields, bf16x%d-split tensor-core MFT, f64 phases" % args.precision,
+            "dtype": PREC_DTYPE.get(args.precision, str(args.precision)),
             "data": "synthetic (seeded)",
             "config": wl.config,
             "e2e": {"value": e2e_value, "unit": "fields/s", "h2d_bytes_per_step": h2d,
@@ -551,6 +552,9 @@ def main():
             "roofline": roofline, "clocks": clk, "cpu_baseline": cpu}
     if fp64 is not None:
         line["fp64_gpu_path"] = fp64
+    if rank == 0 and ws == 1 and args.workload == "piaacmc" and args.precision != 16 \
+            and not args.no_cpu:
+        line["high_precision"] = high_precision_leg(args, ctx, stream, W, cg, wl, value)
     if wl.reg is not None:
         line["contrast_sample"] = float(contrast[0].item())
     if rank == 0:
@@ -558,6 +562,57 @@ def main():
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+PREC_DTYPE = {
+    6: "f32 fields, bf16x6-split tensor-core MFT, f64 phases",
+    3: "f32 fields, bf16x3-split tensor-core MFT, f64 phases",
+    16: "f32 fields, exponent-aligned bf16x6 MFT (exact tensor sums, two-float accumulation), "
+        "two-float FFT/Fresnel passes, f64 phases, two-float image",
+}
+
+
+def high_precision_leg(args, ctx, stream, W, cg, wl, fast_value):
+    """The same PIAACMC workload at CSG_PREC_HIGH: device-timed fields/s over
+    the same number of steps, and the final-field error of the first field
+    (on-axis, candidate 0) of both modes against the plain FP64 GPU path
+    (complex128 cuFFT / ZGEMM, equal to the FP64 oracle to 1e-10),
+    peak-normalised to that path's calibration image peak."""
+    import copy
+    import torch
+    from baseline.fp64_gpu import Fp64Piaacmc
+    a2 = copy.copy(args)
+    a2.precision = 16
+    with torch.cuda.stream(stream):
+        hw = SETUP["piaacmc"](a2, ctx, W, cg, 0)
+        for _ in range(args.warmup):
+            hw.cor.execute(calibrating=False, use_graph=True)
+        ctx.sync()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            hw.cor.execute(calibrating=False, use_graph=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        # field 0 of each mode against the FP64 GPU path
+        img_f = wl.cor.execute(calibrating=False, use_graph=False)[0].double()
+        img_h = hw.cor.execute(calibrating=False, use_graph=False)[0].double() + \
+            hw.cor.image_lo()[0].double()
+        ctx.sync()
+    ref = Fp64Piaacmc(hw.inp, hw.spec)
+    sags0 = hw.host_in[0].to("cuda")
+    e_ref = ref.field(0, 1.0, sags0)
+    peak = ref.field(0, 1.0, sags0, calibrating=True).abs().max().item()
+    err = lambda t: ((torch.complex(t[0], t[1]) - e_ref).abs().max() / peak).item()  # noqa: E731
+    value = hw.B * args.steps / (ms / 1e3)
+    out = {"value": value, "unit": "fields/s", "ms_per_step": ms / args.steps,
+           "relative_to_default": value / fast_value, "dtype": PREC_DTYPE[16],
+           "field_error_vs_fp64": {"default": err(img_f), "high": err(img_h),
+                                   "normalisation": "calibration image peak, field 0"}}
+    hw.cor.close()
+    return out
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per k_split_gemm launch,
