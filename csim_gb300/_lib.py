@@ -82,7 +82,8 @@ SIGNATURES = {
     "csg_chain_add_complex_mask": ([P, P, P, I, I, I], None),
     "csg_chain_add_fpm_hex": ([P, P, P, I, I, I, D, D, D, D, D, D, I], None),
     "csg_chain_add_fpm_hex_double": ([P, P, P, I, I, I, D, D, D, D, I], None),
-    "csg_chain_add_fpm_mask": ([P, P, P, I, I, I, D, P, D, D, I, P, P, I], None),
+    "csg_chain_add_fpm_mask": ([P, P, P, I, I, I, I, D, P, D, D, I, P, P, I], None),
+    "csg_chain_set_reference_calibration": ([P, I], None),
     "csg_chain_add_fpm_double_mask": ([P, P, P, I, I, P, D, D, I], None),
     "csg_chain_add_fraunhofer": ([P, I, D, D], None),
     "csg_chain_add_fft_fpm": ([P, I, P, P, I], None),

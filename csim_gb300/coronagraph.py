@@ -58,9 +58,11 @@ class ComplexMask:
 @dataclass
 class FpmPupToLyotMask:
     """fpmPupToLyot with a fixed mask (fpmCMCForPupToLyot, fpmBinaryForPupToLyot):
-    complex mask [n_mask][rows][cols] (or 2-D) of pixel pixelScale (metres),
-    lambdaFocalLength per wavelength (with fRatioSign), doBabinet; calibMask
-    (None: ones) is what the calibration walk applies when disabled for it."""
+    complex mask cube [n_mask][rows][cols] (or 2-D) of pixel pixelScale
+    (metres), of which slice maskIndex (-1: the first) is applied at every
+    wavelength as the reference does; lambdaFocalLength per wavelength (with
+    fRatioSign), doBabinet; calibMask [rows][cols] (None: ones) is what the
+    calibration walk applies when disabled for it."""
     mask: np.ndarray
     pixelScale: float
     lambdaFocalLength: np.ndarray
@@ -69,6 +71,7 @@ class FpmPupToLyotMask:
     doBabinet: bool = True
     calibMask: np.ndarray | None = None
     disableForCalibration: bool = True
+    maskIndex: int = -1
 
 
 @dataclass
@@ -76,12 +79,15 @@ class DoubleFraunhoferFPM:
     """doubleFraunhoferFPM: zoom FFT to a padFactor N grid whose pixel is
     2 (beamRadius / (pixelScale N zoomFactor)) lambda 80 for each wavelength,
     the fixed complex mask on its centred block, zoom FFT back (lambda f =
-    +-3.52 lambda)."""
+    +-3.52 lambda). mask: [rows][cols] or the reference's cube
+    [n_slices][rows][cols], of which slice maskIndex (-1: the first) is used
+    (doubleFraunhoferFPM.cpp:86-95)."""
     mask: np.ndarray
     zoomFactor: float
     padFactor: float = 2.0
     disableForCalibration: bool = True
     lambdaFocalFactor: float = 3.52  # doubleFraunhoferFPM.cpp:44-45
+    maskIndex: int = -1
 
 
 @dataclass
@@ -171,7 +177,7 @@ class Coronagraph:
 
     def __init__(self, ctx: Context, tel: Telescope, ef: EField, elements: list,
                  precision: int = CSG_PREC_BF16X6, support_crop: bool = True,
-                 fft_fpm_babinet: bool = True):
+                 fft_fpm_babinet: bool = True, reference_calibration: bool = False):
         self.ctx, self.tel, self.ef, self.elements = ctx, tel, ef, elements
         lam = np.ascontiguousarray(ef.wavelengths, dtype=np.float64)
         h = C.c_void_p()
@@ -180,6 +186,9 @@ class Coronagraph:
         self.h = h
         call("csg_chain_set_support_crop", self.h, int(support_crop))
         call("csg_chain_set_fft_fpm_babinet", self.h, int(fft_fpm_babinet))
+        # fixed-mask FPMs without Babinet: calibrate only the first wavelength,
+        # as the reference's compute-once calibration transform does
+        call("csg_chain_set_reference_calibration", self.h, int(reference_calibration))
         self.n_hex = None
         self.n_out = None
         self.out_pixel = None
@@ -217,15 +226,19 @@ class Coronagraph:
             cre = cim = None
             if e.calibMask is not None:
                 cm = np.asarray(e.calibMask)
-                cm = cm[None] if cm.ndim == 2 else cm
-                assert cm.shape == m.shape, "calibMask must have the mask's shape"
+                if cm.shape != m.shape[1:]:
+                    raise ValueError("calibMask must be [rows][cols] of the mask")
                 cre, cim = _f32(cm.real), _f32(cm.imag)
             ptr = lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None  # noqa: E731
-            call("csg_chain_add_fpm_mask", self.h, ptr(re), ptr(im), m.shape[0], m.shape[1],
-                 m.shape[2], e.pixelScale, ptr(lf), e.fRatioSign, e.zoomFftSign,
+            call("csg_chain_add_fpm_mask", self.h, ptr(re), ptr(im), m.shape[0], int(e.maskIndex),
+                 m.shape[1], m.shape[2], e.pixelScale, ptr(lf), e.fRatioSign, e.zoomFftSign,
                  int(e.doBabinet), ptr(cre), ptr(cim), int(e.disableForCalibration))
         elif isinstance(e, DoubleFraunhoferFPM):
             m = np.asarray(e.mask)
+            if m.ndim == 3:
+                m = m[max(int(e.maskIndex), 0)]
+            if m.ndim != 2:
+                raise ValueError("doubleFraunhoferFPM mask must be [rows][cols] or a cube")
             re, im = _f32(m.real), _f32(m.imag)
             ef = self.ef
             zpx = np.ascontiguousarray(

@@ -144,6 +144,9 @@ struct csg_chain {
   int precision = 6;
   bool crop_support = true;
   bool fft_fpm_babinet = true;  // padded-FFT occulters in Babinet form when compact
+  // fixed-mask FPMs without Babinet: calibrate the first wavelength only, as
+  // the reference's compute-once calibration hat does
+  bool ref_calibration = false;
   bool planned = false;  // lazily built transforms are up to date
   std::vector<Elem> elems;
   // batch description (device)
@@ -204,6 +207,8 @@ int csg_chain_create(csg_ctx* ctx, csg_chain** out, int n, double pixel_scale, i
   CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3 ||
                 precision == CSG_PREC_HIGH,
             CSG_E_ARG, "csg_chain_create: precision must be a CSG_PREC_* value");
+  CSG_CHECK(all_finite(lambda, n_lambda) && all_finite(&pixel_scale, 1), CSG_E_NAN,
+            "csg_chain_create: non-finite wavelength or pixel scale");
   csg_chain* c = new csg_chain();
   c->ctx = ctx;
   c->n = n;
@@ -332,6 +337,8 @@ int csg_chain_add_mirror(csg_chain* c, const float* sag, double sign) {
 // it on every call, csim_fft.cpp:386).
 int csg_chain_add_fresnel(csg_chain* c, double z, double ap_rad) {
   CSG_CHECK(c && ap_rad > 0, CSG_E_ARG, "csg_chain_add_fresnel: bad argument");
+  CSG_CHECK(all_finite(&z, 1) && all_finite(&ap_rad, 1), CSG_E_NAN,
+            "csg_chain_add_fresnel: non-finite distance or aperture radius");
   DeviceGuard g(c->ctx->device);
   Elem e;
   e.kind = E_FRESNEL;
@@ -475,16 +482,22 @@ int csg_chain_add_fpm_hex(csg_chain* c, const int16_t* hex_id, const uint16_t* c
 // fpmPupToLyot.cpp:303-367, 521-557): the hex element's transform pair with
 // the mask uploaded once per wavelength instead of built from sags.
 int csg_chain_add_fpm_mask(csg_chain* c, const float* mask_re, const float* mask_im, int n_mask,
-                           int rows, int cols, double mask_pixel, const double* lf,
+                           int mask_index, int rows, int cols, double mask_pixel, const double* lf,
                            double f_ratio_sign, double zoom_fft_sign, int babinet,
                            const float* calib_re, const float* calib_im,
                            int disable_for_calibration) {
   CSG_CHECK(c && mask_re && lf, CSG_E_ARG, "csg_chain_add_fpm_mask: null argument");
   const int n = c->n, L = c->n_lambda;
-  CSG_CHECK(rows >= 8 && cols >= 8 && rows % 8 == 0 && cols % 8 == 0 &&
-                (n_mask == 1 || n_mask == L) && mask_pixel > 0.0,
+  CSG_CHECK(rows >= 8 && cols >= 8 && rows % 8 == 0 && cols % 8 == 0 && n_mask >= 1 &&
+                mask_pixel > 0.0,
             CSG_E_SHAPE,
-            "csg_chain_add_fpm_mask: rows and cols must be multiples of 8, n_mask 1 or n_lambda");
+            "csg_chain_add_fpm_mask: rows and cols must be multiples of 8 and n_mask >= 1");
+  CSG_CHECK(mask_index >= -1 && mask_index < n_mask, CSG_E_ARG,
+            "csg_chain_add_fpm_mask: mask_index must be -1 or a slice of the mask cube");
+  // the reference applies one slice to every wavelength: maskIndex, or the
+  // first slice it processes when the script leaves it at -1
+  // (fpmCMCForPupToLyot::set_fpmMatAmp, fpmPupToLyot.cpp:355-360)
+  const int slice = mask_index < 0 ? 0 : mask_index;
   DeviceGuard g(c->ctx->device);
   cudaStream_t st = c->ctx->stream;
   Elem e;
@@ -497,10 +510,11 @@ int csg_chain_add_fpm_mask(csg_chain* c, const float* mask_re, const float* mask
   e.dm = mask_pixel;
   // planar per-wavelength multipliers: M - 1 (Babinet) or M
   const size_t plane = (size_t)rows * cols;
-  auto planes = [&](const float* re, const float* im, bool ones) {
+  // the calibration mask is a single plane ([rows][cols], the binary
+  // adapter's calibMat) applied at every wavelength
+  auto planes = [&](const float* re, const float* im, bool ones, size_t src) {
     std::vector<float> d((size_t)L * 2 * plane);
     for (int l = 0; l < L; ++l) {
-      const size_t src = (size_t)(n_mask == 1 ? 0 : l) * plane;
       for (size_t p = 0; p < plane; ++p) {
         const float mr = ones ? 1.f : re[src + p], mi = ones || !im ? 0.f : im[src + p];
         d[(size_t)l * 2 * plane + p] = e.bab ? mr - 1.f : mr;
@@ -509,14 +523,24 @@ int csg_chain_add_fpm_mask(csg_chain* c, const float* mask_re, const float* mask
     }
     return d;
   };
-  std::vector<float> d = planes(mask_re, mask_im, false);
+  std::vector<float> d = planes(mask_re, mask_im, false, (size_t)slice * plane);
   e.dmask = dev_copy(d.data(), d.size(), st);
   CSG_CHECK(e.dmask, CSG_E_NOMEM, "csg_chain_add_fpm_mask: allocation failed");
   // the calibration mask, unless it leaves the field as it is (ones with Babinet)
   if (disable_for_calibration && (calib_re || !e.bab)) {
-    std::vector<float> cd = planes(calib_re, calib_im, calib_re == nullptr);
+    std::vector<float> cd = planes(calib_re, calib_im, calib_re == nullptr, 0);
+    if (c->ref_calibration && !e.bab) {
+      // the reference's calibration transform exists for the first
+      // wavelength only; the others keep a zero mask hat, so their
+      // calibration fields are zero (fpmPupToLyot.cpp:56, 86-92)
+      std::fill(cd.begin() + 2 * plane, cd.end(), 0.f);
+    }
     e.cmask = dev_copy(cd.data(), cd.size(), st);
-    CSG_CHECK(e.cmask, CSG_E_NOMEM, "csg_chain_add_fpm_mask: allocation failed");
+    if (!e.cmask) {
+      cudaFree(e.dmask);
+      set_error("csg_chain_add_fpm_mask: allocation failed");
+      return CSG_E_NOMEM;
+    }
   }
   std::vector<double> lfv(lf, lf + L), pref1(2 * L, 0.0), pref2(2 * L, 0.0);
   for (int l = 0; l < L; ++l) {
@@ -1622,6 +1646,14 @@ int csg_chain_image(csg_chain* c, float** dev_image, int* n_out) {
   *n_out = 0;
   for (auto& e : c->elems)
     if (e.kind == E_FRAUNHOFER) *n_out = e.n_out;
+  return CSG_OK;
+}
+
+// Fixed-mask FPMs added after this call reproduce the reference's
+// calibration-hat behaviour (see the header).
+int csg_chain_set_reference_calibration(csg_chain* c, int enable) {
+  CSG_CHECK(c, CSG_E_ARG, "csg_chain_set_reference_calibration: null chain");
+  c->ref_calibration = enable != 0;
   return CSG_OK;
 }
 

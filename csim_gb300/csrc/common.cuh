@@ -137,6 +137,13 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// Whether every value of a host array is finite (CSG_E_NAN checks).
+inline bool all_finite(const double* v, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!(v[i] - v[i] == 0.0)) return false;
+  return true;
+}
+
 inline int grid_for(long long n, int block, int cap = 152 * 32) {
   long long g = (n + block - 1) / block;
   if (g > cap) g = cap;

@@ -301,6 +301,9 @@ int csg_de_set_bounds(csg_de* de, const double* global_lo, const double* global_
                       const double* init_lo, const double* init_hi) {
   CSG_CHECK(de && global_lo && global_hi && init_lo && init_hi, CSG_E_ARG,
             "csg_de_set_bounds: null argument");
+  CSG_CHECK(all_finite(global_lo, de->d.nvar) && all_finite(global_hi, de->d.nvar) &&
+                all_finite(init_lo, de->d.nvar) && all_finite(init_hi, de->d.nvar),
+            CSG_E_NAN, "csg_de_set_bounds: non-finite bound");
   DeviceGuard g(de->ctx->device);
   const size_t b = (size_t)de->d.nvar * 8;
   cudaStream_t st = de->ctx->stream;

@@ -975,6 +975,8 @@ int csg_fft2d_prec(csg_ctx* ctx, float* field, int n_fields, int n, int directio
 int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
                 double ap_rad, double z) {
   CSG_CHECK(ctx && field && lambda, CSG_E_ARG, "csg_fresnel: null argument");
+  CSG_CHECK(all_finite(&z, 1) && all_finite(&ap_rad, 1), CSG_E_NAN,
+            "csg_fresnel: non-finite distance or aperture radius");
   CSG_CHECK(ap_rad > 0, CSG_E_ARG, "csg_fresnel: apRad must be positive");
   DeviceGuard g(ctx->device);
   FresnelArgs fa{lambda, z, ap_rad};
@@ -988,6 +990,8 @@ int csg_fresnel_prec(csg_ctx* ctx, float* field, int n_fields, int n, const doub
             CSG_E_ARG, "csg_fresnel_prec: bad precision");
   if (precision != CSG_PREC_HIGH) return csg_fresnel(ctx, field, n_fields, n, lambda, ap_rad, z);
   CSG_CHECK(ctx && field && lambda, CSG_E_ARG, "csg_fresnel_prec: null argument");
+  CSG_CHECK(all_finite(&z, 1) && all_finite(&ap_rad, 1), CSG_E_NAN,
+            "csg_fresnel_prec: non-finite distance or aperture radius");
   CSG_CHECK(ap_rad > 0, CSG_E_ARG, "csg_fresnel_prec: apRad must be positive");
   CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
             "FFT size must be a power of two in [64, 4096]");

@@ -512,6 +512,13 @@ static int create_plan(csg_ctx* ctx, csg_mft** plan, int n_in_y, int n_in_x, int
             "csg_mft_create: precision must be CSG_PREC_BF16X6, CSG_PREC_BF16X3 or CSG_PREC_HIGH");
   for (int s = 0; s < n_slots; ++s)
     CSG_CHECK(lf[s] != 0.0, CSG_E_ARG, "csg_mft_create: zero lambda*f");
+  {
+    const int rs = n_out ? n_slots : 1;
+    CSG_CHECK(all_finite(yin, n_in_y) && all_finite(xin, n_in_x) &&
+                  all_finite(yout, (size_t)rs * n_out_y) && all_finite(xout, (size_t)rs * n_out_x) &&
+                  all_finite(lf, n_slots) && (!pref || all_finite(pref, 2 * (size_t)n_slots)),
+              CSG_E_NAN, "csg_mft_create: non-finite coordinate, lambda*f or prefactor");
+  }
   DeviceGuard g(ctx->device);
   csg_mft* m = new csg_mft();
   m->ctx = ctx;

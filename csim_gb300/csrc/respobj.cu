@@ -135,6 +135,9 @@ int csg_respobj_create(csg_ctx* ctx, csg_respobj** obj, const double* m_host, in
   CSG_CHECK(ctx && obj && m_host && wavelength, CSG_E_ARG, "csg_respobj_create: null argument");
   CSG_CHECK(n_mat > 0 && npix > 0 && ncol > 1, CSG_E_SHAPE, "csg_respobj_create: bad shape");
   CSG_CHECK(objective == 0 || objective == 1, CSG_E_ARG, "csg_respobj_create: objective 0 or 1");
+  CSG_CHECK(all_finite(&calib, 1) && all_finite(wavelength, n_mat) &&
+                all_finite(m_host, (size_t)n_mat * npix * ncol * 2),
+            CSG_E_NAN, "csg_respobj_create: non-finite response matrix, wavelength or calibration");
   CSG_CHECK(calib > 0, CSG_E_ARG, "csg_respobj_create: calibration must be positive");
   DeviceGuard g(ctx->device);
   cudaStream_t st = ctx->stream;

@@ -37,7 +37,7 @@ extern "C" {
 #define CSG_E_CUDA (-3)     /* CUDA runtime/driver error */
 #define CSG_E_TIMEOUT (-4)  /* a device-side bounded wait ran out */
 #define CSG_E_NOMEM (-5)    /* device allocation failed */
-#define CSG_E_NAN (-6)      /* non-finite value where a finite one is required */
+#define CSG_E_NAN (-6)      /* non-finite host value where a finite one is required */
 #define CSG_E_STATE (-7)    /* object used in the wrong state */
 
 #define CSG_LAYOUT_COLMAJOR 0 /* Armadillo cube: (r,c,s) at r + c*R + s*R*C */
@@ -232,7 +232,9 @@ int csg_hex_mask(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int
  * device address (a one-time set-up); make that first call before any stream
  * capture. All calls share the one array: calls whose work overlaps on the
  * GPU (different streams or contexts on one device) race and must be
- * ordered by the caller. */
+ * ordered by the caller. The array's device address is looked up once per
+ * device and kept for the process; after cudaDeviceReset it is no longer
+ * valid, so a process that resets a device must not call this again on it. */
 #define CSG_HEX_NOALLOC_MAX_PHASORS 262144
 int csg_hex_mask_noalloc(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* count, int S,
                          int n_sub, const double* sags, int n_hex, int n_out, const int* cand,
@@ -290,16 +292,21 @@ int csg_chain_add_fpm_double_mask(csg_chain* chain, const float* mask_re, const 
  * in the same matrix-Fourier form as csg_chain_add_fpm_hex:
  *   babinet != 0:  E <- E + c MFT2[(M - 1) MFT1[E]]   (CMC with doBabinet)
  *   babinet == 0:  E <- c MFT2[M MFT1[E]]             (binary, CMC without)
- * mask_re / mask_im (host, mask_im may be null): [n_mask][rows][cols] with
- * n_mask 1 or n_lambda, pixel mask_pixel (maskGeom.set_xy(mask, pixel)),
- * rows and cols multiples of 8; lf: the lambdaFocalLength of each wavelength
- * (fRatioSign lambda focalRatio 2 beamRadius for the CMC, fRatioSign lambda
- * primaryfLength for the binary mask); c = zoomFftSign mask_pixel^2 dx^2 /
- * (fRatioSign lf^2). calib_re / calib_im (may be null: a mask of ones, the
- * CMC's fpmMatAmpCalib): the mask the calibration walk applies when
- * disable_for_calibration is set (the binary adapter's calibMat). */
+ * mask_re / mask_im (host, mask_im may be null): the reference's mask cube
+ * [n_mask][rows][cols] (complexMaskCube), of which slice mask_index is
+ * applied at every wavelength (maskIndex, fpmPupToLyot.cpp:355-360; -1, the
+ * reference's default, takes slice 0); pixel mask_pixel (maskGeom.set_xy(mask,
+ * pixel)), rows and cols multiples of 8; lf: the lambdaFocalLength of each
+ * wavelength (fRatioSign lambda focalRatio 2 beamRadius for the CMC,
+ * fRatioSign lambda primaryfLength for the binary mask); c = zoomFftSign
+ * mask_pixel^2 dx^2 / (fRatioSign lf^2). calib_re / calib_im ([rows][cols],
+ * may be null: a mask of ones, the CMC's fpmMatAmpCalib): the mask the
+ * calibration walk applies when disable_for_calibration is set (the binary
+ * adapter's calibMat), at every wavelength unless
+ * csg_chain_set_reference_calibration is on. */
 int csg_chain_add_fpm_mask(csg_chain* chain, const float* mask_re, const float* mask_im,
-                           int n_mask, int rows, int cols, double mask_pixel, const double* lf,
+                           int n_mask, int mask_index, int rows, int cols, double mask_pixel,
+                           const double* lf,
                            double f_ratio_sign, double zoom_fft_sign, int babinet,
                            const float* calib_re, const float* calib_im,
                            int disable_for_calibration);
@@ -329,6 +336,17 @@ int csg_chain_add_fpm_hex(csg_chain* chain, const int16_t* hex_id, const uint16_
                           int n_sub, int n_hex, double dm, double focal_ratio, double beam_radius,
                           double f_ratio_sign, double zoom_fft_sign, double phase_sign,
                           int disable_for_calibration);
+/* The reference computes the calibration mask's transform once, for the
+ * first wavelength its loop reaches, and leaves the other wavelengths' with
+ * a zero transform (fftMaskHatCalibComputed, fpmPupToLyot.cpp:56, 86-92).
+ * With a Babinet mask (hex, CMC with doBabinet) the calibration mask is
+ * 1 - 1 = 0 at every wavelength, so nothing changes; without Babinet (the
+ * binary adapter, CMC without doBabinet) the calibration field of every
+ * wavelength but the first is zero there. This library calibrates every
+ * wavelength with its own transform by default; enable != 0 makes fixed-mask
+ * FPMs added after this call reproduce the reference (first wavelength
+ * only, the result of its loop on one thread). Default 0. */
+int csg_chain_set_reference_calibration(csg_chain* chain, int enable);
 /* Hex FPMs added after this call transform only the bounding box of the
  * support of fliplr(M) - 1 (rounded out to multiples of 128): M = 1 wherever
  * no hex covers a mask pixel, for any sags, so the Babinet term is exactly

@@ -415,3 +415,57 @@ def test_double_fraunhofer_fixed_mask_matches_oracle(ctx):
           f"{e_img:.3e} (of the calibration peak)")
     assert e_cal < 1e-6 and e_img < 1e-6, (e_cal, e_img)
     cor.close()
+
+
+def _fixed_mask_chain(ctx, mask, calib, babinet, mask_index=-1, reference_calibration=False):
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import workloads as W
+    spec = small_spec(wavelengths=(640e-9, 660e-9))
+    a = W.piaacmc_arrays(spec, [cg.PointSource(1.0, 0.0, 0.0)])
+    ef, tel = a["ef"], a["tel"]
+    lfl = np.array([-1.0 * lam * spec.fpm_focal_ratio * 2 * ef.beamRadiusPhysical
+                    for lam in a["lam"]])
+    elems = [cg.Mask(a["pupil"]), cg.Mirror(a["sag1"], 1.0),
+             cg.FpmPupToLyotMask(mask, a["dm"], lfl, -1.0, -1.0, babinet, calib,
+                                 maskIndex=mask_index),
+             cg.Mask(a["lyot"]), cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov)]
+    cor = cg.Coronagraph(ctx, tel, ef, elems, 6, True,
+                         reference_calibration=reference_calibration)
+    cor.batch_all(1)
+    img = cor.execute(calibrating=False).clone()
+    cal = cor.execute(calibrating=True).clone()
+    ctx.sync()
+    li = np.asarray(cor._batch[0])
+    cor.close()
+    return img, cal, li
+
+
+def test_fixed_mask_fpm_uses_one_mask_slice(ctx):
+    """The reference applies one slice of the mask cube, maskIndex (the first
+    slice when it is -1), at every wavelength (fpmPupToLyot.cpp:355-360): a
+    three-slice cube with maskIndex 2 gives the images of slice 2 alone, and
+    maskIndex -1 those of slice 0."""
+    rng = np.random.default_rng(23)
+    cube = (0.6 + 0.4 * rng.random((3, 32, 24))) * np.exp(-1j * rng.uniform(-2, 2, (3, 32, 24)))
+    for idx, sl in ((2, 2), (-1, 0)):
+        img_c, cal_c, _ = _fixed_mask_chain(ctx, cube, None, True, mask_index=idx)
+        img_s, cal_s, _ = _fixed_mask_chain(ctx, cube[sl], None, True)
+        assert torch.equal(img_c, img_s) and torch.equal(cal_c, cal_s), idx
+
+
+def test_reference_calibration_first_wavelength_only(ctx):
+    """Binary mask (no Babinet) with its calibration mask at two wavelengths:
+    by default every wavelength's calibration field is its own transform;
+    with reference_calibration, as the reference's compute-once calibration
+    transform leaves it (fpmPupToLyot.cpp:56, 86-92), the first wavelength's
+    field is unchanged and the second's is zero."""
+    yy, xx = np.mgrid[0:32, 0:32]
+    mask = (np.hypot(yy - 15.5, xx - 15.5) > 6.0).astype(np.complex128)
+    calib = np.ones((32, 32), np.complex128)
+    img0, cal0, li = _fixed_mask_chain(ctx, mask, calib, False)
+    img1, cal1, _ = _fixed_mask_chain(ctx, mask, calib, False, reference_calibration=True)
+    first, second = li == 0, li == 1
+    assert torch.equal(img0, img1)
+    assert torch.equal(cal1[first], cal0[first])
+    assert cal0[second].abs().max().item() > 0
+    assert cal1[second].abs().max().item() == 0.0
