@@ -43,6 +43,7 @@ SIGNATURES = {
     "csg_last_error": ([], C.c_char_p),
     "csg_sync": ([P], None),
     "csg_set_stream": ([P, P], None),
+    "csg_set_wait_budget": ([P, C.c_longlong], None),
     "csg_get_stream": ([P], P),
     "csg_alloc": ([P, SZ, C.POINTER(P)], None),
     "csg_free": ([P, P], None),

@@ -168,6 +168,13 @@ int csg_sync(csg_ctx* c) {
   return CSG_OK;
 }
 
+int csg_set_wait_budget(csg_ctx* c, long long cycles) {
+  CSG_CHECK(c != nullptr, CSG_E_ARG, "csg_set_wait_budget: null context");
+  CSG_CHECK(cycles >= 0, CSG_E_ARG, "csg_set_wait_budget: cycles must be >= 0");
+  c->wait_budget = cycles;
+  return CSG_OK;
+}
+
 int csg_set_stream(csg_ctx* c, void* stream) {
   CSG_CHECK(c != nullptr, CSG_E_ARG, "csg_set_stream: null context");
   // NULL selects CUDA's default stream (stream 0), which is what torch's

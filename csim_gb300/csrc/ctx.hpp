@@ -31,6 +31,7 @@ struct csg_ctx {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   int* status = nullptr;            // device int, 0 = ok
+  long long wait_budget = 0;        // bounded-wait cycles of the GEMMs (0: default)
   std::set<void*> allocations;
   int sm_count = 0;
   // pipelined readout (csg_readout_d2h): two device staging buffers, each

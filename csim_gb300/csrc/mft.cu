@@ -752,6 +752,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.accumulate = 0;
     p.status = ctx->status;
     p.valid = m->valid;
+    p.wait_budget = ctx->wait_budget;
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     // algorithmic work: 8 flops per complex multiply-add of the contraction
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->ny * m->no * m->nx);
@@ -791,6 +792,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.accumulate = accumulate;
     p.status = ctx->status;
     p.valid = m->valid;
+    p.wait_budget = ctx->wait_budget;
     p.out_lo = out_lo;
     CUtensorMap to;
     p.tma_out = make_map_f32_out(&to, out + (size_t)outw.r0 * outw.pitch + outw.c0, m->no, m->mo,

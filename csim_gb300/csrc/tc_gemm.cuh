@@ -58,6 +58,10 @@ struct Params {
   // high precision, EPI_F32: the low words of the two-float results, stored
   // per thread beside `out` (same window and pitch); null: not written
   float* out_lo;
+  // cycles a role waits for another before the tile walk gives up (the
+  // context's csg_set_wait_budget; 0: kWaitBudgetCycles). The clean-up after
+  // a give-up always waits with the full budget.
+  long long wait_budget;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -87,12 +91,13 @@ __device__ __forceinline__ uint32_t mbar_try_wait(uint32_t bar, uint32_t parity)
 }
 
 // Bounded wait: false once the cycle budget is spent.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          long long budget = kWaitBudgetCycles) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try_wait(a, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(a, parity)) {
-    if (clock64() - t0 > kWaitBudgetCycles) return false;
+    if (clock64() - t0 > budget) return false;
   }
   return true;
 }
@@ -441,6 +446,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int n_tiles_total = p.n_fields * p.m_tiles * p.n_tiles;
   const int n_parts = p.n_terms > 3 ? 3 : 2;  // parts the issued products read
   const int k_iters = 2 * p.k_blocks;         // (data component c, K block) per tile
+  const long long wb = p.wait_budget > 0 ? p.wait_budget : kWaitBudgetCycles;
+  long long g_issued = 0;  // producer lane: loads issued (their stages' phases)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -480,11 +487,12 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int it = 0; it < k_iters; ++it, ++g) {
           const int stage = (int)(g % STAGES);
           const uint32_t phase = (uint32_t)((g / STAGES) & 1);
-          if (g >= STAGES && !mbar_wait(&empty[stage], phase ^ 1)) {
+          if (g >= STAGES && !mbar_wait(&empty[stage], phase ^ 1, wb)) {
             atomicExch(p.status, 1);
             *abort_flag = 1;
           }
           if (*abort_flag) break;
+          g_issued = g + 1;
           const int kb = it % p.k_blocks;
           const int c = it / p.k_blocks;
           uint8_t* sA = sbase + stage * CF::STAGE_BYTES;
@@ -518,19 +526,17 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint32_t phase = (uint32_t)((g / STAGES) & 1);
           const int ts = (int)(g % NSLOT);
           const uint32_t round = (uint32_t)((g / NSLOT) & 1);
-          if (g >= NSLOT) ok = mbar_wait(&tempty[ts], round ^ 1u);
-          if (ok) ok = mbar_wait(&full[stage], phase);
+          if (g >= NSLOT) ok = mbar_wait(&tempty[ts], round ^ 1u, wb);
+          if (ok) ok = mbar_wait(&full[stage], phase, wb);
           // the previous tile's persistent slot must be read before this
           // tile's first products overwrite them
-          if (ok && it == 0 && j > 0) ok = mbar_wait(gfree, (uint32_t)((j - 1) & 1));
+          if (ok && it == 0 && j > 0) ok = mbar_wait(gfree, (uint32_t)((j - 1) & 1), wb);
           if (!ok || *abort_flag) {
             ok = false;
             atomicExch(p.status, 2);
             *abort_flag = 1;
-            // let the products already issued finish before tensor memory
-            // is released (bounded wait), then release the drain warps' waits
-            umma_commit(quiesce);
-            mbar_wait(quiesce, 0);
+            // release the drain warps' waits (they see the flag and stop);
+            // the products already issued are waited out at the end
             for (int s = 0; s < NSLOT; ++s) mbar_arrive(&tfull[s]);
             mbar_arrive(gdone);
             break;
@@ -589,7 +595,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int it = 0; it < (beyond ? 0 : k_iters); ++it, ++g) {
         const int ts = (int)(g % NSLOT);
         const uint32_t round = (uint32_t)((g / NSLOT) & 1);
-        ok = mbar_wait(&tfull[ts], round);
+        ok = mbar_wait(&tfull[ts], round, wb);
         ok = __all_sync(0xffffffffu, ok && !*abort_flag);
         if (!ok) break;
         tc_fence_after();
@@ -603,11 +609,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       if (ok && !beyond) {
         // the tile's persistent slot is complete once its last commit lands
-        ok = mbar_wait(gdone, (uint32_t)(j & 1));
+        ok = mbar_wait(gdone, (uint32_t)(j & 1), wb);
         ok = __all_sync(0xffffffffu, ok && !*abort_flag);
       }
       if (!ok) {
         atomicExch(p.status, 3);
+        *abort_flag = 1;
         break;
       }
       if (!beyond) {
@@ -638,7 +645,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (lane == (jj & 31)) xown[jj] = m;
         }
         mbar_arrive(&pairbar[warp >> 1]);  // every lane of both warps (release)
-        ok = mbar_wait(&pairbar[warp >> 1], (uint32_t)(xt & 1));
+        ok = mbar_wait(&pairbar[warp >> 1], (uint32_t)(xt & 1), wb);
         ok = __all_sync(0xffffffffu, ok && !*abort_flag);
         ++xt;
         if (!ok) {
@@ -826,6 +833,24 @@ __global__ void __launch_bounds__(THREADS, 1)
     // the staged boxes must be read before the CTA's shared memory goes
     if (EPI == EPI_F32 && lane == 0) bulk_wait_read_all();
     __syncwarp();
+  }
+  tc_fence_before();
+  __syncthreads();
+  // After a give-up (the flag is settled: every role has stopped), nothing
+  // asynchronous may outlive the CTA: the MMA thread waits for the products
+  // it issued (tensor memory is released next) and the producer for the
+  // operand loads still in flight, which complete their stages' full
+  // barriers when the bytes land (only the last STAGES loads can be pending:
+  // each was issued after the one STAGES before it had been consumed).
+  if (*abort_flag) {
+    if (warp == MMA_WARP && lane == 0) {
+      umma_commit(quiesce);
+      mbar_wait(quiesce, 0);
+    }
+    if (warp == PRODUCER_WARP && lane == 0) {
+      for (long long i = g_issued > STAGES ? g_issued - STAGES : 0; i < g_issued; ++i)
+        mbar_wait(&full[(int)(i % STAGES)], (uint32_t)((i / STAGES) & 1));
+    }
   }
   tc_fence_before();
   __syncthreads();

@@ -75,6 +75,15 @@ const char* csg_last_error(void);
 /* Wait for the context's stream and report CSG_E_TIMEOUT if a kernel gave up
  * on a bounded wait since the last call. */
 int csg_sync(csg_ctx* ctx);
+/* Cycles a tensor-core transform launched from this context lets one of its
+ * roles (operand loads, products, drains) wait for another before it gives
+ * up: it then stops, waits out its own operand loads and products, releases
+ * its tensor memory and records the failure, which the next csg_sync reports
+ * as CSG_E_TIMEOUT (the context stays usable). 0 (the default) is about one
+ * second at the GPU's clock, far above any legitimate wait; a small value
+ * makes the give-up path testable. Graphs captured before a change keep the
+ * value they were captured with. */
+int csg_set_wait_budget(csg_ctx* ctx, long long cycles);
 /* Run subsequent work on an external stream (a cudaStream_t; NULL is CUDA's
  * default stream). A new context runs on its own non-blocking stream. */
 int csg_set_stream(csg_ctx* ctx, void* stream);
