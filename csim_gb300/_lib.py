@@ -74,7 +74,7 @@ SIGNATURES = {
     "csg_mft_workspace_bytes": ([P, I], SZ),
     "csg_hex_mask": ([P, P, P, I, I, P, I, I, P, P, D, I, D, I, P], None),
     "csg_hex_mask_noalloc": ([P, P, P, I, I, P, I, I, P, P, D, I, D, I, P], None),
-    "csg_hex_tables":([P, P, P, I, I, I, D, D, D, I, I, D, D, P, P, P], None),
+    "csg_hex_tables": ([P, P, P, I, I, I, D, D, D, I, I, D, D, P, P, P, I], None),
     "csg_chain_create": ([P, C.POINTER(P), I, D, I, P, I], None),
     "csg_chain_destroy": ([P], None),
     "csg_chain_add_mask": ([P, P, I, I], None),

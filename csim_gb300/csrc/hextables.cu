@@ -47,9 +47,17 @@ __global__ void k_hex_sample_index(int S, int n_sub, int A, double pixel_scale, 
   }
 }
 
+// stale != 0: the reference's row check as its loop runs on one OpenMP
+// thread (complexHexMaskFPM.cpp:395-423): the check's row index is the
+// midpoint's until the row's first passing cell and afterwards the one left
+// by the last sub-sample of the cell before. The sample indices grow with
+// the pixel index, so in a row whose midpoint index is on the array the
+// first passing cell is the first column whose midpoint index is; after it
+// the check uses the last sub-sample's row index.
 __global__ void k_hex_interp(const int* __restrict__ design, int A, int S, int n_sub,
                              const int* __restrict__ sidx, int16_t* __restrict__ hex_id,
-                             uint16_t* __restrict__ count, int* __restrict__ overflow) {
+                             uint16_t* __restrict__ count, int* __restrict__ overflow,
+                             int stale) {
   const long long plane = (long long)S * S;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < plane;
        p += (long long)gridDim.x * blockDim.x) {
@@ -60,7 +68,13 @@ __global__ void k_hex_interp(const int* __restrict__ design, int A, int S, int n
     int list[3] = {-1, -1, -1};
     unsigned cnt[3] = {0, 0, 0};
     int nl = 0, over = 0;
-    const bool inside = ri[c] >= 0 && ri[c] < A && rj[c] >= 0 && rj[c] < A;
+    bool inside = ri[c] >= 0 && ri[c] < A && rj[c] >= 0 && rj[c] < A;
+    if (stale && inside) {
+      const int jp = j > 0 ? sidx[(j - 1) * n_sub + c] : -1;
+      const bool first = j == 0 || jp < 0 || jp >= A;
+      const bool last_on = ri[n_sub - 1] >= 0 && ri[n_sub - 1] < A;
+      inside = first || last_on;
+    }
     if (inside) {
       for (int a = 0; a < n_sub; ++a) {
         const int ii1 = ri[a];
@@ -107,12 +121,12 @@ extern "C" int csg_hex_tables(csg_ctx* ctx, const double* hex_x, const double* h
                               int n_rings, int design_size, double fpm_scale_factor,
                               double hex_gap, double pitch, int S, int n_sub, double pixel_scale,
                               double fpm_radius, int16_t* hex_id, uint16_t* count,
-                              int* n_overflow) {
+                              int* n_overflow, int reference_single_thread) {
   CSG_CHECK(ctx && hex_x && hex_y && hex_id && count, CSG_E_ARG, "csg_hex_tables: null argument");
   CSG_CHECK(n_hex > 0 && n_hex < 32767 && n_rings > 0 && design_size > 0 && S > 0 && n_sub > 0 &&
                 n_sub * n_sub < 65536,
             CSG_E_SHAPE, "csg_hex_tables: bad size");
-  CSG_CHECK(pixel_scale > 0 && fpm_radius > 0 && pitch > 0, CSG_E_ARG,
+  CSG_CHECK(pixel_scale > 0 && fpm_radius > 0 && pitch > 0 && fpm_scale_factor > 0, CSG_E_ARG,
             "csg_hex_tables: non-positive scale");
   DeviceGuard g(ctx->device);
   cudaStream_t st = ctx->stream;
@@ -136,8 +150,8 @@ extern "C" int csg_hex_tables(csg_ctx* ctx, const double* hex_x, const double* h
                                                                             pixel_scale, ac1, xc1,
                                                                             sidx);
   CSG_LAUNCH_CHECK();
-  k_hex_interp<<<grid_for((long long)S * S, 128), 128, 0, st>>>(design, A, S, n_sub, sidx, hex_id,
-                                                                count, over);
+  k_hex_interp<<<grid_for((long long)S * S, 128), 128, 0, st>>>(
+      design, A, S, n_sub, sidx, hex_id, count, over, reference_single_thread ? 1 : 0);
   CSG_LAUNCH_CHECK();
   int h_over = 0;
   CSG_CUDA(cudaMemcpyAsync(&h_over, over, sizeof(int), cudaMemcpyDeviceToHost, st));

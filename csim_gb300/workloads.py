@@ -24,16 +24,17 @@ from .runtime import Context, dvec, ptr
 
 
 def hex_tables(ctx: Context, hex_x, hex_y, n_rings, design_size, fpm_scale_factor, hex_gap,
-               pitch, S, n_sub, pixel_scale, fpm_radius):
+               pitch, S, n_sub, pixel_scale, fpm_radius, reference_single_thread=False):
     """Interpolation tables [3][S][S] (int16 ids, uint16 counts) built on the
-    GPU; returned as host numpy arrays."""
+    GPU; returned as host numpy arrays. reference_single_thread: the
+    reference's tables as its loop builds them on one OpenMP thread."""
     hx, hy = dvec(hex_x), dvec(hex_y)
     ids = torch.empty((3, S, S), dtype=torch.int16, device="cuda")
     cnt = torch.empty((3, S, S), dtype=torch.int16, device="cuda")
     over = C.c_int()
     call("csg_hex_tables", ctx.h, ptr(hx), ptr(hy), hx.numel(), n_rings, design_size,
          fpm_scale_factor, hex_gap, pitch, S, n_sub, pixel_scale, fpm_radius, ptr(ids), ptr(cnt),
-         C.byref(over))
+         C.byref(over), int(bool(reference_single_thread)))
     return ids.cpu().numpy(), cnt.cpu().numpy().view(np.uint16), over.value
 
 

@@ -257,11 +257,19 @@ int csg_hex_mask_noalloc(csg_ctx* ctx, const int16_t* hex_id, const uint16_t* co
  * formula exactly). Design array A x A, mask S x S at pixel_scale, n_sub^2
  * samples per mask pixel. Where hexes overlap the highest index wins; a
  * fourth distinct hex in one pixel is counted as outside and reported in
- * *n_overflow (the reference asserts). Synchronous. */
+ * *n_overflow (the reference asserts). reference_single_thread != 0
+ * reproduces the reference's tables as its loop produces them on one OpenMP
+ * thread: the on-array check of each cell after a row's first passing cell
+ * uses the row index left by the previous cell's last sub-sample
+ * (complexHexMaskFPM.cpp:395-423), which drops the cells of the rows whose
+ * last sub-samples fall off the design array (only where hexes reach the
+ * array's edge does this change a table value); 0 checks every cell at its
+ * midpoint. Synchronous. */
 int csg_hex_tables(csg_ctx* ctx, const double* hex_x, const double* hex_y, int n_hex,
                    int n_rings, int design_size, double fpm_scale_factor, double hex_gap,
                    double pitch, int S, int n_sub, double pixel_scale, double fpm_radius,
-                   int16_t* hex_id, uint16_t* count, int* n_overflow);
+                   int16_t* hex_id, uint16_t* count, int* n_overflow,
+                   int reference_single_thread);
 
 /* ------------------------------------------------- coronagraph chain */
 /* Batched element walk: coronagraph::init (coronagraph.cpp:50-168) builds the

@@ -55,10 +55,14 @@ void make_hex_array(const double* hex_x, const double* hex_y, int n_hex, int n_r
 }
 
 /* hex_id / count: [3][S][S]. Returns the number of pixels that met a fourth
- * distinct hex. */
+ * distinct hex. stale != 0 reproduces the reference's loop as it runs on one
+ * OpenMP thread: its on-array check of a cell uses the row index ii1 left by
+ * the last sub-sample of the previous processed cell of the row (the variable
+ * is shared by the check and the sub-sample loop, complexHexMaskFPM.cpp:
+ * 395-423), the midpoint's only until the first cell of the row passes. */
 int make_interpolation_data(const int32_t* design, int A, int S, int n_sub, double pixel_scale,
                             double fpm_radius, double fpm_scale_factor, int16_t* hex_id,
-                            uint16_t* count) {
+                            uint16_t* count, int stale) {
   const double ac1 = -S / 2.0 - 0.5;
   const double xc1 = (0.5 / fpm_radius) * fpm_scale_factor;
   const long plane = (long)S * S;
@@ -71,11 +75,16 @@ int make_interpolation_data(const int32_t* design, int A, int S, int n_sub, doub
     const int iii_c = (int)(n_sub / 2.0);
     const double xc = (i + ac1 + (0.5 + iii_c) / ((double)n_sub)) * pixel_scale;
     const int ii1c = (int)((0.5 + xc * xc1) * A + 0.5);
+    int ii1_check = ii1c;
     for (int j = 0; j < S; ++j) {
       const int jjj_c = (int)(n_sub / 2.0);
       const double yc = (j + ac1 + (0.5 + jjj_c) / ((double)n_sub)) * pixel_scale;
       const int jj1c = (int)((0.5 + yc * xc1) * A + 0.5);
-      if (ii1c < 0 || ii1c >= A || jj1c < 0 || jj1c >= A) continue;
+      if (ii1_check < 0 || ii1_check >= A || jj1c < 0 || jj1c >= A) continue;
+      if (stale) {  /* the sub-sample loop leaves its last row index behind */
+        const double xl = (i + ac1 + (0.5 + (n_sub - 1)) / ((double)n_sub)) * pixel_scale;
+        ii1_check = (int)((0.5 + xl * xc1) * A + 0.5);
+      }
       int list[3];
       int nl = 0;
       unsigned cnt[3] = {0, 0, 0};

@@ -37,7 +37,7 @@ def lib() -> C.CDLL:
         _lib.make_hex_array.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                         C.c_double, P]
         _lib.make_interpolation_data.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_double,
-                                                 C.c_double, C.c_double, P, P]
+                                                 C.c_double, C.c_double, P, P, C.c_int]
         _lib.make_interpolation_data.restype = C.c_int
     return _lib
 
@@ -55,10 +55,14 @@ def hex_design_array(hex_x, hex_y, n_rings, A, fpm_scale_factor, hex_gap, pitch)
     return d
 
 
-def interpolation_tables(design, S, n_sub, pixel_scale, fpm_radius, fpm_scale_factor):
+def interpolation_tables(design, S, n_sub, pixel_scale, fpm_radius, fpm_scale_factor,
+                         stale=False):
+    """make_interpolation_data (complexHexMaskFPM.cpp:372-469); stale: the
+    reference's row check as its loop runs on one OpenMP thread."""
     design = np.ascontiguousarray(design, np.int32)
     ids = np.empty((3, S, S), np.int16)
     cnt = np.empty((3, S, S), np.uint16)
     over = lib().make_interpolation_data(_p(design), design.shape[0], S, n_sub, pixel_scale,
-                                         fpm_radius, fpm_scale_factor, _p(ids), _p(cnt))
+                                         fpm_radius, fpm_scale_factor, _p(ids), _p(cnt),
+                                         int(bool(stale)))
     return ids, cnt, over

@@ -1,8 +1,8 @@
 """Generate the committed golden fixtures from the reference's own data files.
 
-Run in a checkout that has the reference tree (read-only) at REF; writes
-tests/golden/*.npz. The GPU machine never needs the reference: the tests read the
-.npz files only.
+Usage: python tests/golden/make_golden.py REFERENCE_TREE (or with the tree's
+path in the CSIM_REFERENCE environment variable); writes tests/golden/*.npz.
+The GPU machine never needs the reference: the tests read the .npz files only.
 
 Fixtures:
   mono_response.npz  donutPiaaFullCircleExample/mono_2_6/responseData: the
@@ -23,7 +23,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from oracle import fits  # noqa: E402
 
-REF = os.environ.get("CSIM_REFERENCE", "/root/reference")
 
 
 def last_best(path):
@@ -32,7 +31,10 @@ def last_best(path):
 
 
 def main():
-    ex = os.path.join(REF, "donutPiaaFullCircleExample")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CSIM_REFERENCE")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("usage: make_golden.py REFERENCE_TREE (or set CSIM_REFERENCE)")
+    ex = os.path.join(ref, "donutPiaaFullCircleExample")
     mono = os.path.join(ex, "mono_2_6")
     m = fits.read_complex(os.path.join(mono, "responseData", "responseData_s0_p0"))
     params = open(os.path.join(mono, "responseData", "problemParams.txt")).read().split("\n")
@@ -49,7 +51,7 @@ def main():
     np.savez(os.path.join(HERE, "mono_response.npz"), M=m, wavelengths=np.array(lam),
              calib=np.array(calib), best_x=np.array(xs), best_val=np.array(bests),
              best_iter=np.array(its), runs=np.array(runs))
-    w = fits.read(os.path.join(REF, "wfirst_sags.fits"))
+    w = fits.read(os.path.join(ref, "wfirst_sags.fits"))
     np.savez(os.path.join(HERE, "hex_counts.npz"), wfirst_sags_len=np.array(w.size))
     print("wrote fixtures; M", m.shape, "calib", calib, "lambda", lam, "best", bests)
 

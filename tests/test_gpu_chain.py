@@ -43,6 +43,22 @@ def test_hex_tables_match_oracle(ctx):
         assert np.array_equal(cnt, rcnt)
 
 
+def test_hex_tables_single_thread_quirk_matches_oracle(ctx):
+    """The GPU tables with reference_single_thread equal the C oracle's
+    restatement of the reference's one-thread loop, bit for bit, on a
+    geometry where the quirk changes a row (hexes reaching the array edge)."""
+    from csim_gb300 import workloads as W
+    hx, hy = W.hex_layout_standard(4)
+    A, S, n_sub, pix = 256, 64, 8, 2e-6
+    d = native.hex_design_array(hx, hy, 4, A, 1.0, 0.01, 1.0)
+    for stale in (False, True):
+        ids, cnt, _ = W.hex_tables(ctx, hx, hy, 4, A, 1.0, 0.01, 1.0, S, n_sub, pix,
+                                   S * pix * 0.49, reference_single_thread=stale)
+        rid, rcnt, _ = native.interpolation_tables(d, S, n_sub, pix, S * pix * 0.49, 1.0,
+                                                   stale=stale)
+        assert np.array_equal(ids, rid) and np.array_equal(cnt, rcnt), stale
+
+
 @pytest.mark.parametrize("conv_form", [False, True])
 def test_piaacmc_chain_matches_oracle(ctx, conv_form):
     from csim_gb300 import coronagraph as cg

@@ -174,3 +174,33 @@ def test_double_fraunhofer_restatement():
     blk[r0:r0 + S, r0:r0 + S] = (m - 1.0) * z[r0:r0 + S, r0:r0 + S]
     dec = zout.mft(z, 0) + zout.mft(blk, 0)
     assert np.abs(out[0] - dec).max() / peak < 1e-12
+
+
+def test_single_thread_row_check_quirk():
+    """make_interpolation_data on one OpenMP thread checks each cell after a
+    row's first passing cell with the row index left by the previous cell's
+    last sub-sample (complexHexMaskFPM.cpp:395-423). Where that index falls
+    off the design array and hexes reach the array's edge (scale factor 1,
+    mask grid a little wider than the array), the reference leaves the rest
+    of that mask row unfilled; the midpoint check fills it. Elsewhere the
+    two agree."""
+    from oracle import native
+    from csim_gb300.synth import hex_layout_standard
+    hx, hy = hex_layout_standard(4)
+    A, S, n_sub, pix = 256, 64, 8, 2e-6
+    d = native.hex_design_array(hx, hy, 4, A, 1.0, 0.01, 1.0)
+    mid = native.interpolation_tables(d, S, n_sub, pix, S * pix * 0.49, 1.0)
+    ref = native.interpolation_tables(d, S, n_sub, pix, S * pix * 0.49, 1.0, stale=True)
+    diff = (mid[0] != ref[0]).any(0) | (mid[1] != ref[1]).any(0)
+    rows = sorted(set(np.argwhere(diff)[:, 0].tolist()))
+    assert rows == [S - 1] and diff.sum() > 10
+    # the reference's unfilled cells read as outside every hex
+    r = S - 1
+    cols = np.argwhere(diff[r])[:, 0]
+    assert (ref[0][:, r, cols] == -1).all()
+    assert (ref[1][0, r, cols] == n_sub * n_sub).all()
+    # with the standard 0.9 scale factor no hex reaches the edge: identical
+    d9 = native.hex_design_array(hx, hy, 4, A, 0.9, 0.01, 1.0)
+    a = native.interpolation_tables(d9, S, n_sub, pix, S * pix * 0.45, 0.9)
+    b = native.interpolation_tables(d9, S, n_sub, pix, S * pix * 0.45, 0.9, stale=True)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
