@@ -337,6 +337,95 @@ def setup_de(args, ctx, W, cg, rank):
     return wl
 
 
+def surrogate_experiment(args):
+    """Surrogate-screened DE against plain GPU DE on the DE configuration
+    (1261 hexes, 5 wavelengths over 10% at 650 nm, the 1024^2 chain,
+    population 64, DE/local-to-best/1 with F 0.7, CR 0.9, initial sags within
+    +-10 nm of zero as the reference's scripts start, bounds +-0.6 um), on
+    optics that admit a deep dark hole (synth.designed_piaacmc_spec). Both
+    arms start from the same population and run for the same wall time;
+    the screened arm's clock includes its training samples (DE trajectory
+    plus random perturbations, all propagated) and training. Reports the
+    wall time to each contrast decade of both arms, the surrogate's RMS
+    log10 error, and the FP64 oracle's contrast for each arm's best vector."""
+    import torch
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import optimize as opt
+    from csim_gb300 import surrogate as sg
+    from csim_gb300 import workloads as W
+    from csim_gb300.runtime import Context
+    from csim_gb300.synth import designed_piaacmc_spec
+    from oracle import chain as oc
+    from oracle import elements as oe
+    ctx = Context(0)
+    lam = tuple(np.linspace(650e-9 * 0.95, 650e-9 * 1.05, 5))
+    spec = designed_piaacmc_spec(n_rings=20, wavelengths=lam, sag_range=0.6e-6)
+    cor, inp = W.build_piaacmc(ctx, spec, precision=args.precision)
+    reg = cg.RegionContrast(ctx, cor.n_out, cor.out_pixel, inp["lod_image"], 2.0, 8.0)
+    P = 64
+    obj = sg.PerLambdaObjective(cor, reg, P)
+    cfg = opt.DEConfig(populationSize=P, globalBounds=(-0.6e-6, 0.6e-6),
+                       initBounds=(-1e-8, 1e-8), fWeight=0.7, crossoverProb=0.9, seed=7)
+    strategy = "deLocalToBest1"
+    zeros = np.zeros(spec.n_hex)
+
+    plain = opt.DifferentialEvolution(ctx, spec.n_hex, cfg)
+    plain.set_trial_buffer(obj.sags)
+    plain.initialise(zeros, 1.0, obj)
+    f0 = plain.stats()[0]
+    h_plain, g_plain = sg.run_plain_de(plain, obj, strategy, args.seconds, 10 ** 9)
+    best_plain = plain.stats(True)
+
+    model = sg.ContrastModel(ctx, spec.n_hex, lam, hidden=(1024, 512, 256),
+                             features=args.features, seed=3)
+    scr = sg.ScreenedDE(ctx, spec.n_hex, cfg, model, draws=args.draws)
+    scr.set_trial_buffer(obj.sags)
+    scr.initialise(zeros, 1.0, obj)
+    assert abs(scr.stats()[0] - f0) <= 1e-12 * abs(f0)  # the same start
+    buf = sg.SampleBuffer(max(args.train_samples, 400000), spec.n_hex, lam)
+    h_scr, g_scr, info = sg.run_screened_de(
+        scr, obj, strategy, args.seconds, 10 ** 9, args.warm_gens, args.train_samples,
+        args.epochs, buf, np.random.default_rng(5), cfg.globalBounds)
+    best_scr = scr.stats(True)
+
+    def oracle_cost(vec):
+        """FP64 oracle contrast of one sag vector (every wavelength)."""
+        fields = [oc.piaacmc_field(inp, spec, lm, 1.0, 0.0, 0.0, vec) for lm in lam]
+        cal = [oc.piaacmc_field(inp, spec, lm, 1.0, 0.0, 0.0, vec, calibrating=True)
+               for lm in lam]
+        full = (np.abs(np.array(fields)) ** 2).sum(0)
+        cmax = (np.abs(np.array(cal)) ** 2).sum(0).max()
+        return oe.region_contrast(full, np.full_like(full, cmax), reg.mask)
+
+    checks = {}
+    for name, (bv, _, _, _, vec) in (("plain", best_plain), ("screened", best_scr)):
+        ref = oracle_cost(vec)
+        checks[name] = {"gpu": bv, "fp64_oracle": ref, "relative": abs(bv - ref) / ref}
+    d_plain, d_scr = sg.decade_times(h_plain), sg.decade_times(h_scr)
+    speedup = {k: d_plain[k] / d_scr[k] for k in d_scr if k in d_plain and d_scr[k] > 0}
+    line = {
+        "metric": "wall time to each dark-hole contrast decade (2-8 lambda/D), plain vs "
+                  "surrogate-screened GPU DE",
+        "unit": "s", "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded)",
+        "config": {"workload": "surrogate-de: DE configuration (1261 hexes, 20 rings, 5 lambda "
+                               "over 10% at 650 nm, 1024^2 chain, population 64, "
+                               "DE/local-to-best/1 F 0.7 CR 0.9, sags start within +-10 nm, "
+                               "bounds +-0.6 um) on prolate-apodized optics; MLP "
+                               f"{model.n_in}-1024-512-256-1 ({args.features} inputs), "
+                               f"{args.draws} draws x 64 screened per generation, top 64 "
+                               "propagated",
+                   "seconds_per_arm": args.seconds, "precision": args.precision},
+        "start_contrast": f0,
+        "plain": {"generations": g_plain, "best": best_plain[0], "decades_s": d_plain},
+        "screened": {"generations": g_scr, "best": best_scr[0], "decades_s": d_scr, **info},
+        "speedup_per_decade": speedup,
+        "time_to_1e-10": {"plain": d_plain.get("1e-10"), "screened": d_scr.get("1e-10")},
+        "oracle_check": checks,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 SETUP = {"piaacmc": setup_piaacmc, "plain_lyot": setup_plain_lyot, "broadband": setup_broadband,
          "de": setup_de}
 
@@ -351,8 +440,16 @@ def main():
     # field) and every FFT grid a whole number of waves
     ap.add_argument("--fields", type=int, default=152)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="piaacmc", choices=sorted(SETUP),
-                    help="piaacmc (headline), plain_lyot, broadband, de")
+    ap.add_argument("--workload", default="piaacmc", choices=sorted(SETUP) + ["surrogate"],
+                    help="piaacmc (headline), plain_lyot, broadband, de, surrogate")
+    ap.add_argument("--seconds", type=float, default=60.0,
+                    help="surrogate: wall time of each DE arm")
+    ap.add_argument("--draws", type=int, default=16, help="surrogate: trial sets per generation")
+    ap.add_argument("--warm-gens", type=int, default=300,
+                    help="surrogate: plain generations collecting training samples")
+    ap.add_argument("--train-samples", type=int, default=200000)
+    ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--features", default="sag", choices=["sag", "phasor"])
     ap.add_argument("--precision", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fft-occulter", action="store_true",
@@ -364,6 +461,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "surrogate":
+        return surrogate_experiment(args)
 
     import torch
     import ctypes as C
