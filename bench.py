@@ -358,6 +358,14 @@ def surrogate_experiment(args):
     from oracle import chain as oc
     from oracle import elements as oe
     ctx = Context(0)
+    stream = torch.cuda.Stream(0)  # graph capture needs a stream of its own
+    ctx.bind_stream(stream)
+    with torch.cuda.stream(stream):
+        return _surrogate_experiment(args, ctx, torch, cg, opt, sg, W, designed_piaacmc_spec, oc,
+                                     oe)
+
+
+def _surrogate_experiment(args, ctx, torch, cg, opt, sg, W, designed_piaacmc_spec, oc, oe):
     lam = tuple(np.linspace(650e-9 * 0.95, 650e-9 * 1.05, 5))
     spec = designed_piaacmc_spec(n_rings=20, wavelengths=lam, sag_range=0.6e-6)
     cor, inp = W.build_piaacmc(ctx, spec, precision=args.precision)
@@ -385,7 +393,7 @@ def surrogate_experiment(args):
     buf = sg.SampleBuffer(max(args.train_samples, 400000), spec.n_hex, lam)
     h_scr, g_scr, info = sg.run_screened_de(
         scr, obj, strategy, args.seconds, 10 ** 9, args.warm_gens, args.train_samples,
-        args.epochs, buf, np.random.default_rng(5), cfg.globalBounds)
+        args.epochs, buf, np.random.default_rng(5), cfg.globalBounds, batch=args.train_batch)
     best_scr = scr.stats(True)
 
     def oracle_cost(vec):
@@ -449,6 +457,7 @@ def main():
                     help="surrogate: plain generations collecting training samples")
     ap.add_argument("--train-samples", type=int, default=200000)
     ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--train-batch", type=int, default=512)
     ap.add_argument("--features", default="sag", choices=["sag", "phasor"])
     ap.add_argument("--precision", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")

@@ -121,14 +121,14 @@ class ContrastModel:
         hist = []
         for _ in range(epochs):
             perm = torch.randperm(n, device="cuda", generator=g)
-            tot, cnt = 0.0, 0
+            tot = torch.zeros((), dtype=torch.float64, device="cuda")
+            cnt = 0
             for s in range(0, n - batch + 1, batch):
                 idx = perm[s:s + batch]
                 self._load(sags[idx].contiguous(), lam[idx].contiguous())
-                loss = self.net.train_step(batch, log10c[idx].contiguous(), lr)
-                tot += float(loss.item())
+                tot += self.net.train_step(batch, log10c[idx].contiguous(), lr)[0]
                 cnt += 1
-            hist.append(tot / max(cnt, 1))
+            hist.append(float(tot.item()) / max(cnt, 1))  # one host sync per epoch
         return hist
 
     def predict(self, sags: torch.Tensor, lam: torch.Tensor) -> torch.Tensor:
@@ -137,11 +137,14 @@ class ContrastModel:
         for s in range(0, n, self.max_batch):
             e = min(n, s + self.max_batch)
             b = (e - s + 7) // 8 * 8
-            sg = torch.zeros((b, self.n_var), dtype=torch.float64, device="cuda")
-            lm = torch.full((b,), self.lam0, dtype=torch.float64, device="cuda")
-            sg[:e - s] = sags[s:e]
-            lm[:e - s] = lam[s:e]
-            self._load(sg, lm)
+            if b == e - s:  # whole batch: the inputs as they are
+                self._load(sags[s:e].contiguous(), lam[s:e].contiguous())
+            else:
+                sg = torch.zeros((b, self.n_var), dtype=torch.float64, device="cuda")
+                lm = torch.full((b,), self.lam0, dtype=torch.float64, device="cuda")
+                sg[:e - s] = sags[s:e]
+                lm[:e - s] = lam[s:e]
+                self._load(sg, lm)
             out[s:e] = self.net.forward(b)[:e - s]
         return out * self.sigma + self.mu
 
@@ -266,7 +269,7 @@ def run_plain_de(de, objective, strategy: str, seconds: float, max_gens: int):
 def run_screened_de(de: "ScreenedDE", objective: PerLambdaObjective, strategy: str,
                     seconds: float, max_gens: int, warm_gens: int, n_train: int, epochs: int,
                     buf: SampleBuffer, rng: np.random.Generator, bounds, retrain_every: int = 100,
-                    log=None):
+                    log=None, batch: int = 512):
     """Surrogate-screened DE, every step on the clock: warm_gens plain
     generations whose trials (all their fields) become training samples,
     random perturbations of the population (log-uniform scales) until
@@ -302,7 +305,8 @@ def run_screened_de(de: "ScreenedDE", objective: PerLambdaObjective, strategy: s
     perm = torch.randperm(buf.n, device="cuda")
     n_hold = buf.n // 10
     hold, tr = perm[:n_hold], perm[n_hold:]
-    model.train(buf.sags[tr], buf.lam[tr], buf.logc[tr], epochs)
+    t_gather = time.perf_counter() - t0
+    model.train(buf.sags[tr], buf.lam[tr], buf.logc[tr], epochs, batch=batch)
     pred = model.predict(buf.sags[hold], buf.lam[hold])
     rms_hold = float(torch.sqrt(((pred - buf.logc[hold]) ** 2).mean()).item())
     t_train = time.perf_counter() - t0
@@ -322,10 +326,11 @@ def run_screened_de(de: "ScreenedDE", objective: PerLambdaObjective, strategy: s
         g2 += 1
         if retrain_every and g2 % retrain_every == 0:
             xs, ls, cs = buf.recent(min(buf.n, 20 * retrain_every * P * L))
-            model.train(xs, ls, cs, 1, restandardise=False)
+            model.train(xs, ls, cs, 1, batch=batch, restandardise=False)
         hist.append((time.perf_counter() - t0, de.stats()[0]))
         if log and g2 % 200 == 0:
             log(g, hist[-1])
-    return hist, g, {"samples_s": t_samples, "trained_s": t_train, "n_samples": int(buf.n),
+    return hist, g, {"warm_generations": warm_gens, "samples_s": t_samples,
+                     "trained_s": t_train, "n_samples": int(buf.n),
                      "rms_log10_holdout": rms_hold,
                      "rms_log10_online": float(np.mean(online)) if online else None}
