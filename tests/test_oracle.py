@@ -204,3 +204,17 @@ def test_single_thread_row_check_quirk():
     a = native.interpolation_tables(d9, S, n_sub, pix, S * pix * 0.45, 0.9)
     b = native.interpolation_tables(d9, S, n_sub, pix, S * pix * 0.45, 0.9, stale=True)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_prolate_apodizer_has_eigenvalue_one_half():
+    """The designed optics' apodization: the fundamental radial prolate of a
+    focal disk whose band-limiting eigenvalue is 1/2 (a pi-phase disk then
+    cancels it in the Lyot plane), monotone from 1 at the centre to ~0.71 at
+    the pupil edge, zero outside."""
+    from csim_gb300.synth import prolate_apodizer, prolate_radial
+    a, alpha = prolate_apodizer(128, 50.0)
+    assert abs(prolate_radial(alpha)[0] - 0.5) < 1e-6
+    assert 0.52 < alpha < 0.54
+    row = a[64, 64:]
+    assert abs(row[0] - 1.0) < 1e-3 and np.all(np.diff(row[:49]) <= 1e-12)
+    assert 0.69 < row[49] < 0.73 and row[60] == 0.0
