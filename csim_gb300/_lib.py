@@ -80,6 +80,7 @@ SIGNATURES = {
     "csg_chain_add_mask": ([P, P, I, I], None),
     "csg_chain_add_mirror": ([P, P, D], None),
     "csg_chain_add_fresnel": ([P, D, D], None),
+    "csg_chain_add_fresnel_padded": ([P, D, D, D], None),
     "csg_chain_add_complex_mask": ([P, P, P, I, I, I], None),
     "csg_chain_add_fpm_hex": ([P, P, P, I, I, I, D, D, D, D, D, D, I], None),
     "csg_chain_add_fpm_hex_double": ([P, P, P, I, I, I, D, D, D, D, I], None),

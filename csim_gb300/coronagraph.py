@@ -43,8 +43,11 @@ class Mirror:
 
 @dataclass
 class FresnelPropagator:
-    """fresnelPropagator (fresnelPropagator.cpp): signed distance z."""
+    """fresnelPropagator (fresnelPropagator.cpp): signed distance z; padFactor
+    other than 1 propagates in a 2N x 2N zero-padded array with padFactor
+    times the aperture radius (fresnelPropagator.cpp:41-54)."""
     z: float
+    padFactor: float = 1.0
 
 
 @dataclass
@@ -72,6 +75,45 @@ class FpmPupToLyotMask:
     calibMask: np.ndarray | None = None
     disableForCalibration: bool = True
     maskIndex: int = -1
+
+
+@dataclass
+class ZoomFftPropagator:
+    """zoomFftPropagator (zoomFftPropagator.cpp:23-91): a zoom FFT of the
+    field to a padFactor N grid of pixel dxprime = 2 (beamRadius / (pixelScale
+    N zoomFactor)) lambda0 80 at lambda f = 3.52 lambda0 (dir +1), or back to
+    N / padFactor pixels of pixelScale at -3.52 lambda0 (dir -1); lambda0 is
+    the first wavelength, used for every wavelength as the reference does.
+    The field changes size, so it runs on its own (``propagate``), not inside
+    a Coronagraph walk: one csg_mft plan per geometry."""
+    zoomFactor: float
+    padFactor: float = 2.0
+    dir: int = 1
+
+    def geometry(self, ef: EField, n_rows: int, n_cols: int):
+        """(output y, output x, pixel, lambda f)."""
+        lam0 = float(np.asarray(ef.wavelengths)[0])
+        if self.dir == 1:
+            d = 2 * (ef.beamRadiusPhysical / (ef.pixelScale * n_rows * self.zoomFactor)) * lam0 * 80
+            nr, nc, lf = int(self.padFactor * n_rows), int(self.padFactor * n_cols), lam0 * 3.52
+        else:
+            d = ef.pixelScale
+            nr, nc = int(n_rows / self.padFactor), int(n_cols / self.padFactor)
+            lf = -lam0 * 3.52
+        return (np.arange(nr) - nr / 2.0) * d, (np.arange(nc) - nc / 2.0) * d, d, lf
+
+    def propagate(self, ctx: Context, field, ef: EField, yin, xin, dxin: float,
+                  precision: int = CSG_PREC_BF16X6):
+        """field [F][2][rows][cols] on the grid (yin, xin) of pixel dxin ->
+        (output field, (yout, xout, pixel))."""
+        from .runtime import Mft
+        n_rows, n_cols = field.shape[-2:]
+        yout, xout, d, lf = self.geometry(ef, n_rows, n_cols)
+        plan = Mft(ctx, yin, xin, yout, xout, [lf], dxin * dxin / (1j * lf), -1.0, precision)
+        out = plan(field, dvec([0] * field.shape[0], torch.int32))
+        ctx.sync()
+        plan.close()
+        return out, (yout, xout, d)
 
 
 @dataclass
@@ -204,7 +246,11 @@ class Coronagraph:
             s = _f32(e.sag)
             call("csg_chain_add_mirror", self.h, s.ctypes.data_as(C.c_void_p), e.mirrorSign)
         elif isinstance(e, FresnelPropagator):
-            call("csg_chain_add_fresnel", self.h, e.z, self.ef.arrayRadiusPhysical)
+            if e.padFactor == 1:
+                call("csg_chain_add_fresnel", self.h, e.z, self.ef.arrayRadiusPhysical)
+            else:
+                call("csg_chain_add_fresnel_padded", self.h, e.z, self.ef.arrayRadiusPhysical,
+                     float(e.padFactor))
         elif isinstance(e, ComplexMask):
             a, p = _f32(e.amp), _f32(e.ph)
             call("csg_chain_add_complex_mask", self.h, a.ctypes.data_as(C.c_void_p),

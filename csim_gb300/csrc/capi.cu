@@ -141,6 +141,9 @@ int csg_destroy(csg_ctx* c) {
   cudaStreamSynchronize(c->stream);
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   for (void* p : c->allocations) cudaFree(p);
+  for (auto& kv : c->dft_plans) csg_mft_destroy(kv.second);
+  if (c->dft_scratch) cudaFree(c->dft_scratch);
+  if (c->dft_zero) cudaFree(c->dft_zero);
   for (int k = 0; k < 2; ++k) {
     if (c->ro_buf[k]) cudaFree(c->ro_buf[k]);
     if (c->ro_ready[k]) cudaEventDestroy(c->ro_ready[k]);

@@ -201,8 +201,8 @@ extern "C" {
 int csg_chain_create(csg_ctx* ctx, csg_chain** out, int n, double pixel_scale, int n_lambda,
                      const double* lambda, int precision) {
   CSG_CHECK(ctx && out && lambda, CSG_E_ARG, "csg_chain_create: null argument");
-  CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
-            "csg_chain_create: the field must be N x N with N a power of two in [64, 4096]");
+  CSG_CHECK(n >= 64 && n <= 4096 && n % 8 == 0, CSG_E_SHAPE,
+            "csg_chain_create: the field must be N x N with N a multiple of 8 in [64, 4096]");
   CSG_CHECK(n_lambda > 0 && pixel_scale > 0, CSG_E_ARG, "csg_chain_create: bad parameters");
   CSG_CHECK(precision == CSG_PREC_BF16X6 || precision == CSG_PREC_BF16X3 ||
                 precision == CSG_PREC_HIGH,
@@ -355,6 +355,56 @@ int csg_chain_add_fresnel(csg_chain* c, double z, double ap_rad) {
       return CSG_E_NOMEM;
     }
     rc = build_fresnel_table_df(c->ctx->stream, c->n, c->lam_slots, c->n_lambda, z, ap_rad,
+                                e.tab4);
+  }
+  if (rc) {
+    cudaFree(e.tab);
+    cudaFree(e.tab4);
+    return rc;
+  }
+  c->elems.push_back(e);
+  c->planned = false;
+  drop_graph(c);
+  return CSG_OK;
+}
+
+// fresnelPropagator with padFactor != 1 (fresnelPropagator.cpp:41-54): the
+// field embedded at [N/2, 3N/2) of a 2N x 2N zero array, propagated with the
+// aperture radius padFactor apRad, and the centre cropped. It runs as the
+// padded-FFT element's band-limited passes with the Fresnel transfer
+// function of the 2N grid as the table: the first row pass reads the N field
+// rows straight from the field, the column pass moves only those rows, and
+// the last row pass writes the centre straight back (exact: the padding is
+// zero, and the crop only needs the centre rows and columns).
+int csg_chain_add_fresnel_padded(csg_chain* c, double z, double ap_rad, double pad_factor) {
+  CSG_CHECK(c && ap_rad > 0 && pad_factor > 0, CSG_E_ARG,
+            "csg_chain_add_fresnel_padded: bad argument");
+  CSG_CHECK(all_finite(&z, 1) && all_finite(&ap_rad, 1) && all_finite(&pad_factor, 1),
+            CSG_E_NAN, "csg_chain_add_fresnel_padded: non-finite argument");
+  if (pad_factor == 1.0) return csg_chain_add_fresnel(c, z, ap_rad);
+  const int P = 2 * c->n;
+  CSG_CHECK(P <= 4096 && (P & (P - 1)) == 0, CSG_E_SHAPE,
+            "csg_chain_add_fresnel_padded: 2N must be a power of two, at most 4096");
+  DeviceGuard g(c->ctx->device);
+  Elem e;
+  e.kind = E_FFT_FPM;
+  e.name = "fresnel_padded";
+  e.P = P;
+  e.bab = 0;
+  e.z = z;
+  e.ap_rad = ap_rad * pad_factor;
+  const size_t n_tab = (size_t)P * P * c->n_lambda;
+  e.tab = dev_copy<float2>(nullptr, n_tab, c->ctx->stream);
+  CSG_CHECK(e.tab, CSG_E_NOMEM, "csg_chain_add_fresnel_padded: allocation failed");
+  int rc = build_fresnel_table(c->ctx->stream, P, c->lam_slots, c->n_lambda, z, e.ap_rad, e.tab);
+  if (!rc && c->precision == CSG_PREC_HIGH) {
+    e.tab4 = dev_copy<float4>(nullptr, n_tab, c->ctx->stream);
+    if (!e.tab4) {
+      cudaFree(e.tab);
+      set_error("csg_chain_add_fresnel_padded: allocation failed");
+      return CSG_E_NOMEM;
+    }
+    rc = build_fresnel_table_df(c->ctx->stream, P, c->lam_slots, c->n_lambda, z, e.ap_rad,
                                 e.tab4);
   }
   if (rc) {
@@ -1073,7 +1123,11 @@ static int prepare(csg_chain* c) {
   const size_t F = (size_t)c->n_fields;
   size_t fpm_need = 0, ph_need = 0, img_need = 0, pad_need = 0;
   for (auto& e : c->elems) {
-    if (e.kind == E_FPM_HEX) {
+    if (e.kind == E_FRESNEL && fft_is_dft_size(c->n)) {
+      // a size that is not a power of two: the Fresnel runs as DFT transforms
+      const int rc = dft_prepare(c->ctx, c->n, c->n_fields, c->precision == CSG_PREC_HIGH);
+      if (rc) return rc;
+    } else if (e.kind == E_FPM_HEX) {
       fpm_need = std::max(fpm_need, F * 2 * e.RR * e.CC * sizeof(float));
       ph_need = std::max(ph_need, F * (e.n_hex + 1) * sizeof(float2));
       int rc = csg_mft_reserve(e.mft1, c->n_fields);
@@ -1237,7 +1291,8 @@ static std::vector<Step> plan_walk(const csg_chain* c, int calibrating) {
       if (prog[i].kind == Step::FRESNEL && prog[i + 1].kind == Step::FPM) {
         int ny = 0, nx = 0;
         mft_input_shape(prog[i + 1].e->mft1, &ny, &nx);
-        if (ny == c->n && nx == c->n && !mft_is_high(prog[i + 1].e->mft1)) {
+        if (ny == c->n && nx == c->n && !mft_is_high(prog[i + 1].e->mft1) &&
+            !fft_is_dft_size(c->n)) {
           prog[i].split_to = prog[i + 1].e->mft1;
           prog[i + 1].presplit = true;
         }
@@ -1264,7 +1319,8 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
           split = mft_split_buffer(s.split_to, F);
           CSG_CHECK(split, CSG_E_NOMEM, "Fresnel: FPM operand buffer allocation failed");
         }
-        if (fft_row_support(n, s.sup0, std::min(s.sup1, n), &sup.lo, &sup.n, high) && sup.n < n)
+        if (!fft_is_dft_size(n) &&
+            fft_row_support(n, s.sup0, std::min(s.sup1, n), &sup.lo, &sup.n, high) && sup.n < n)
           rc = fft2d_fused(ctx, c->field, F, n, -1, &fa, s.pro, s.epi, fi, nullptr, &sup, split,
                            high);
         else

@@ -9,6 +9,7 @@
 
 #include <atomic>
 #include <map>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -42,6 +43,13 @@ struct csg_ctx {
   cudaEvent_t ro_ready[2] = {nullptr, nullptr};  // staging filled (context stream)
   cudaEvent_t ro_done[2] = {nullptr, nullptr};   // staging copied out (copy stream)
   int ro_next = 0;
+  // DFT plans of non-power-of-two 2-D transforms, by (n, sign, precision),
+  // and their spectrum scratch (grow-only)
+  std::map<std::tuple<int, int, int>, csg_mft*> dft_plans;
+  void* dft_scratch = nullptr;
+  size_t dft_scratch_bytes = 0;
+  int* dft_zero = nullptr;  // operator slot 0 for every field
+  int dft_zero_n = 0;
   // opt-in per-kernel timing (CUDA events on the launching stream)
   bool prof = false;
   std::vector<csg::ProfPending> pending;

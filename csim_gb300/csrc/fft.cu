@@ -900,14 +900,155 @@ static int run_fft_n(csg_ctx* ctx, float* field, int F, int n, int direction,
   }
 }
 
+// ------------------------------------ sizes that are not powers of two
+// The reference plans FFTW for any size (csim_fft.cpp:111-115). Sizes the
+// register FFT does not cover (multiples of 8 that are not powers of two, up
+// to 8192) run the 2-D DFT as a matrix Fourier transform on the tensor cores:
+// X[k1][k2] = sum x[n1][n2] exp(-+2 pi i (n1 k1 + n2 k2) / N), i.e. integer
+// coordinates and lambda f = N, so every operator phase is exact in FP64;
+// the inverse carries the 1 / N^2. A Fresnel propagation multiplies the
+// spectrum by the transfer function between the two (in FFT order, the
+// table of its wavelength slot or evaluated in place). O(N^3) work instead
+// of O(N^2 log N), on the tensor cores.
+static int dft_plan(csg_ctx* ctx, int n, int sgn, int precision, csg_mft** out) {
+  const auto key = std::make_tuple(n, sgn, precision);
+  auto it = ctx->dft_plans.find(key);
+  if (it != ctx->dft_plans.end()) {
+    *out = it->second;
+    return CSG_OK;
+  }
+  std::vector<double> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = (double)i;
+  const double lf = (double)n;
+  const double pref[2] = {sgn > 0 ? 1.0 / ((double)n * (double)n) : 1.0, 0.0};
+  csg_mft* m = nullptr;
+  const int rc = csg_mft_create(ctx, &m, n, n, n, n, idx.data(), idx.data(), idx.data(),
+                                idx.data(), 1, &lf, pref, (double)sgn, precision);
+  if (rc) return rc;
+  ctx->dft_plans[key] = m;
+  *out = m;
+  return CSG_OK;
+}
+
+// The spectrum times the Fresnel transfer function of each field's
+// wavelength (FFT order), from the table or evaluated here.
+__global__ void k_fresnel_mul(float* __restrict__ spec, int N, const __grid_constant__ FresnelArgs fa) {
+  const int f = blockIdx.y;
+  const size_t plane = (size_t)N * N;
+  float* re = spec + (size_t)f * 2 * plane;
+  float* im = re + plane;
+  __shared__ FresnelConsts shc;
+  if (!fa.H && !fa.H4) {
+    if (threadIdx.x == 0) shc = fresnel_consts(fa.lambda[f], fa.z, fa.ap_rad);
+    __syncthreads();
+  }
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < plane;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float2 w;
+    if (fa.H4) {
+      const float4 h = fa.H4[(size_t)fa.slot[f] * plane + i];
+      w = make_float2(h.x + h.y, h.z + h.w);
+    } else if (fa.H) {
+      w = fa.H[(size_t)fa.slot[f] * plane + i];
+    } else {
+      w = fresnel_h(N, (int)(i / N), (int)(i % N), shc);
+    }
+    const float a = re[i], b = im[i];
+    re[i] = a * w.x - b * w.y;
+    im[i] = a * w.y + b * w.x;
+  }
+}
+
+// Plans, spectrum scratch and the all-zero slot vector of F fields of size n
+// (allocates: called before any capture; the chain calls it when planning).
+int dft_prepare(csg_ctx* ctx, int n, int F, bool high) {
+  CSG_CHECK(n % 8 == 0 && n <= 8192, CSG_E_SHAPE,
+            "FFT: sizes that are not powers of two must be multiples of 8, at most 8192");
+  const int prec = high ? CSG_PREC_HIGH : CSG_PREC_BF16X6;
+  csg_mft* m = nullptr;
+  int rc = dft_plan(ctx, n, -1, prec, &m);
+  if (!rc) rc = dft_plan(ctx, n, +1, prec, &m);
+  if (rc) return rc;
+  const size_t bytes = (size_t)F * 2 * n * n * sizeof(float);
+  if (ctx->dft_scratch_bytes < bytes) {
+    if (ctx->dft_scratch) cudaFree(ctx->dft_scratch);
+    ctx->dft_scratch = nullptr;
+    ctx->dft_scratch_bytes = 0;
+    CSG_CUDA(cudaMalloc(&ctx->dft_scratch, bytes));
+    ctx->dft_scratch_bytes = bytes;
+  }
+  if (ctx->dft_zero_n < F) {
+    if (ctx->dft_zero) cudaFree(ctx->dft_zero);
+    ctx->dft_zero = nullptr;
+    ctx->dft_zero_n = 0;
+    CSG_CUDA(cudaMalloc((void**)&ctx->dft_zero, sizeof(int) * F));
+    CSG_CUDA(cudaMemset(ctx->dft_zero, 0, sizeof(int) * F));
+    ctx->dft_zero_n = F;
+  }
+  for (int i = 0; i < F; i += 65535) {  // the split kernels' grid.y bound
+    csg_mft* p = nullptr;
+    dft_plan(ctx, n, -1, prec, &p);
+    if ((rc = csg_mft_reserve(p, std::min(F - i, 65535)))) return rc;
+    dft_plan(ctx, n, +1, prec, &p);
+    if ((rc = csg_mft_reserve(p, std::min(F - i, 65535)))) return rc;
+  }
+  return CSG_OK;
+}
+
+static int dft2d_mft(csg_ctx* ctx, float* field, int F, int n, int direction,
+                     const FresnelArgs* fa, const PixOps& pro, const PixOps& epi,
+                     const FieldInfo& fi, bool high) {
+  cudaStream_t st = ctx->stream;
+  const int prec = high ? CSG_PREC_HIGH : CSG_PREC_BF16X6;
+  const size_t bytes = (size_t)F * 2 * n * n * sizeof(float);
+  auto fit = ctx->dft_plans.find(std::make_tuple(n, -1, prec));
+  auto iit = ctx->dft_plans.find(std::make_tuple(n, +1, prec));
+  CSG_CHECK(fit != ctx->dft_plans.end() && iit != ctx->dft_plans.end() &&
+                ctx->dft_scratch_bytes >= bytes && ctx->dft_zero_n >= F,
+            CSG_E_STATE, "FFT: the DFT of this size was not prepared (dft_prepare)");
+  int rc = CSG_OK;
+  if (pro.n && (rc = pixops_pass(st, field, F, n, n, pro, fi))) return rc;
+  float* tmp = static_cast<float*>(ctx->dft_scratch);
+  const int* zero = ctx->dft_zero;  // every field on operator slot 0
+  csg_mft *fwd = fit->second, *inv = iit->second;
+  {
+    if (fa) {
+      rc = mft_execute_ops(ctx, fwd, field, tmp, F, zero, 0, nullptr, nullptr, PixOps(), fi);
+      if (!rc) {
+        dim3 grid(grid_for((long long)n * n, 256, 512), F);
+        k_fresnel_mul<<<grid, 256, 0, st>>>(tmp, n, *fa);
+        CSG_LAUNCH_CHECK();
+      }
+      if (!rc)
+        rc = mft_execute_ops(ctx, inv, tmp, field, F, zero, 0, nullptr, nullptr, PixOps(), fi);
+    } else {
+      rc = mft_execute_ops(ctx, direction < 0 ? fwd : inv, field, tmp, F, zero, 0, nullptr,
+                           nullptr, PixOps(), fi);
+      if (!rc && cudaMemcpyAsync(field, tmp, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+        set_error("FFT: copy failed");
+        rc = CSG_E_CUDA;
+      }
+    }
+  }
+  if (!rc && epi.n) rc = pixops_pass(st, field, F, n, n, epi, fi);
+  return rc;
+}
+
+bool fft_is_dft_size(int n) { return n >= 8 && (n & (n - 1)) != 0; }
+
 // 2-D FFT or Fresnel propagation of F square N x N fields with fused element
 // ops (pro before the transform, epi after it); high: two-float arithmetic.
 int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const FresnelArgs* fa,
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi, const FftBand* band,
                 const FftBand* support, __nv_bfloat16* split_out, bool high) {
-  CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
-            "FFT size must be a power of two in [64, 4096]");
   CSG_CHECK(F > 0 && (long long)F * n < (1LL << 31), CSG_E_SHAPE, "FFT: bad field count");
+  if (fft_is_dft_size(n)) {
+    CSG_CHECK(!band && !support && !split_out, CSG_E_ARG,
+              "FFT: band, support and split outputs need a power-of-two size");
+    return dft2d_mft(ctx, field, F, n, direction, fa, pro, epi, fi, high);
+  }
+  CSG_CHECK(n >= 64 && n <= 4096, CSG_E_SHAPE,
+            "FFT: power-of-two sizes must be in [64, 4096]");
   FftBand bd, sp;
   if (band) {
     CSG_CHECK(fa && !pro.n && !epi.n && band->src && band->dst && !band->split && !support &&
@@ -956,6 +1097,10 @@ int csg_fft2d(csg_ctx* ctx, float* field, int n_fields, int n, int direction) {
   CSG_CHECK(ctx && field, CSG_E_ARG, "csg_fft2d: null argument");
   CSG_CHECK(direction == -1 || direction == 1, CSG_E_ARG, "csg_fft2d: direction must be -1 or +1");
   DeviceGuard g(ctx->device);
+  if (fft_is_dft_size(n)) {
+    const int rc = dft_prepare(ctx, n, n_fields, false);
+    if (rc) return rc;
+  }
   return fft2d_fused(ctx, field, n_fields, n, direction, nullptr, PixOps(), PixOps(), FieldInfo());
 }
 
@@ -968,6 +1113,10 @@ int csg_fft2d_prec(csg_ctx* ctx, float* field, int n_fields, int n, int directio
   CSG_CHECK(direction == -1 || direction == 1, CSG_E_ARG,
             "csg_fft2d_prec: direction must be -1 or +1");
   DeviceGuard g(ctx->device);
+  if (fft_is_dft_size(n)) {
+    const int rc = dft_prepare(ctx, n, n_fields, precision == CSG_PREC_HIGH);
+    if (rc) return rc;
+  }
   return fft2d_fused(ctx, field, n_fields, n, direction, nullptr, PixOps(), PixOps(), FieldInfo(),
                      nullptr, nullptr, nullptr, precision == CSG_PREC_HIGH);
 }
@@ -979,6 +1128,10 @@ int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* l
             "csg_fresnel: non-finite distance or aperture radius");
   CSG_CHECK(ap_rad > 0, CSG_E_ARG, "csg_fresnel: apRad must be positive");
   DeviceGuard g(ctx->device);
+  if (fft_is_dft_size(n)) {
+    const int rc = dft_prepare(ctx, n, n_fields, false);
+    if (rc) return rc;
+  }
   FresnelArgs fa{lambda, z, ap_rad};
   return fft2d_fused(ctx, field, n_fields, n, -1, &fa, PixOps(), PixOps(), FieldInfo());
 }
@@ -993,10 +1146,14 @@ int csg_fresnel_prec(csg_ctx* ctx, float* field, int n_fields, int n, const doub
   CSG_CHECK(all_finite(&z, 1) && all_finite(&ap_rad, 1), CSG_E_NAN,
             "csg_fresnel_prec: non-finite distance or aperture radius");
   CSG_CHECK(ap_rad > 0, CSG_E_ARG, "csg_fresnel_prec: apRad must be positive");
-  CSG_CHECK(n >= 64 && n <= 4096 && (n & (n - 1)) == 0, CSG_E_SHAPE,
-            "FFT size must be a power of two in [64, 4096]");
   CSG_CHECK(n_fields > 0, CSG_E_SHAPE, "csg_fresnel_prec: n_fields must be positive");
   DeviceGuard g(ctx->device);
+  if (fft_is_dft_size(n)) {
+    const int rc = dft_prepare(ctx, n, n_fields, true);
+    if (rc) return rc;
+  } else {
+    CSG_CHECK(n >= 64 && n <= 4096, CSG_E_SHAPE, "FFT: power-of-two sizes must be in [64, 4096]");
+  }
   cudaStream_t st = ctx->stream;
   // one two-float transfer function per field (its own wavelength), built in
   // FP64 for this call: the fields' slot is their own index

@@ -299,6 +299,11 @@ int fft2d_fused(csg_ctx* ctx, float* field, int F, int n, int direction, const F
                 const PixOps& pro, const PixOps& epi, const FieldInfo& fi,
                 const FftBand* band = nullptr, const FftBand* support = nullptr,
                 __nv_bfloat16* split_out = nullptr, bool high = false);
+// Sizes that are not powers of two: the 2-D DFT runs as a matrix Fourier
+// transform; dft_prepare creates its plans and buffers for F fields
+// (allocates, so before any graph capture).
+bool fft_is_dft_size(int n);
+int dft_prepare(csg_ctx* ctx, int n, int F, bool high);
 // Whether fft2d_fused can run an N-point padded transform band-limited to
 // [lo, lo + n) (fp32 or two-float passes).
 bool fft_band_supported(int N, int lo, int n, bool high = false);

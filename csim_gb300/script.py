@@ -265,9 +265,8 @@ class _Builder:
             return cg.Mirror(sag.astype(np.float32), _float(blk.get("sign", "1")))
         if k == "fresnelPropagator":
             _check_keys(blk, _COMMON | {"propagationSign", "padFactor"})
-            if _float(blk.get("padFactor", "1")) != 1:
-                raise ScriptError("fresnelPropagator: padFactor other than 1 is not supported")
-            return ("fresnel", _float(blk.get("propagationSign", "1")))
+            return ("fresnel", _float(blk.get("propagationSign", "1")),
+                    _float(blk.get("padFactor", "1")))
         if k == "complexMask":
             _check_keys(blk, _COMMON | {"filename", "maskIndex"})
             if int(_float(blk.get("maskIndex", "0"))) != 0:
@@ -399,7 +398,7 @@ def load(path: str, ctx, base_dir: str | None = None, precision: int = 6) -> Scr
         if isinstance(e, tuple) and e[0] == "fresnel":
             if i == 0 or i == len(built) - 1:
                 raise ScriptError("fresnelPropagator needs an element before and after it")
-            elems.append(cg.FresnelPropagator(e[1] * abs(pos[i + 1] - pos[i - 1])))
+            elems.append(cg.FresnelPropagator(e[1] * abs(pos[i + 1] - pos[i - 1]), e[2]))
         else:
             elems.append(e)
     cor = cg.Coronagraph(ctx, tel, ef, elems, precision)

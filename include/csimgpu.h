@@ -155,7 +155,11 @@ int csg_complex_mask(csg_ctx* ctx, float* field, int n_fields, int rows, int col
 /* ------------------------------------------------------ 2-D transforms */
 /* fft::execute / ifft::execute on a square N x N slice (csim_fft.cpp:62-95,
  * :127, :192-193): forward exp(-i), inverse exp(+i) divided by N^2.
- * N is a power of two, 64 <= N <= 4096. direction: -1 forward, +1 inverse. */
+ * N a power of two in [64, 4096] (register-resident FFT passes), or any other
+ * multiple of 8 up to 8192, which FFTW plans as well (csim_fft.cpp:111-115):
+ * those run as an exact-phase DFT matrix product on the tensor cores (O(N^3);
+ * the first call for a size builds and keeps its plans in the context).
+ * direction: -1 forward, +1 inverse. */
 int csg_fft2d(csg_ctx* ctx, float* field, int n_fields, int n, int direction);
 /* csg_fft2d with a precision: CSG_PREC_HIGH runs the passes in two-float
  * arithmetic (about 48-bit intermediates; fields stay fp32 in memory). */
@@ -277,7 +281,9 @@ int csg_hex_tables(csg_ctx* ctx, const double* hex_x, const double* hex_y, int n
  * the list is built with the csg_chain_add_* calls (in optical order) and one
  * csg_chain_execute runs every element once over a whole batch of fields,
  * each field one (wavelength, source, candidate) triple. The field is
- * N x N (N a power of two) at pixel_scale metres; lambda[n_lambda] are the
+ * N x N (N a multiple of 8 in [64, 4096]; a Fresnel element at a size that
+ * is not a power of two runs as DFT products, see csg_fft2d) at pixel_scale
+ * metres; lambda[n_lambda] are the
  * efield's wavelengths (efield.cpp:351-417). `precision` is CSG_PREC_*. */
 int csg_chain_create(csg_ctx* ctx, csg_chain** chain, int n, double pixel_scale, int n_lambda,
                      const double* lambda, int precision);
@@ -292,6 +298,12 @@ int csg_chain_add_mirror(csg_chain* chain, const float* sag, double sign);
  * propagationSign |next.position - prev.position|, ap_rad = the efield's
  * arrayRadiusPhysical (efield.cpp:419-430). */
 int csg_chain_add_fresnel(csg_chain* chain, double z, double ap_rad);
+/* fresnelPropagator with padFactor (fresnelPropagator.cpp:41-54): the field
+ * is embedded at the centre of a 2N x 2N zero array, propagated with aperture
+ * radius pad_factor ap_rad (the reference's padded array is 2N for any
+ * padFactor other than 1) and cropped back; pad_factor 1 is
+ * csg_chain_add_fresnel. 2N at most 4096. */
+int csg_chain_add_fresnel_padded(csg_chain* chain, double z, double ap_rad, double pad_factor);
 /* complexMask (complexMask.cpp:24-66): centred amp exp(-i ph), host fp32. */
 int csg_chain_add_complex_mask(csg_chain* chain, const float* amp, const float* ph, int mrows,
                                int mcols, int disable_for_calibration);

@@ -368,3 +368,32 @@ def opt_hex_resp_objective(m_cubes, wavelengths, calib: float, x: np.ndarray,
             pix += (e * e.conj()).real
     red = pix.mean(0) if objective == "mean" else pix.max(0)
     return red / calib
+
+
+# ---------------------------------------------------- zoomFftPropagator --
+def zoom_fft_propagator_geometry(n_rows: int, n_cols: int, beam_radius: float,
+                                 pixel_scale: float, lambda0: float, zoom_factor: float,
+                                 pad_factor: float, direction: int):
+    """zoomFftPropagator::execute (zoomFftPropagator.cpp:23-91): the output
+    grid and lambda f. dir +1: padFactor N pixels of dxprime =
+    2 (beamRadius / (pixelScale N zoomFactor)) lambda0 80 at (i - n/2) dxprime,
+    lambda f = 3.52 lambda0; dir -1: N / padFactor pixels of pixelScale at
+    (i - n/2) pixelScale, lambda f = -3.52 lambda0 (lambda0: the first
+    wavelength, for every slice)."""
+    if direction == 1:
+        d = 2 * (beam_radius / (pixel_scale * n_rows * zoom_factor)) * lambda0 * 80
+        nr, nc, lf = int(pad_factor * n_rows), int(pad_factor * n_cols), lambda0 * 3.52
+    else:
+        d = pixel_scale
+        nr, nc, lf = int(n_rows / pad_factor), int(n_cols / pad_factor), -lambda0 * 3.52
+    return ArrayGeom((np.arange(nc) - nc / 2.0) * d, (np.arange(nr) - nr / 2.0) * d, d, d), lf
+
+
+def zoom_fft_propagator(cube, gin: ArrayGeom, beam_radius: float, pixel_scale: float,
+                        lambdas, zoom_factor: float, pad_factor: float, direction: int):
+    """The element on every slice: zoomFft from gin to the element's grid."""
+    n_rows, n_cols = cube.shape[-2:]
+    gout, lf = zoom_fft_propagator_geometry(n_rows, n_cols, beam_radius, pixel_scale,
+                                            float(lambdas[0]), zoom_factor, pad_factor, direction)
+    z = ZoomFft(gin, gout, [lf] * len(lambdas))
+    return np.stack([z.mft(cube[k], k) for k in range(len(lambdas))]), gout

@@ -15,6 +15,7 @@ import pytest
 import torch
 
 from oracle import chain as oc
+from oracle import csim_fft as of
 from oracle import elements as oe
 from oracle import native
 
@@ -485,3 +486,76 @@ def test_reference_calibration_first_wavelength_only(ctx):
     assert torch.equal(cal1[first], cal0[first])
     assert cal0[second].abs().max().item() > 0
     assert cal1[second].abs().max().item() == 0.0
+
+
+@pytest.mark.parametrize("precision", [6, 16])
+def test_padded_fresnel_matches_oracle(ctx, precision):
+    """fresnelPropagator with padFactor 2 (fresnelPropagator.cpp:41-54): the
+    field propagated in a 2N zero-padded array with twice the aperture
+    radius, cropped; the chain's band-limited padded passes against the FP64
+    oracle's explicit pad / propagate / crop."""
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import workloads as W
+    spec = small_spec(wavelengths=(640e-9, 660e-9), z=0.4)
+    a = W.piaacmc_arrays(spec, [cg.PointSource(1.0, 0.0, 0.0), cg.PointSource(0.7, 0.03, 0.0)])
+    ef, tel = a["ef"], a["tel"]
+    elems = [cg.Mask(a["pupil"]), cg.Mirror(a["sag1"], 1.0), cg.FresnelPropagator(spec.z, 2.0),
+             cg.Mirror(a["sag2"], -1.0), cg.Mask(a["lyot"]),
+             cg.FraunhoferFocal(a["lam_ref"], spec.spl, spec.n_out_fov)]
+    cor = cg.Coronagraph(ctx, tel, ef, elems, precision, True)
+    F = cor.batch_all(1)
+    im = cor.execute().clone()
+    full = im.double() + (cor.image_lo().double() if precision == 16 else 0.0)
+    ctx.sync()
+    got = full[:, 0].cpu().numpy() + 1j * full[:, 1].cpu().numpy()
+    li, amp, tip, tilt, _ = cor._batch
+    n, dx = spec.n, a["dx"]
+    geom = of.ArrayGeom.set_xy(n, n, dx)
+    n_out = int(np.ceil(spec.n_out_fov * spec.spl))
+    gout = of.ArrayGeom.set_xy(n_out, n_out, a["lod_image"] / spec.spl)
+    err, peak = 0.0, 0.0
+    for f in range(F):
+        lam = float(a["lam"][li[f]])
+        e = oe.point_source_field(geom, 1, amp[f] * amp[f], tip[f], tilt[f])
+        e = oe.mask_apply(e, a["pupil"])
+        e = oe.mirror_apply(e, a["sag1"].astype(np.float64), [lam], 1.0)
+        e = oe.fresnel_element(e, [lam], ef.arrayRadiusPhysical, spec.z, pad=2)
+        e = oe.mirror_apply(e, a["sag2"].astype(np.float64), [lam], -1.0)
+        e = oe.mask_apply(e, a["lyot"])
+        ref = oe.fraunhofer_focal(e, geom, gout, [lam], ef.beamRadiusPhysical,
+                                  tel.primaryfRatio)[0]
+        peak = max(peak, np.abs(ref).max())
+        err = max(err, np.abs(got[f] - ref).max())
+    err /= peak
+    print(f"\npadded Fresnel (padFactor 2) precision {precision}: field error {err:.3e} of the "
+          "image peak")
+    assert err < (1e-7 if precision == 16 else 1e-6), err
+    cor.close()
+
+
+def test_zoom_fft_propagator_pair_matches_oracle(ctx):
+    """zoomFftPropagator (zoomFftPropagator.cpp:23-91) out to the padded zoom
+    grid and back, one wavelength (the element takes the first wavelength's
+    lambda f for every slice), against the oracle's restatement."""
+    from csim_gb300 import coronagraph as cg
+    from csim_gb300 import runtime as R
+    from csim_gb300.synth import EField, PointSource, circle_mask
+    n, br = 128, 0.01
+    dx = 2 * br / 100
+    lam = np.array([6.5e-7])
+    ef = EField(n, br, dx, lam, [PointSource()])
+    geom = of.ArrayGeom.set_xy(n, n, dx)
+    e = oe.mask_apply(oe.point_source_field(geom, 1, 1.0, 0.1, 0.0), circle_mask(n, 50.0))
+    out_ref, g1 = oe.zoom_fft_propagator(e, geom, br, dx, lam, 4.0, 2.0, 1)
+    back_ref, g2 = oe.zoom_fft_propagator(out_ref, g1, br, dx, lam, 4.0, 2.0, -1)
+    fwd = cg.ZoomFftPropagator(4.0, 2.0, 1)
+    out, (y1, x1, d1) = fwd.propagate(ctx, R.to_planar(e), ef, geom.pixelY, geom.pixelX, dx)
+    assert np.allclose(x1, g1.pixelX) and d1 == g1.pixelSizeX
+    inv = cg.ZoomFftPropagator(4.0, 2.0, -1)
+    back, (y2, x2, d2) = inv.propagate(ctx, out, ef, y1, x1, d1)
+    got1, got2 = R.from_planar(out)[0], R.from_planar(back)[0]
+    e1 = np.abs(got1 - out_ref[0]).max() / np.abs(out_ref[0]).max()
+    e2 = np.abs(got2 - back_ref[0]).max() / np.abs(back_ref[0]).max()
+    print(f"\nzoomFftPropagator pair: {e1:.3e}, {e2:.3e}")
+    assert got1.shape == (256, 256) and got2.shape == (128, 128)
+    assert e1 < 1e-6 and e2 < 1e-6

@@ -125,7 +125,8 @@ def test_unsupported_input_raises(tmp_path):
         b.element(S.Block("zoomDftPropagator"), None, None)
     with pytest.raises(S.ScriptError, match="key"):
         b.element(S.Block("fresnelPropagator", [("bogus", "1")]), None, None)
-    with pytest.raises(S.ScriptError, match="padFactor"):
-        b.element(S.Block("fresnelPropagator", [("padFactor", "2")]), None, None)
+    # padFactor is supported: the element carries it
+    assert b.element(S.Block("fresnelPropagator", [("padFactor", "2")]), None, None) == \
+        ("fresnel", 1.0, 2.0)
     with pytest.raises(S.ScriptError, match="on or off"):
         b.element(S.Block("mask", [("disableForCalibration", "yes")]), None, None)
