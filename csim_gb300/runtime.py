@@ -30,7 +30,7 @@ def to_planar(e: np.ndarray, device="cuda") -> torch.Tensor:
     reference-facing path)."""
     e = np.asarray(e)
     e = e.reshape((-1,) + e.shape[-2:])
-    out = np.stack([e.real, e.imag], axis=1).astype(np.float32)
+    out = np.ascontiguousarray(np.stack([e.real, e.imag], axis=1), dtype=np.float32)
     return torch.from_numpy(out).to(device)
 
 
