@@ -41,7 +41,12 @@ class Fp64Piaacmc:
     dtype=torch.complex64 gives the same plain path in single precision
     (every table, field and product complex64): the precision comparator."""
 
-    def __init__(self, inp: dict, spec, device: str = "cuda", dtype=torch.complex128):
+    def __init__(self, inp: dict, spec, device: str = "cuda", dtype=torch.complex128,
+                 fpm_box=None):
+        """fpm_box (r0, c0, rows, cols): transform only that box of the mask
+        grid (where fliplr(M) - 1 can be nonzero) and only the Lyot stop's
+        bounding window of the pupil plane, the exact crops the GPU chain
+        makes, so the comparison isolates precision and batching."""
         self.dev = torch.device(device)
         self.dtype = dtype
         ef, tel = inp["ef"], inp["tel"]
@@ -61,6 +66,11 @@ class Fp64Piaacmc:
         fr = np.fft.fftfreq(n, 1.0 / n)  # integer frequency index in FFT order
         f2 = fr[:, None] ** 2 + fr[None, :] ** 2
         ap_rad = ef.arrayRadiusPhysical
+        self.box = fpm_box
+        if fpm_box is not None:
+            nz = np.nonzero(inp["lyot"])
+            self.win = (int(nz[0].min()), int(nz[0].max()) + 1, int(nz[1].min()),
+                        int(nz[1].max()) + 1)
         self.per_lam = []
         for lam in inp["lam"]:
             k = 2.0 * math.pi / lam
@@ -98,6 +108,20 @@ class Fp64Piaacmc:
         e = amp * c(p["pre"])
         e = torch.fft.ifft2(torch.fft.fft2(e) * c(p["H"]))
         e = e * c(p["m2"])
+        if self.box is not None:  # the support box and the Lyot window only
+            r0, c0, R, C = self.box
+            w0, w1, v0, v1 = self.win
+            if not calibrating:
+                A1, A2 = c(p["A1"]), c(p["A2"])
+                f = A1[r0:r0 + R] @ e @ A1[c0:c0 + C].T
+                m = c(self.mask(sags, p["lam"]))[r0:r0 + R, c0:c0 + C]
+                g = complex(p["c"]) * (A2[w0:w1, r0:r0 + R] @ (m * f) @ A2[v0:v1, c0:c0 + C].T)
+                ew = e[w0:w1, v0:v1] + g
+            else:
+                ew = e[w0:w1, v0:v1]
+            ew = ew * c(self.lyot)[w0:w1, v0:v1]
+            A3 = c(p["A3"])
+            return complex(p["pref3"]) * (A3[:, w0:w1] @ ew @ A3[:, v0:v1].T)
         if not calibrating:
             A1, A2 = c(p["A1"]), c(p["A2"])
             f = A1 @ e @ A1.T  # square grids: the same operator on both axes

@@ -90,3 +90,62 @@ def test_sharded_de_matches_single_process():
         assert np.array_equal(pop, ref_pop), rank
         assert np.array_equal(f, ref_f), rank
         assert best == ref_best
+
+
+class _ChainLikeObjective:
+    """A CPU stand-in for optimize.PropagatedObjective with its call shape:
+    a fixed batch of `pop` candidates whose sags are copied into the
+    objective's own buffer (the chain's sag buffer) before evaluating, and
+    a cost per candidate: here the response-matrix contrast of the oracle
+    (optObjective.cpp:24-69) on a seeded matrix."""
+
+    def __init__(self, pop, nvar, seed=3):
+        rng = np.random.default_rng(seed)
+        self.m = (rng.standard_normal((2, 40, nvar + 1))
+                  + 1j * rng.standard_normal((2, 40, nvar + 1)))
+        self.lam = np.array([6.3e-7, 6.7e-7])
+        self.sags = torch.zeros((pop, nvar), dtype=torch.float64)
+        self.pop = pop
+
+    def __call__(self, x, out):
+        if x.shape[0] != self.pop:
+            raise ValueError("batch size differs from the chain's")
+        self.sags.copy_(x)
+        from oracle.elements import opt_hex_resp_objective
+        v = opt_hex_resp_objective(self.m, self.lam, 1.0, self.sags.numpy().T * 1e-7)
+        out.copy_(torch.as_tensor(np.asarray(v, np.float64).ravel()))
+        return out
+
+
+def _worker_chain(rank, world, port, q):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        lo, hi = shard_range(10, rank, world)  # each rank's chain holds its slice
+        pop, f, best = _run_de(ShardedObjective(_ChainLikeObjective(hi - lo, 6)))
+        q.put((rank, pop, f, best))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_propagated_objective_matches_single_process():
+    """ShardedObjective around an objective with PropagatedObjective's call
+    shape: every rank builds its chain for its own slice of the population
+    (shard_range), and the sharded DE equals one process evaluating the whole
+    population with one chain."""
+    ref_pop, ref_f, ref_best = _run_de(_ChainLikeObjective(10, 6))
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    world, port = 2, _free_port()
+    procs = [ctx.Process(target=_worker_chain, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=120) for _ in range(world)]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, pop, f, best in got:
+        assert np.array_equal(pop, ref_pop), rank
+        assert np.array_equal(f, ref_f), rank
+        assert best == ref_best
