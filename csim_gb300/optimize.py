@@ -100,6 +100,11 @@ class GraphedGeneration:
 
     def __init__(self, de: "DifferentialEvolution", strategy: str, objective,
                  stream: torch.cuda.Stream):
+        from .sharding import ShardedObjective
+        if isinstance(objective, ShardedObjective):
+            # the per-generation all-gather stays outside captured graphs: a
+            # sharded generation runs eager, the chain's own graph replayed
+            raise ValueError("a sharded objective runs the eager generation, not a captured one")
         self.de, self.graph = de, torch.cuda.CUDAGraph()
         code = STRATEGIES[strategy]
         cfg = de.cfg

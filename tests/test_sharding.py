@@ -149,3 +149,12 @@ def test_sharded_propagated_objective_matches_single_process():
         assert np.array_equal(pop, ref_pop), rank
         assert np.array_equal(f, ref_f), rank
         assert best == ref_best
+
+
+def test_sharded_objective_not_captured_in_generation_graph():
+    """The all-gather stays outside captured graphs: GraphedGeneration
+    refuses a ShardedObjective before touching the device."""
+    from csim_gb300.optimize import GraphedGeneration
+    sharded = object.__new__(ShardedObjective)
+    with pytest.raises(ValueError, match="eager"):
+        GraphedGeneration(None, "deRand1", sharded, None)
