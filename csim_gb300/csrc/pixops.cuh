@@ -92,33 +92,50 @@ __device__ __forceinline__ float pick(const float* v, int i) {
   return x;
 }
 
+// OP_SOURCE for NE pixels (r + e dr, c + e dc): replaces them by the point
+// source's field (flat for an on-axis source).
+template <int NE>
+__device__ __forceinline__ void pix_source_n(const PixConsts& k, int r, int c, int dr, int dc,
+                                             int R, int C, float* re, float* im) {
+  if (k.sxh == 0.f && k.syh == 0.f && k.sxl == 0.f && k.syl == 0.f) {
+#pragma unroll
+    for (int e = 0; e < NE; ++e) re[e] = k.amp, im[e] = 0.f;
+  } else {
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      const float xc = (float)(c + e * dc) - 0.5f * (float)(C - 1);
+      const float yr = (float)(r + e * dr) - 0.5f * (float)(R - 1);
+      float t = frac_prod(xc, k.sxh, k.sxl) + frac_prod(yr, k.syh, k.syl);
+      t -= rintf(t);
+      float s, co;
+      sincospif(2.f * t, &s, &co);
+      re[e] = k.amp * co;
+      im[e] = k.amp * s;
+    }
+  }
+}
+
 // Apply the ops to NE pixels (r + e dr, c + e dc), e < NE, of an R x C field
 // held in registers. Ops are applied one at a time over all NE pixels, so
-// each op's NE table reads are issued together.
+// each op's NE table reads are issued together. OP_SOURCE is only ever the
+// first op (it replaces the pixel) and is applied before the op loop: its
+// per-pixel phase does not depend on the op, and inside the loop the
+// compiler would hoist that arithmetic out of it and evaluate it for every
+// op program, with or without a source.
 template <int NE>
 __device__ __forceinline__ void pix_apply_n(const PixOps& ops, const PixConsts& k, int r, int c,
                                             int dr, int dc, int R, int C, float* re, float* im) {
+  int i0 = 0;
+  if (ops.n && ops.kind[0] == OP_SOURCE) {
+    pix_source_n<NE>(k, r, c, dr, dc, R, C, re, im);
+    i0 = 1;
+  }
 #pragma unroll 1
-  for (int i = 0; i < ops.n; ++i) {
+  for (int i = i0; i < ops.n; ++i) {
     const int kind = ops.kind[i];
     const float* a = ops.a[i];
     if (kind == OP_SOURCE) {
-      if (k.sxh == 0.f && k.syh == 0.f && k.sxl == 0.f && k.syl == 0.f) {
-#pragma unroll
-        for (int e = 0; e < NE; ++e) re[e] = k.amp, im[e] = 0.f;
-      } else {
-#pragma unroll
-        for (int e = 0; e < NE; ++e) {
-          const float xc = (float)(c + e * dc) - 0.5f * (float)(C - 1);
-          const float yr = (float)(r + e * dr) - 0.5f * (float)(R - 1);
-          float t = frac_prod(xc, k.sxh, k.sxl) + frac_prod(yr, k.syh, k.syl);
-          t -= rintf(t);
-          float s, co;
-          sincospif(2.f * t, &s, &co);
-          re[e] = k.amp * co;
-          im[e] = k.amp * s;
-        }
-      }
+      continue;  // never past the first op
     } else if (kind == OP_MASK) {
       float m[NE];
 #pragma unroll
