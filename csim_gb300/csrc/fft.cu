@@ -195,20 +195,60 @@ constexpr int bitrev(int q, int bits) {
 }
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
+// Packed fp32 pairs: one add.f32x2 / sub.f32x2 instruction for two sums
+// (the register pairs are formed and split by mov.b64, which costs nothing
+// when the two values sit in adjacent registers).
+__device__ __forceinline__ void add2(float a0, float a1, float b0, float b1, float& s0, float& s1) {
+  asm("{\n\t.reg .b64 x, y, r;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+      "add.rn.f32x2 r, x, y;\n\tmov.b64 {%0, %1}, r;\n\t}"
+      : "=f"(s0), "=f"(s1)
+      : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+__device__ __forceinline__ void sub2(float a0, float a1, float b0, float b1, float& s0, float& s1) {
+  asm("{\n\t.reg .b64 x, y, r;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+      "sub.rn.f32x2 r, x, y;\n\tmov.b64 {%0, %1}, r;\n\t}"
+      : "=f"(s0), "=f"(s1)
+      : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
 // Radix-2 decimation-in-frequency network on R register values (natural
-// order in, bit-reversed order out). sg = -1 forward, +1 inverse.
+// order in, bit-reversed order out). sg = -1 forward, +1 inverse. In fp32
+// the sums and differences of butterflies k and k + 1 (HALF >= 2) go
+// through packed pairs: the same round-to-nearest results, half the adds
+// issued.
 template <int R, int HALF, bool INV, class T>
 __device__ __forceinline__ void dif_stage(T* xr, T* xi) {
   if constexpr (HALF >= 1) {
+    constexpr bool PAIRED = std::is_same<T, float>::value && HALF >= 2;
 #pragma unroll
     for (int base = 0; base < R; base += 2 * HALF) {
+      T dpr[HALF], dpi[HALF];  // differences (paired path)
+      if constexpr (PAIRED) {
+#pragma unroll
+        for (int k = 0; k < HALF; k += 2) {
+          const int a = base + k, b = base + k + HALF;
+          float sr0, sr1, si0, si1;
+          sub2(xr[a], xr[a + 1], xr[b], xr[b + 1], dpr[k], dpr[k + 1]);
+          sub2(xi[a], xi[a + 1], xi[b], xi[b + 1], dpi[k], dpi[k + 1]);
+          add2(xr[a], xr[a + 1], xr[b], xr[b + 1], sr0, sr1);
+          add2(xi[a], xi[a + 1], xi[b], xi[b + 1], si0, si1);
+          xr[a] = sr0, xr[a + 1] = sr1, xi[a] = si0, xi[a + 1] = si1;
+        }
+      }
 #pragma unroll
       for (int k = 0; k < HALF; ++k) {
-        const T ar = xr[base + k], ai = xi[base + k];
-        const T br = xr[base + k + HALF], bi = xi[base + k + HALF];
-        xr[base + k] = vadd(ar, br);
-        xi[base + k] = vadd(ai, bi);
-        const T dr = vsub(ar, br), di = vsub(ai, bi);
+        T dr, di;
+        if constexpr (PAIRED) {
+          dr = dpr[k];
+          di = dpi[k];
+        } else {
+          const T ar = xr[base + k], ai = xi[base + k];
+          const T br = xr[base + k + HALF], bi = xi[base + k + HALF];
+          xr[base + k] = vadd(ar, br);
+          xi[base + k] = vadd(ai, bi);
+          dr = vsub(ar, br);
+          di = vsub(ai, bi);
+        }
         constexpr int step = 32 / (2 * HALF);  // twiddle W_{2 HALF}^k = W_32^(k step)
         const int m = k * step;
         if (m == 0) {
