@@ -356,11 +356,11 @@ void terms_for(int precision, tc::Params& p) {
   p.n_terms = precision == CSG_PREC_BF16X3 ? 3 : 6;
 }
 
-template <int BN, bool OP_IS_A, int EPI, bool HP = false>
+template <int BN, bool OP_IS_A, int EPI, bool HP = false, int KB = 0>
 static int launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const tc::Params& p,
                        int grid, cudaStream_t st, const CUtensorMap* o = nullptr) {
-  auto kern = tc::k_split_gemm<BN, OP_IS_A, EPI, HP>;
-  constexpr size_t smem = tc::smem_bytes<BN, EPI, HP>();
+  auto kern = tc::k_split_gemm<BN, OP_IS_A, EPI, HP, KB>;
+  constexpr size_t smem = tc::smem_bytes<BN, EPI, HP, KB>();
   static bool attr_set = false;  // per template instance
   if (!attr_set) {
     CSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

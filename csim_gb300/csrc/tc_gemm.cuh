@@ -254,11 +254,19 @@ constexpr int MAX_PARTS = 3;
 // room for two or three stages, and tensor memory holds one 256-column
 // rotating hi x hi slot beside the small products' slot: hi x hi is
 // committed first, so its drain overlaps the rest of the block.
-template <int BN, int EPI, bool HP = false>
+//
+// KB_ selects the K block explicitly (0: 64, or 32 for 256-wide tiles).
+// Measured on the 1024^2 PIAACMC chain at 76 fields: 128-wide tiles with
+// four 32-wide-K stages kept the tensor pipe 55% busy against 66% for two
+// 64-wide ones (twice the per-block barrier, commit and drain overhead for
+// no gain in operand latency), so the 64-wide blocks stay the default.
+template <int BN, int EPI, bool HP = false, int KB_ = 0>
 struct Cfg {
   static_assert(BN == 64 || BN == 128 || BN == 256, "N tile must be 64, 128 or 256");
   static_assert(!HP || BN <= 128, "high precision: N tile 64 or 128");
-  static constexpr int KB = BN == 256 ? 32 : BK;  // K elements per pipeline stage
+  static_assert(KB_ == 0 || KB_ == 32 || KB_ == 64, "K block: 32 or 64 elements");
+  static constexpr int KB = KB_ ? KB_ : (BN == 256 ? 32 : BK);  // K elements per stage
+  static_assert(BN != 256 || KB == 32, "256-wide tiles use 32-wide K blocks");
   static constexpr uint32_t A_BYTES = BM * KB * 2;
   static constexpr uint32_t B_BYTES = BN * KB * 2;
   static constexpr uint32_t STAGE_BYTES = MAX_PARTS * (A_BYTES + B_BYTES);
@@ -266,9 +274,12 @@ struct Cfg {
   // the per-column group maxima of each warp, double-buffered by tile
   static constexpr uint32_t STAGING_BYTES =
       EPI == 1 ? DRAIN_WARPS * 4096 : (HP ? 2 * DRAIN_WARPS * (BN / 2) * 4 : 0);
-  // 192 KB (+ 32 KB staging) at N = 128; 216 KB or 144 KB (+ 32 KB) at 64
-  // and at 256
-  static constexpr int STAGES = BN == 128 ? 2 : (EPI == 1 ? 2 : 3);
+  // as many operand stages as fit beside the staging region and the
+  // barriers (at most four): two 96 KB stages at N = 128 with 64-wide K
+  // blocks, four 48 KB stages with 32-wide ones
+  static constexpr int STAGES_FIT = (int)((232448u - STAGING_BYTES - 1536u) / STAGE_BYTES);
+  static constexpr int STAGES = STAGES_FIT < 4 ? STAGES_FIT : 4;
+  static_assert(STAGES >= 2, "at least two operand stages");
   static constexpr int NSLOT = BN == 256 ? 1 : 3;  // rotating hi x hi slots
   static constexpr int TMEM_COLS = BN * (1 + NSLOT);  // small products + rotating
   static constexpr int COLS_PER_WARP = BN / 2;      // two warps share a lane quadrant
@@ -277,9 +288,9 @@ struct Cfg {
   static_assert(SMEM <= 232448, "shared memory per CTA");
 };
 
-template <int BN, int EPI, bool HP = false>
+template <int BN, int EPI, bool HP = false, int KB_ = 0>
 constexpr size_t smem_bytes() {
-  return Cfg<BN, EPI, HP>::SMEM;
+  return Cfg<BN, EPI, HP, KB_>::SMEM;
 }
 
 // Drain one lane quadrant's CPW columns at taddr into acc (+=).
@@ -417,11 +428,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int BN, bool OP_IS_A, int EPI, bool HP = false>
+template <int BN, bool OP_IS_A, int EPI, bool HP = false, int KB_ = 0>
 __global__ void __launch_bounds__(THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const __grid_constant__ CUtensorMap tmO, const Params p) {
-  using CF = Cfg<BN, EPI, HP>;
+  using CF = Cfg<BN, EPI, HP, KB_>;
   constexpr int STAGES = CF::STAGES;
   constexpr int NSLOT = CF::NSLOT;  // rotating group-0 slots
   constexpr int CPW = CF::COLS_PER_WARP;
