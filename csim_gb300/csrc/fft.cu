@@ -970,32 +970,96 @@ static int dft_plan(csg_ctx* ctx, int n, int sgn, int precision, csg_mft** out) 
   return CSG_OK;
 }
 
-// The spectrum times the Fresnel transfer function of each field's
-// wavelength (FFT order), from the table or evaluated here.
+// The DFT-product Fresnel factors the transfer function as H = c H' with
+// c = exp(2 pi i z / lambda) (H at zero frequency) and propagates
+//   E' = c (E + IDFT[DFT(E) (H' - 1)]):
+// H' - 1 vanishes at zero frequency and stays small where the spectrum of a
+// smooth field is concentrated, so the inverse transform's input has a far
+// smaller dynamic range than DFT(E) H (whose zero-frequency term dominates
+// every 64-element group it sits in and sets the rounding of the rest).
+
+// c of each field, FP64-evaluated (cos, sin; two-float as (hi, lo) pairs).
+__device__ __forceinline__ void fresnel_unit(double lam, double z, dfl& cr, dfl& ci) {
+  const double zl = z / lam;
+  double sn, cs;
+  sincospi(2.0 * (zl - rint(zl)), &sn, &cs);
+  const float2 a = split_f64(cs), b = split_f64(sn);
+  cr = dfl{a.x, a.y};
+  ci = dfl{b.x, b.y};
+}
+
+// The spectrum times H' - 1 of each field's wavelength (FFT order), from
+// the table (H conj(c) - 1) or evaluated here (exp(2 pi i tau) - 1 with
+// tau the phase past z / lambda: (-2 sin^2(pi tau), sin(2 pi tau))).
 __global__ void k_fresnel_mul(float* __restrict__ spec, int N, const __grid_constant__ FresnelArgs fa) {
   const int f = blockIdx.y;
   const size_t plane = (size_t)N * N;
   float* re = spec + (size_t)f * 2 * plane;
   float* im = re + plane;
   __shared__ FresnelConsts shc;
-  if (!fa.H && !fa.H4) {
-    if (threadIdx.x == 0) shc = fresnel_consts(fa.lambda[f], fa.z, fa.ap_rad);
-    __syncthreads();
+  __shared__ float2 shu;
+  if (threadIdx.x == 0) {
+    shc = fresnel_consts(fa.lambda[f], fa.z, fa.ap_rad);
+    shc.t0 = 0.f;  // the in-place evaluation gives H' itself
+    dfl cr, ci;
+    fresnel_unit(fa.lambda[f], fa.z, cr, ci);
+    shu = make_float2(cr.h, ci.h);
   }
+  __syncthreads();
+  const float2 u = shu;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < plane;
        i += (size_t)gridDim.x * blockDim.x) {
-    float2 w;
-    if (fa.H4) {
-      const float4 h = fa.H4[(size_t)fa.slot[f] * plane + i];
-      w = make_float2(h.x + h.y, h.z + h.w);
-    } else if (fa.H) {
-      w = fa.H[(size_t)fa.slot[f] * plane + i];
+    float2 w;  // H' - 1
+    if (fa.H4 || fa.H) {
+      float2 h;
+      if (fa.H4) {
+        const float4 q = fa.H4[(size_t)fa.slot[f] * plane + i];
+        h = make_float2(q.x + q.y, q.z + q.w);
+      } else {
+        h = fa.H[(size_t)fa.slot[f] * plane + i];
+      }
+      w = make_float2(fmaf(h.x, u.x, fmaf(h.y, u.y, -1.f)), fmaf(h.y, u.x, -h.x * u.y));
     } else {
-      w = fresnel_h(N, (int)(i / N), (int)(i % N), shc);
+      const int r = (int)(i / N), c = (int)(i % N);
+      const int fr = r < N / 2 ? r : r - N;
+      const int fc = c < N / 2 ? c : c - N;
+      const float f2 = (float)(fr * fr + fc * fc);
+      const float eps = shc.c_eps * f2;
+      const float sq = sqrtf(1.f - eps);
+      const float hh = eps / (2.f * (1.f + sq) * (1.f + sq));
+      float tt = -frac_prod(f2, shc.khi, shc.klo) - shc.K * f2 * hh;
+      tt -= rintf(tt);
+      float s1, c1, s2, c2;
+      sincospif(tt, &s1, &c1);
+      sincospif(2.f * tt, &s2, &c2);
+      w = make_float2(-2.f * s1 * s1, s2);
     }
     const float a = re[i], b = im[i];
     re[i] = a * w.x - b * w.y;
     im[i] = a * w.y + b * w.x;
+  }
+}
+
+// Each field times its c (the last step of E' = c (E + ...)).
+__global__ void k_fresnel_unit(float* __restrict__ field, int N, const double* __restrict__ lambda,
+                               double z) {
+  const int f = blockIdx.y;
+  const size_t plane = (size_t)N * N;
+  float* re = field + (size_t)f * 2 * plane;
+  float* im = re + plane;
+  __shared__ float2 shu;
+  if (threadIdx.x == 0) {
+    dfl cr, ci;
+    fresnel_unit(lambda[f], z, cr, ci);
+    shu = make_float2(cr.h, ci.h);
+  }
+  __syncthreads();
+  const float2 u = shu;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < plane;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float a = re[i], b = im[i];
+    re[i] = a * u.x - b * u.y;
+    im[i] = a * u.y + b * u.x;
   }
 }
 
@@ -1053,14 +1117,20 @@ static int dft2d_mft(csg_ctx* ctx, float* field, int F, int n, int direction,
   csg_mft *fwd = fit->second, *inv = iit->second;
   {
     if (fa) {
+      // E' = c (E + IDFT[DFT(E) (H' - 1)]): the inverse accumulates into the
+      // field, which still holds E
+      const dim3 grid(grid_for((long long)n * n, 256, 512), F);
       rc = mft_execute_ops(ctx, fwd, field, tmp, F, zero, 0, nullptr, nullptr, PixOps(), fi);
       if (!rc) {
-        dim3 grid(grid_for((long long)n * n, 256, 512), F);
         k_fresnel_mul<<<grid, 256, 0, st>>>(tmp, n, *fa);
         CSG_LAUNCH_CHECK();
       }
       if (!rc)
-        rc = mft_execute_ops(ctx, inv, tmp, field, F, zero, 0, nullptr, nullptr, PixOps(), fi);
+        rc = mft_execute_ops(ctx, inv, tmp, field, F, zero, 1, nullptr, nullptr, PixOps(), fi);
+      if (!rc) {
+        k_fresnel_unit<<<grid, 256, 0, st>>>(field, n, fa->lambda, fa->z);
+        CSG_LAUNCH_CHECK();
+      }
     } else {
       rc = mft_execute_ops(ctx, direction < 0 ? fwd : inv, field, tmp, F, zero, 0, nullptr,
                            nullptr, PixOps(), fi);

@@ -350,6 +350,17 @@ __global__ void k_split_field_aligned(const float* __restrict__ in,
   }
 }
 
+// L2 prefetch distance of the GEMM's field operand, in K blocks (tuning
+// override CSG_GEMM_PREFETCH, 0 to 16; default 0: off).
+static int gemm_prefetch() {
+  static const int pf = [] {
+    const char* e = getenv("CSG_GEMM_PREFETCH");
+    const int v = e ? atoi(e) : 0;
+    return v < 0 ? 0 : (v > 16 ? 16 : v);
+  }();
+  return pf;
+}
+
 // The GEMM issues a prefix of its fixed product order (tc::term_a, tc::term_b):
 // all six products for bf16x6, the three largest for bf16x3.
 void terms_for(int precision, tc::Params& p) {
@@ -753,6 +764,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.status = ctx->status;
     p.valid = m->valid;
     p.wait_budget = ctx->wait_budget;
+    p.prefetch = gemm_prefetch();
     const int grid = n_fields * p.m_tiles * p.n_tiles;
     // algorithmic work: 8 flops per complex multiply-add of the contraction
     ProfScope ps(ctx, "mft_gemm", 8.0 * F * m->ny * m->no * m->nx);
@@ -793,6 +805,7 @@ int csg::mft_execute_ops(csg_ctx* ctx, csg_mft* m, const float* in, float* out, 
     p.status = ctx->status;
     p.valid = m->valid;
     p.wait_budget = ctx->wait_budget;
+    p.prefetch = gemm_prefetch();
     p.out_lo = out_lo;
     CUtensorMap to;
     p.tma_out = make_map_f32_out(&to, out + (size_t)outw.r0 * outw.pitch + outw.c0, m->no, m->mo,

@@ -62,6 +62,9 @@ struct Params {
   // context's csg_set_wait_budget; 0: kWaitBudgetCycles). The clean-up after
   // a give-up always waits with the full budget.
   long long wait_budget;
+  // K blocks ahead at which the producer prefetches the field operand's
+  // parts into L2 (0: no prefetch)
+  int prefetch;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -109,6 +112,14 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, ui
       " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(tm)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
       : "memory");
+}
+
+// L2 prefetch of one box at (x, y, z) (no shared memory, no completion).
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* tm, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                   reinterpret_cast<uint64_t>(tm)),
+               "r"(x), "r"(y), "r"(z)
+               : "memory");
 }
 
 // Shared -> global tile store, or element-wise fp32 add into global (the
@@ -520,6 +531,20 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             tma_load_3d(sA + pp * CF::A_BYTES, &tmA, &full[stage], kb * CF::KB, tc.row_a0, za);
             tma_load_3d(sB + pp * CF::B_BYTES, &tmB, &full[stage], kb * CF::KB, tc.row_b0, zb);
+          }
+          // The field operand streams from DRAM (the operator stays in L2):
+          // its parts for block it + PF are prefetched into L2 now, so that
+          // their loads, issued with only one stage of lead, find them there.
+          const int PF = p.prefetch;
+          if (PF > 0 && it + PF < k_iters) {
+            const int kbp = (it + PF) % p.k_blocks, cp = (it + PF) / p.k_blocks;
+            for (int pp = 0; pp < n_parts; ++pp) {
+              const int zd = (tc.field * 3 + pp) * 2 + cp;
+              if (!OP_IS_A)
+                tma_prefetch_3d(&tmA, kbp * CF::KB, tc.row_a0, zd);
+              else
+                tma_prefetch_3d(&tmB, kbp * CF::KB, tc.row_b0, zd);
+            }
           }
         }
       }

@@ -42,13 +42,17 @@ def test_fresnel_size_1000_matches_oracle(ctx, precision):
     ap = (np.hypot(xx - n / 2 + 0.5, yy - n / 2 + 0.5) < 0.4 * n).astype(np.float64)
     e = oe.mask_apply(oe.point_source_field(geom, 2, 1.0, 0.05, -0.02), ap)
     t = R.to_planar(e)
+    e32 = R.from_planar(t)  # the input as uploaded (fp32), the oracle's input too
     ctx.fresnel(t, R.dvec(lam), dx * n / 2, 0.3, precision=precision)
     ctx.sync()
     got = R.from_planar(t)
-    ref = oe.fresnel_element(e, lam, dx * n / 2, 0.3)
+    ref = oe.fresnel_element(e32, lam, dx * n / 2, 0.3)
     err = np.abs(got - ref).max() / np.abs(ref).max()
     print(f"\nFresnel 1000^2 precision {precision}: {err:.3e} of the field peak")
-    assert err < 2e-6, err
+    # the DFT product propagates E + IDFT[DFT(E) (H' - 1)] (H' = H without
+    # its zero-frequency phase): measured 3.1e-7 / 3.3e-7, set by the
+    # three-part split of the transforms in both modes
+    assert err < 5e-7, err
 
 
 def test_chain_at_size_1000_matches_oracle(ctx):
