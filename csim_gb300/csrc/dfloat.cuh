@@ -35,6 +35,47 @@ __device__ __forceinline__ dfl df_add(dfl a, dfl b) {
   fast_two_sum(s, e, r.h, r.l);
   return r;
 }
+// a0 + b0 and a1 + b1 (or a - b) with the same operations as df_add, on
+// packed fp32 pairs (add.rn.f32x2 / sub.rn.f32x2: the same round-to-nearest
+// results per lane, one instruction for both sums).
+__device__ __forceinline__ void df_add2(dfl a0, dfl a1, dfl b0, dfl b1, dfl& r0, dfl& r1) {
+  asm("{\n\t.reg .b64 ah, al, bh, bl, s, bb, t, u, e, rh, rl;\n\t"
+      "mov.b64 ah, {%4, %5};\n\tmov.b64 al, {%6, %7};\n\t"
+      "mov.b64 bh, {%8, %9};\n\tmov.b64 bl, {%10, %11};\n\t"
+      "add.rn.f32x2 s, ah, bh;\n\t"   // TwoSum(ah, bh)
+      "sub.rn.f32x2 bb, s, ah;\n\t"
+      "sub.rn.f32x2 t, s, bb;\n\t"
+      "sub.rn.f32x2 t, ah, t;\n\t"
+      "sub.rn.f32x2 u, bh, bb;\n\t"
+      "add.rn.f32x2 e, t, u;\n\t"
+      "add.rn.f32x2 u, al, bl;\n\t"   // + (al + bl)
+      "add.rn.f32x2 e, e, u;\n\t"
+      "add.rn.f32x2 rh, s, e;\n\t"    // fast TwoSum renormalisation
+      "sub.rn.f32x2 u, rh, s;\n\t"
+      "sub.rn.f32x2 rl, e, u;\n\t"
+      "mov.b64 {%0, %1}, rh;\n\tmov.b64 {%2, %3}, rl;\n\t}"
+      : "=f"(r0.h), "=f"(r1.h), "=f"(r0.l), "=f"(r1.l)
+      : "f"(a0.h), "f"(a1.h), "f"(a0.l), "f"(a1.l), "f"(b0.h), "f"(b1.h), "f"(b0.l), "f"(b1.l));
+}
+__device__ __forceinline__ void df_sub2(dfl a0, dfl a1, dfl b0, dfl b1, dfl& r0, dfl& r1) {
+  asm("{\n\t.reg .b64 ah, al, bh, bl, s, bb, t, u, e, rh, rl;\n\t"
+      "mov.b64 ah, {%4, %5};\n\tmov.b64 al, {%6, %7};\n\t"
+      "mov.b64 bh, {%8, %9};\n\tmov.b64 bl, {%10, %11};\n\t"
+      "sub.rn.f32x2 s, ah, bh;\n\t"   // TwoSum(ah, -bh)
+      "sub.rn.f32x2 bb, s, ah;\n\t"
+      "sub.rn.f32x2 t, s, bb;\n\t"
+      "sub.rn.f32x2 t, ah, t;\n\t"
+      "add.rn.f32x2 u, bh, bb;\n\t"   // (-bh - bb) = -(bh + bb)
+      "sub.rn.f32x2 e, t, u;\n\t"
+      "sub.rn.f32x2 u, al, bl;\n\t"   // + (al - bl)
+      "add.rn.f32x2 e, e, u;\n\t"
+      "add.rn.f32x2 rh, s, e;\n\t"
+      "sub.rn.f32x2 u, rh, s;\n\t"
+      "sub.rn.f32x2 rl, e, u;\n\t"
+      "mov.b64 {%0, %1}, rh;\n\tmov.b64 {%2, %3}, rl;\n\t}"
+      : "=f"(r0.h), "=f"(r1.h), "=f"(r0.l), "=f"(r1.l)
+      : "f"(a0.h), "f"(a1.h), "f"(a0.l), "f"(a1.l), "f"(b0.h), "f"(b1.h), "f"(b0.l), "f"(b1.l));
+}
 __device__ __forceinline__ dfl df_neg(dfl a) { return dfl{-a.h, -a.l}; }
 __device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
 __device__ __forceinline__ dfl df_scale(dfl a, float p2) { return dfl{a.h * p2, a.l * p2}; }

@@ -211,15 +211,31 @@ __device__ __forceinline__ void sub2(float a0, float a1, float b0, float b1, flo
       : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
 }
 
+// Sums and differences of two values at once (packed pairs).
+__device__ __forceinline__ void pair_add(float a0, float a1, float b0, float b1, float& r0,
+                                         float& r1) {
+  add2(a0, a1, b0, b1, r0, r1);
+}
+__device__ __forceinline__ void pair_sub(float a0, float a1, float b0, float b1, float& r0,
+                                         float& r1) {
+  sub2(a0, a1, b0, b1, r0, r1);
+}
+__device__ __forceinline__ void pair_add(dfl a0, dfl a1, dfl b0, dfl b1, dfl& r0, dfl& r1) {
+  df_add2(a0, a1, b0, b1, r0, r1);
+}
+__device__ __forceinline__ void pair_sub(dfl a0, dfl a1, dfl b0, dfl b1, dfl& r0, dfl& r1) {
+  df_sub2(a0, a1, b0, b1, r0, r1);
+}
+
 // Radix-2 decimation-in-frequency network on R register values (natural
-// order in, bit-reversed order out). sg = -1 forward, +1 inverse. In fp32
-// the sums and differences of butterflies k and k + 1 (HALF >= 2) go
-// through packed pairs: the same round-to-nearest results, half the adds
-// issued.
+// order in, bit-reversed order out). sg = -1 forward, +1 inverse. The sums
+// and differences of butterflies k and k + 1 (HALF >= 2) go through packed
+// pairs (fp32 or two-float): the same round-to-nearest results, half the
+// adds issued.
 template <int R, int HALF, bool INV, class T>
 __device__ __forceinline__ void dif_stage(T* xr, T* xi) {
   if constexpr (HALF >= 1) {
-    constexpr bool PAIRED = std::is_same<T, float>::value && HALF >= 2;
+    constexpr bool PAIRED = HALF >= 2;
 #pragma unroll
     for (int base = 0; base < R; base += 2 * HALF) {
       T dpr[HALF], dpi[HALF];  // differences (paired path)
@@ -227,11 +243,11 @@ __device__ __forceinline__ void dif_stage(T* xr, T* xi) {
 #pragma unroll
         for (int k = 0; k < HALF; k += 2) {
           const int a = base + k, b = base + k + HALF;
-          float sr0, sr1, si0, si1;
-          sub2(xr[a], xr[a + 1], xr[b], xr[b + 1], dpr[k], dpr[k + 1]);
-          sub2(xi[a], xi[a + 1], xi[b], xi[b + 1], dpi[k], dpi[k + 1]);
-          add2(xr[a], xr[a + 1], xr[b], xr[b + 1], sr0, sr1);
-          add2(xi[a], xi[a + 1], xi[b], xi[b + 1], si0, si1);
+          T sr0, sr1, si0, si1;
+          pair_sub(xr[a], xr[a + 1], xr[b], xr[b + 1], dpr[k], dpr[k + 1]);
+          pair_sub(xi[a], xi[a + 1], xi[b], xi[b + 1], dpi[k], dpi[k + 1]);
+          pair_add(xr[a], xr[a + 1], xr[b], xr[b + 1], sr0, sr1);
+          pair_add(xi[a], xi[a + 1], xi[b], xi[b + 1], si0, si1);
           xr[a] = sr0, xr[a + 1] = sr1, xi[a] = si0, xi[a + 1] = si1;
         }
       }
@@ -420,13 +436,17 @@ struct RowCfg {
   static constexpr size_t SMEM = (size_t)ROWS * N * 8 * words_of<T>();
 };
 // Column tile width: 8 columns (32-byte row segments) at N = 1024. Two-float
-// tiles hold 256 threads (one CTA per SM with up to 255 registers: the
-// transfer-function product and the inverse transform need them; 64 KB of
-// shared memory), 4 columns at N = 1024.
+// tiles hold 128 threads (2 columns at N = 1024, 32 KB of shared memory),
+// three CTAs per SM within 168 registers. Measured on the 152-field PIAACMC
+// step at CSG_PREC_HIGH: the Fresnel column pass at 256 threads and one CTA
+// per SM (255 registers, no spills) issued at 32% of peak and took 10.1 ms
+// of an 18.4 ms step; at 128 threads x 3 CTAs (336 bytes of spills in the
+// transfer-function pass) 7.2 ms; 256 x 2 or 128 x 4 CTAs (128 registers,
+// more spills) 9.8 and 10.0 ms.
 constexpr int default_cols(int n) { return n <= 512 ? 16 : (n == 1024 ? 8 : 4); }
 template <class T>
 constexpr int cols_for(int n) {
-  return std::is_same<T, dfl>::value ? (256 / (n / 16) > 0 ? 256 / (n / 16) : 1)
+  return std::is_same<T, dfl>::value ? (128 / (n / 16) > 0 ? 128 / (n / 16) : 1)
                                      : default_cols(n);
 }
 template <int N, int E, int COLS, class T = float>
@@ -434,7 +454,7 @@ struct ColCfg {
   static constexpr int TPT = N / E;
   static constexpr int THREADS = COLS * TPT;
   static constexpr int MIN_BLOCKS =
-      std::is_same<T, dfl>::value ? 1 : min_blocks_t<T>(E, THREADS);
+      std::is_same<T, dfl>::value ? (THREADS <= 128 ? 3 : 1) : min_blocks_t<T>(E, THREADS);
   static constexpr int PLANE = COLS * N;
   static constexpr size_t SMEM = (size_t)COLS * N * 8 * words_of<T>();
 };
