@@ -84,8 +84,10 @@ def _code(fn, *args):
 def test_rejected_calls_return_status_codes(ctx):
     from csim_gb300 import runtime as R
     f = torch.zeros((1, 2, 96, 96), dtype=torch.float32, device="cuda")
-    # non-power-of-two FFT sizes are refused with CSG_E_SHAPE
-    assert _code("csg_fft2d", ctx.h, P(f.data_ptr()), 1, 96, -1)[0] == -2
+    # sizes that are neither powers of two nor multiples of 8 are refused
+    # with CSG_E_SHAPE before the field is touched (96 runs as a DFT product)
+    assert _code("csg_fft2d", ctx.h, P(f.data_ptr()), 1, 100, -1)[0] == -2
+    assert _code("csg_fft2d", ctx.h, P(f.data_ptr()), 1, 96, -1)[0] == 0
     # bad enums: direction, precision, layout
     g = torch.zeros((1, 2, 64, 64), dtype=torch.float32, device="cuda")
     assert _code("csg_fft2d", ctx.h, P(g.data_ptr()), 1, 64, 0)[0] == -1
