@@ -174,7 +174,10 @@ int csg_fresnel(csg_ctx* ctx, float* field, int n_fields, int n, const double* l
 /* csg_fresnel with a precision: CSG_PREC_HIGH evaluates the transfer function
  * in FP64 and runs the three passes in two-float arithmetic (fields stay fp32
  * in memory); it allocates a per-call table of n_fields * n^2 * 16 bytes and
- * returns after the work is done. Other precisions are csg_fresnel. */
+ * returns after the work is done. Other precisions are csg_fresnel. Sizes
+ * that are not powers of two propagate E' = c (E + IDFT[DFT(E) (H/c - 1)]),
+ * c = exp(2 pi i z / lambda_f), with the DFT products of csg_fft2d: about
+ * 3e-7 of the field peak in every precision. */
 int csg_fresnel_prec(csg_ctx* ctx, float* field, int n_fields, int n, const double* lambda,
                      double ap_rad, double z, int precision);
 
