@@ -166,10 +166,9 @@ struct csg_chain {
   float* image = nullptr;       // [F][2][n_out][n_out]
   float* image_lo = nullptr;    // CSG_PREC_HIGH: low-order words of the image
   float* padbuf = nullptr;      // [F][2][P][P] (padded-FFT focal-plane masks)
-  float* spec_lo = nullptr;     // CSG_PREC_HIGH Fresnel: the column spectrum's low words [F][2][n][n]
   double* sags = nullptr;       // [n_cand][n_hex]
   int n_cand = 0, sag_hex = 0;
-  size_t fpm_cap = 0, img_cap = 0, ph_cap = 0, pad_cap = 0, img_lo_cap = 0, spec_lo_cap = 0;
+  size_t fpm_cap = 0, img_cap = 0, ph_cap = 0, pad_cap = 0, img_lo_cap = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_calib = -1;
@@ -253,7 +252,7 @@ int csg_chain_destroy(csg_chain* c) {
   for (void* p : {(void*)c->slot, (void*)c->lam_f, (void*)c->amp, (void*)c->tip, (void*)c->tilt,
                   (void*)c->cand, (void*)c->ident, (void*)c->field, (void*)c->fpm,
                   (void*)c->fpm_mask, (void*)c->phasors, (void*)c->image, (void*)c->image_lo,
-                  (void*)c->sags, (void*)c->spec_lo,
+                  (void*)c->sags,
                   (void*)c->lam_slots, (void*)c->padbuf})
     cudaFree(p);
   delete c;
@@ -1122,15 +1121,12 @@ static int prepare(csg_chain* c) {
   int prc = build_plans(c);
   if (prc) return prc;
   const size_t F = (size_t)c->n_fields;
-  size_t fpm_need = 0, ph_need = 0, img_need = 0, pad_need = 0, spec_need = 0;
+  size_t fpm_need = 0, ph_need = 0, img_need = 0, pad_need = 0;
   for (auto& e : c->elems) {
     if (e.kind == E_FRESNEL && fft_is_dft_size(c->n)) {
       // a size that is not a power of two: the Fresnel runs as DFT transforms
       const int rc = dft_prepare(c->ctx, c->n, c->n_fields, c->precision == CSG_PREC_HIGH);
       if (rc) return rc;
-    } else if (e.kind == E_FRESNEL && c->precision == CSG_PREC_HIGH) {
-      // the two-float column pass in two halves keeps the spectrum's low words
-      spec_need = F * 2 * (size_t)c->n * c->n * sizeof(float);
     } else if (e.kind == E_FPM_HEX) {
       fpm_need = std::max(fpm_need, F * 2 * e.RR * e.CC * sizeof(float));
       ph_need = std::max(ph_need, F * (e.n_hex + 1) * sizeof(float2));
@@ -1170,7 +1166,6 @@ static int prepare(csg_chain* c) {
   if (!rc) rc = ensure_buf(&c->image, c->img_cap, img_need);
   if (!rc && c->precision == CSG_PREC_HIGH) rc = ensure_buf(&c->image_lo, c->img_lo_cap, img_need);
   if (!rc) rc = ensure_buf(&c->padbuf, c->pad_cap, pad_need);
-  if (!rc) rc = ensure_buf(&c->spec_lo, c->spec_lo_cap, spec_need);
   return rc;
 }
 
@@ -1318,7 +1313,6 @@ static int run_step(csg_chain* c, const Step& s, const FieldInfo& fi, int F) {
       case Step::FRESNEL: {
         const bool high = c->precision == CSG_PREC_HIGH;
         FresnelArgs fa{c->lam_f, s.e->z, s.e->ap_rad, s.e->tab, c->slot, s.e->tab4};
-        if (high && !fft_is_dft_size(n)) fa.spec_lo = c->spec_lo;
         FftBand sup;  // rows a mask left nonzero, widened to the transform's row groups
         __nv_bfloat16* split = nullptr;
         if (s.split_to) {

@@ -693,9 +693,7 @@ int table_to_df(cudaStream_t st, const float2* in, float4* out, long long n) {
   return CSG_OK;
 }
 
-// Column pass; MODE 0: forward, 1: inverse, 2: forward * H(lambda_f) * inverse;
-// two-float only: 3: forward * H stored as (hi in the field, lo in
-// fa.spec_lo), 4: the inverse of such a two-float spectrum.
+// Column pass; MODE 0: forward, 1: inverse, 2: forward * H(lambda_f) * inverse.
 // Thread (t, u) = (threadIdx % COLS, threadIdx / COLS) owns rows u + s N/16
 // of column c0 + t: a warp's load or store covers 32/COLS rows x COLS
 // consecutive floats. In MODE 2 the forward transform leaves each thread
@@ -727,22 +725,12 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS, T>::THREADS,
   // input and, unless store_all, not stored (band_n = 0: every row)
   const int s0 = band_n ? band_lo / TPT : 0, s1 = band_n ? (band_lo + band_n) / TPT : E;
   const int w0 = store_all ? 0 : s0, w1 = store_all ? E : s1;
-  // modes 3 and 4: the spectrum's low words, laid out as the field
-  float* lre = nullptr;
-  float* lim = nullptr;
-  if constexpr (DF && MODE >= 3) {
-    lre = fa.spec_lo + (size_t)f * 2 * plane + (size_t)u * N + c0 + t;
-    lim = lre + plane;
-  }
 #pragma unroll
   for (int s = 0; s < E; ++s) {
     const bool in = s >= s0 && s < s1;
     const float a = in ? fre[(size_t)s * TPT * N] : 0.f;
     const float b = in ? fim[(size_t)s * TPT * N] : 0.f;
-    if constexpr (DF && MODE == 4) {
-      xr[s] = dfl{a, in ? lre[(size_t)s * TPT * N] : 0.f};
-      xi[s] = dfl{b, in ? lim[(size_t)s * TPT * N] : 0.f};
-    } else if constexpr (DF) {
+    if constexpr (DF) {
       xr[s] = df_from(a);
       xi[s] = df_from(b);
     } else {
@@ -750,8 +738,8 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS, T>::THREADS,
       xi[s] = b;
     }
   }
-  fft_regs<N, E, MODE == 1 || MODE == 4, A, LO>(xr, xi, re, im, t, u, tw);
-  if (MODE == 2 || MODE == 3) {
+  fft_regs<N, E, MODE == 1, A, LO>(xr, xi, re, im, t, u, tw);
+  if (MODE == 2) {
     if constexpr (DF) {
       const float4* Hs = fa.H4 + (size_t)fa.slot[f] * plane + (size_t)u * N + c0 + t;
 #pragma unroll
@@ -794,20 +782,13 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS, T>::THREADS,
         xi[s] = a * w.y + xi[s] * w.x;
       }
     }
-    if constexpr (MODE == 2) {
-      __syncthreads();  // the forward transform's last reads precede the inverse's writes
-      fft_regs<N, E, true, A, LO>(xr, xi, re, im, t, u, tw);
-    }
+    __syncthreads();  // the forward transform's last reads precede the inverse's writes
+    fft_regs<N, E, true, A, LO>(xr, xi, re, im, t, u, tw);
   }
 #pragma unroll
   for (int s = 0; s < E; ++s)
     if (s >= w0 && s < w1) {
-      if constexpr (DF && MODE == 3) {
-        fre[(size_t)s * TPT * N] = xr[s].h;
-        fim[(size_t)s * TPT * N] = xi[s].h;
-        lre[(size_t)s * TPT * N] = xr[s].l;
-        lim[(size_t)s * TPT * N] = xi[s].l;
-      } else if constexpr (DF) {
+      if constexpr (DF) {
         fre[(size_t)s * TPT * N] = df_round(xr[s]);
         fim[(size_t)s * TPT * N] = df_round(xi[s]);
       } else {
@@ -833,21 +814,6 @@ static int launch_cols(cudaStream_t st, float* field, int F, int mode,
   using CC = ColCfg<N, E, COLS, T>;
   const int grid = F * (N / COLS);
   int rc;
-  if constexpr (std::is_same<T, dfl>::value) {
-    if (mode == 3) {
-      if ((rc = prep_smem(k_fft_cols<N, E, 3, COLS, T>, CC::SMEM))) return rc;
-      k_fft_cols<N, E, 3, COLS, T><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa, band.lo,
-                                                                        band.n, store_all);
-      CSG_LAUNCH_CHECK();
-      return CSG_OK;
-    }
-    if (mode == 4) {
-      if ((rc = prep_smem(k_fft_cols<N, E, 4, COLS, T>, CC::SMEM))) return rc;
-      k_fft_cols<N, E, 4, COLS, T><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa, 0, 0, 0);
-      CSG_LAUNCH_CHECK();
-      return CSG_OK;
-    }
-  }
   if (mode == 2) {
     if ((rc = prep_smem(k_fft_cols<N, E, 2, COLS, T>, CC::SMEM))) return rc;
     k_fft_cols<N, E, 2, COLS, T><<<grid, CC::THREADS, CC::SMEM, st>>>(field, tw, *fa, band.lo,
@@ -923,10 +889,8 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
     return launch_rows<N, elems_for<T>(N), T>(st, field, F, inv, scale, tw, p, e, fi, bd);
   };
   auto cols = [&](int mode, const FftBand& bd, int store_all) -> int {
-    double bytes = store_all ? (double)F * N * (N + bd.n) * 8.0 : pass_bytes;
-    if (mode == 3) bytes += (double)F * N * N * 8.0;  // + the spectrum's low words
-    if (mode == 4) bytes = (double)F * N * N * 24.0;  // hi + lo read, field written
-    ProfScope ps(ctx, mode >= 2 ? "fft_cols_fresnel" : "fft_cols", 0, bytes);
+    const double bytes = store_all ? (double)F * N * (N + bd.n) * 8.0 : pass_bytes;
+    ProfScope ps(ctx, mode == 2 ? "fft_cols_fresnel" : "fft_cols", 0, bytes);
     if constexpr (N == 1024 && !DF) {
       if (e16) return launch_cols<N, 16, 8, T>(st, field, F, mode, tw, fa, bd, store_all);
       if (c_over == 4) return launch_cols<N, 32, 4, T>(st, field, F, mode, tw, fa, bd, store_all);
@@ -938,28 +902,16 @@ static int run_fft(csg_ctx* ctx, float* field, int F, int direction, const Fresn
   };
   FftBand whole, last = band;
   whole.split = last.split = split_out;  // the last pass also writes the split
-  // the Fresnel's column work: one fused pass, or (two-float with a
-  // spectrum buffer, whole rows) forward x H then the inverse: each half
-  // fits 168 registers without spilling, where the fused pass spills
-  auto fresnel_cols = [&](const FftBand& bd, int store_all) -> int {
-    if constexpr (DF) {
-      if (fa->spec_lo && !bd.src && !bd.dst) {
-        const int r = cols(3, bd, 1);
-        return r ? r : cols(4, FftBand(), 0);
-      }
-    }
-    return cols(2, bd, store_all);
-  };
   if (fa && sup.n) {
     // rows outside the prologue's support are zero: the first row pass
     // skips them (leaving them unwritten) and the column pass reads only
     // the support's rows and writes every row
     if ((rc = rows(false, 1.f, pro, none, sup))) return rc;
-    if ((rc = fresnel_cols(sup, 1))) return rc;
+    if ((rc = cols(2, sup, 1))) return rc;
     return rows(true, inv_scale, none, epi, whole);
   } else if (fa) {
     if ((rc = rows(false, 1.f, pro, none, band))) return rc;
-    if ((rc = (band.n ? cols(2, band, 0) : fresnel_cols(band, 0)))) return rc;
+    if ((rc = cols(2, band, 0))) return rc;
     return rows(true, inv_scale, none, epi, last);
   } else if (direction < 0) {
     if ((rc = rows(false, 1.f, pro, none, band))) return rc;
@@ -1338,15 +1290,10 @@ int csg_fresnel_prec(csg_ctx* ctx, float* field, int n_fields, int n, const doub
   const size_t plane = (size_t)n * n;
   float4* H4 = nullptr;
   int* slot = nullptr;
-  float* spec_lo = nullptr;  // power-of-two sizes: the column spectrum's low words
-  const bool split_cols = !fft_is_dft_size(n);
   if (cudaMallocAsync(&H4, plane * n_fields * sizeof(float4), st) != cudaSuccess ||
-      cudaMallocAsync(&slot, n_fields * sizeof(int), st) != cudaSuccess ||
-      (split_cols &&
-       cudaMallocAsync(&spec_lo, plane * 2 * n_fields * sizeof(float), st) != cudaSuccess)) {
+      cudaMallocAsync(&slot, n_fields * sizeof(int), st) != cudaSuccess) {
     cudaGetLastError();
     if (H4) cudaFreeAsync(H4, st);
-    if (slot) cudaFreeAsync(slot, st);
     set_error("csg_fresnel_prec: allocation failed");
     return CSG_E_NOMEM;
   }
@@ -1361,14 +1308,12 @@ int csg_fresnel_prec(csg_ctx* ctx, float* field, int n_fields, int n, const doub
   if (!rc) rc = build_fresnel_table_df(st, n, lambda, n_fields, z, ap_rad, H4);
   if (!rc) {
     FresnelArgs fa{lambda, z, ap_rad, nullptr, slot, H4};
-    fa.spec_lo = spec_lo;
     rc = fft2d_fused(ctx, field, n_fields, n, -1, &fa, PixOps(), PixOps(), FieldInfo(), nullptr,
                      nullptr, nullptr, true);
   }
   cudaStreamSynchronize(st);  // the host index vector and the tables
   cudaFreeAsync(H4, st);
   cudaFreeAsync(slot, st);
-  if (spec_lo) cudaFreeAsync(spec_lo, st);
   return rc;
 }
 

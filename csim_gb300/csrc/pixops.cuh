@@ -270,10 +270,6 @@ struct FresnelArgs {
   // two-float transfer-function table [slot][N][N] (cos hi, cos lo, sin hi,
   // sin lo): required by the two-float (CSG_PREC_HIGH) passes
   const float4* H4 = nullptr;
-  // two-float passes: the low words of the column spectrum [field][2][N][N]
-  // (the column pass split in two: forward x H storing the spectrum as fp32
-  // pairs, then the inverse); null: one fused column pass
-  float* spec_lo = nullptr;
 };
 
 // Per-wavelength tables, built once per chain in FP64-reduced phases:
