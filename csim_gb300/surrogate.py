@@ -6,7 +6,7 @@ dark-hole contrast at that wavelength. It is trained on samples the GPU
 propagator itself produces (random and DE-trajectory sag vectors), and in
 ``ScreenedDE`` it ranks several DE trial vectors per population member each
 generation; only the best-ranked trial of each member is propagated in full
-and judged by the true objective (plain DE is the fallback: with one draw
+and evaluated by the true objective (plain DE is the fallback: with one draw
 per member it is exactly the reference's DE).
 """
 from __future__ import annotations
@@ -301,7 +301,7 @@ def run_screened_de(de: "ScreenedDE", objective: PerLambdaObjective, strategy: s
         objective(x.clamp(lo, hi), out)
         buf.add(objective.sags, objective.field_c)
     t_samples = time.perf_counter() - t0
-    # 10% of the samples held out to judge the surrogate
+    # 10% of the samples held out to validate the surrogate
     perm = torch.randperm(buf.n, device="cuda")
     n_hold = buf.n // 10
     hold, tr = perm[:n_hold], perm[n_hold:]
