@@ -70,6 +70,24 @@ def test_fresnel_is_unitary_and_reversible():
     assert np.abs(back - e).max() < 1e-10
 
 
+def test_fresnel_unit_phase_form():
+    """The form the DFT-product Fresnel (sizes that are not powers of two)
+    evaluates: E' = c (E + IDFT[DFT(E) (H / c - 1)]), c = exp(2 pi i z / lambda)
+    the transfer function at zero frequency, equals fresnelPropagateAS."""
+    rng = np.random.default_rng(4)
+    n, lam, ap, z = 96, 6.5e-7, 0.01, 0.7
+    e = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    ref = of.fresnel_propagate_as(e[None], [lam], ap, z)[0]
+    f = np.fft.fftfreq(n, 1.0 / n)
+    f2 = f[:, None] ** 2 + f[None, :] ** 2
+    zl = z / lam
+    tau = -zl * (0.25 * (lam / ap) ** 2 * f2) / (1 + np.sqrt(1 - 0.25 * (lam / ap) ** 2 * f2))
+    c = np.exp(2j * np.pi * (zl - np.rint(zl)))
+    hm1 = np.exp(2j * np.pi * tau) - 1.0  # H / c - 1
+    got = c * (e + np.fft.ifft2(np.fft.fft2(e) * hm1))
+    assert np.abs(got - ref).max() < 1e-9 * np.abs(ref).max()
+
+
 def test_fft_shift_floor_and_truncate():
     a = np.arange(25.0).reshape(5, 5)
     assert np.array_equal(of.fft_shift(a), np.fft.fftshift(a))  # floor(5/2)=2 == numpy for odd
