@@ -436,17 +436,18 @@ struct RowCfg {
   static constexpr size_t SMEM = (size_t)ROWS * N * 8 * words_of<T>();
 };
 // Column tile width: 8 columns (32-byte row segments) at N = 1024. Two-float
-// tiles hold 128 threads (2 columns at N = 1024, 32 KB of shared memory),
-// three CTAs per SM within 168 registers. Measured on the 152-field PIAACMC
-// step at CSG_PREC_HIGH: the Fresnel column pass at 256 threads and one CTA
-// per SM (255 registers, no spills) issued at 32% of peak and took 10.1 ms
-// of an 18.4 ms step; at 128 threads x 3 CTAs (336 bytes of spills in the
-// transfer-function pass) 7.2 ms; 256 x 2 or 128 x 4 CTAs (128 registers,
-// more spills) 9.8 and 10.0 ms.
+// tiles hold 256 threads (4 columns at N = 1024, 64 KB of shared memory),
+// two CTAs per SM within 128 registers: the transfer-function pass fits
+// without spilling once the inverse transform's indices are opaque (see
+// k_fft_cols). Measured on the 152-field PIAACMC step at CSG_PREC_HIGH, the
+// Fresnel column pass per step: 10.1 ms at one 256-thread CTA per SM (255
+// registers), 7.2 ms at three 128-thread CTAs (168 registers, 336 bytes of
+// spills), 4.4 ms at two 256-thread CTAs with the opaque indices (5.1 ms at
+// four 128-thread CTAs).
 constexpr int default_cols(int n) { return n <= 512 ? 16 : (n == 1024 ? 8 : 4); }
 template <class T>
 constexpr int cols_for(int n) {
-  return std::is_same<T, dfl>::value ? (128 / (n / 16) > 0 ? 128 / (n / 16) : 1)
+  return std::is_same<T, dfl>::value ? (256 / (n / 16) > 0 ? 256 / (n / 16) : 1)
                                      : default_cols(n);
 }
 template <int N, int E, int COLS, class T = float>
@@ -454,7 +455,7 @@ struct ColCfg {
   static constexpr int TPT = N / E;
   static constexpr int THREADS = COLS * TPT;
   static constexpr int MIN_BLOCKS =
-      std::is_same<T, dfl>::value ? (THREADS <= 128 ? 3 : 1) : min_blocks_t<T>(E, THREADS);
+      std::is_same<T, dfl>::value ? (THREADS <= 128 ? 4 : 2) : min_blocks_t<T>(E, THREADS);
   static constexpr int PLANE = COLS * N;
   static constexpr size_t SMEM = (size_t)COLS * N * 8 * words_of<T>();
 };
@@ -783,7 +784,12 @@ __global__ void __launch_bounds__(ColCfg<N, E, COLS, T>::THREADS,
       }
     }
     __syncthreads();  // the forward transform's last reads precede the inverse's writes
-    fft_regs<N, E, true, A, LO>(xr, xi, re, im, t, u, tw);
+    // the inverse's indices pass through an opaque copy, so its address
+    // arithmetic is not computed ahead (and held) across the forward
+    // transform and the product
+    int t2 = t, u2 = u;
+    asm volatile("" : "+r"(t2), "+r"(u2));
+    fft_regs<N, E, true, A, LO>(xr, xi, re, im, t2, u2, tw);
   }
 #pragma unroll
   for (int s = 0; s < E; ++s)
